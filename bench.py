@@ -1,0 +1,403 @@
+"""Benchmark: BC1/BC3 + mips Mtexels/s on one GB300 (or N replicas).
+
+Workload (default): one 4096x4096 RGBA8 texture, sRGB colour at 8x scale with an independent
+alpha field, Kaiser mip chain (width 3, alpha 4, stretch 1) with sRGB->linear input and
+linear->sRGB output, AlphaMode_Transparency, BC3 Normal quality, 13 levels (22,369,621 texels,
+1,398,103 blocks). A step is one pass of the whole chain: filter every level and encode every
+block. Mtexels/s = encoded texels of all levels / step time.
+
+  value    : device time per step (CUDA events on the launching stream) with the texture resident
+             in HBM; L2 is flushed (256 MiB write) between steps, outside the timed events.
+  e2e      : the same step through the C ABI with host buffers (ntg_compress_chain_host from
+             pinned memory: BGRA8 in, blocks out, copies inside the timed region).
+  roofline : the dominant kernel (the BC3 cluster-fit encoder) against the FP32 issue rate of the
+             clocks seen, plus the mip filter against measured HBM bandwidth.
+  cpu_baseline : the oracle port (C restatement of the reference path) on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload c1|c0]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "nvidia-texture-tools_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "BC1/BC3+mips Mtexels/s, learned-proposal vs plain cluster fit at equal RMSE"
+UNIT = "Mtexels/s"
+FLUSH_BYTES = 256 << 20
+
+WORKLOADS = {
+    # name: (w, h, format, quality, filter, alpha_mode, in_xform, out_xform, description)
+    "c1": (4096, 4096, 4, 1, 2, 1, 2, 2,
+           "4096x4096 RGBA8 sRGB, Kaiser(w3,a4,s1) mips, transparency, BC3 Normal, 13 levels"),
+    "c0": (512, 512, 1, 1, 0, 0, 0, 0, "512x512 RGBA8 linear, box mips, BC1 Normal, 10 levels"),
+}
+
+# FP32 operations of one cluster-split evaluation of squish's WeightedClusterFit::Compress4
+# (src/nvtt/squish/weightedclusterfit.cpp:505-545), each multiply/add/min/max/floor/divide counted
+# once: w3 3, alpha2 4, beta2 4, alphabeta 2, factor 4, alphax 12, betax 3, a 12, b 12, clamp 12,
+# grid snap 24, e1 39, error 5, compare 1, running sums 4.
+OPS_PER_SPLIT = 141
+
+
+def splits(count: int) -> int:
+    return (count + 1) * (count + 2) * (count + 3) // 6
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.index, self.proc, self.lines = index, None, []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "of measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "of fallback"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl != "reference" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value, device=None):
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload_texture(name):
+    import ntg.synth as synth
+    w, h = WORKLOADS[name][:2]
+    if name == "c1":
+        return synth.texture_c1(w=w, h=h)
+    return synth.texture_c0(w=w, h=h)
+
+
+def chain_texels(w, h):
+    import ntg
+    return sum(lw * lh for lw, lh in ntg.chain_levels(w, h))
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU legs (oracle port): the reference's algorithm on the host cores
+
+def cpu_chain(oracle, bgra, spec, threads):
+    """Mips single-threaded (as the reference filters), encode on `threads` host threads."""
+    w, h, fmt, quality, filt, am, ix, ox = spec[:8]
+    width = {0: 0.5, 1: 1.0, 2: 3.0}[filt]
+    t0 = time.perf_counter()
+    _, enc = oracle.mip_chain(bgra, w, h, filt, width, 4.0, 1.0, 2, am, ix, ox, 2.2)
+    t1 = time.perf_counter()
+    for lv in enc:
+        lw, lh = lv.shape[2], lv.shape[1]
+        flat = lv.reshape(-1)
+        if fmt == 1:
+            oracle.bc1_image(flat, lw, lh, am, quality, threads=threads)
+        elif fmt == 4:
+            oracle.bc3_image(flat, lw, lh, am, quality, threads=threads)
+        else:
+            oracle.bc5_image(flat, lw, lh, quality, threads=threads)
+    t2 = time.perf_counter()
+    return t2 - t0, t1 - t0, t2 - t1
+
+
+def cpu_sample(name, bgra, threads):
+    """The bounded CPU sample: the full chain of the workload's texture (C1: ~10-30 s of CPU work)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    oracle = pyoracle.Oracle()
+    spec = WORKLOADS[name]
+    total, mips, enc = cpu_chain(oracle, bgra, spec, threads)
+    texels = chain_texels(spec[0], spec[1])
+    return {"value": texels / total / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"the full {name} chain ({texels} texels): mips on 1 thread {mips:.2f} s, "
+                      f"encode on {threads} threads {enc:.2f} s"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return 0
+    name = args.workload
+    spec = WORKLOADS[name]
+    bgra = workload_texture(name)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build_oracle()
+    oracle = pyoracle.Oracle()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_chain(oracle, bgra, spec, threads)
+    times = [cpu_chain(oracle, bgra, spec, threads)[0] for _ in range(args.steps)]
+    texels = chain_texels(spec[0], spec[1])
+    value = texels * len(times) / sum(times) / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": spec[8], "texels_per_step": texels},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"full {name} chain per step; the reference library itself is not built on "
+                                       "this host (its source tree is absent), its C restatement in oracle/ runs"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU leg
+
+def split_counts(ctx, levels_flat, spec, steps_table):
+    """Distinct RGB colours per block of every level after the BC3 quantiser (the squish split
+    count), for the algorithmic FLOP count of the encoder. Level 0 uses the 8-bit tables."""
+    import torch
+    import ntg
+    w, h = spec[0], spec[1]
+    total_splits, off = 0, 0
+    steps = torch.from_numpy(steps_table[1:].copy()).cuda()
+    for lw, lh in ntg.chain_levels(w, h):
+        n = lw * lh
+        lv = levels_flat[off: off + 4 * n].view(4, lh, lw)
+        off += 4 * n
+        rgb = lv[:3]
+        q = torch.searchsorted(steps, rgb.contiguous(), right=True).to(torch.int64)  # counts steps <= x
+        q = torch.where(torch.isnan(rgb), torch.zeros_like(q), q)
+        code = (q[0] << 16) | (q[1] << 8) | q[2]
+        bh, bw = (lh + 3) // 4, (lw + 3) // 4
+        # ColorBlock edge repetition for partial blocks: i % size within the block
+        by = torch.arange(bh * 4, device=code.device)
+        bx = torch.arange(bw * 4, device=code.device)
+        yy = (by // 4) * 4 + (by % 4) % torch.clamp(lh - (by // 4) * 4, max=4)
+        xx = (bx // 4) * 4 + (bx % 4) % torch.clamp(lw - (bx // 4) * 4, max=4)
+        blk = code[yy][:, xx].view(bh, 4, bw, 4).permute(0, 2, 1, 3).reshape(-1, 16)
+        s, _ = torch.sort(blk, dim=1)
+        distinct = 1 + (s[:, 1:] != s[:, :-1]).sum(dim=1)
+        cnt = distinct.to(torch.int64)
+        sp = (cnt + 1) * (cnt + 2) * (cnt + 3) // 6
+        sp = torch.where(cnt == 1, torch.zeros_like(sp), sp)  # single colour: table lookup, no fit
+        total_splits += int(sp.sum().item())
+    return total_splits
+
+
+def run_gpu(args):
+    import torch
+    import ntg
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    name = args.workload
+    spec = WORKLOADS[name]
+    w, h, fmt, quality, filt, am, ix, ox, desc = spec
+    ctx = ntg.Context(local)
+    opt = ntg.ChainOptions.make(format=fmt, quality=quality, filter=filt, alpha_mode=am, in_xform=ix,
+                                out_xform=ox, gamma=2.2)
+    bgra = workload_texture(name)
+    texels = chain_texels(w, h)
+    d_bgra = torch.from_numpy(bgra).cuda()
+    d_out = torch.empty(ntg.chain_bytes(w, h, opt), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    levels = len(ntg.chain_levels(w, h))
+    launches_per_step = (levels - 1) + 1 + (1 if filt == 0 and am == 0 else 0)
+
+    for _ in range(args.warmup):
+        ctx.compress_chain(d_bgra, w, h, opt, out=d_out)
+    torch.cuda.synchronize()
+
+    # device-resident timing: CUDA events around each step, L2 flushed in between
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    ctx.profile(True)  # phase events (mips / encode) recorded by the library on this stream
+    phase = []
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t_wall = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            ctx.compress_chain(d_bgra, w, h, opt, out=d_out)
+            ends[i].record(stream)
+            phase.append(ctx.profile_read())  # waits for this step's events; the next flush follows
+        torch.cuda.synchronize()
+        barrier(world)
+        wall = time.perf_counter() - t_wall
+    ctx.profile(False)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    mips_ms = sum(p[0] for p in phase) / len(phase)
+    enc_ms = sum(p[1] for p in phase) / len(phase)
+    dev_ms = max_over_ranks(world, sum(step_ms), torch.device("cuda"))
+    value = world * texels * args.steps / (dev_ms / 1000.0) / 1e6
+
+    # end to end through the host-buffer C-ABI call, pinned buffers
+    h_in = torch.from_numpy(bgra.reshape(-1)).pin_memory()
+    h_out = torch.empty(d_out.numel(), dtype=torch.uint8).pin_memory()
+    in_np, out_np = h_in.numpy(), h_out.numpy()
+    ctx.compress_chain_host(in_np, w, h, opt, out=out_np)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.compress_chain_host(in_np, w, h, opt, out=out_np)
+    e2e_s = max_over_ranks(world, time.perf_counter() - t0, torch.device("cuda"))
+    e2e_value = world * texels * args.steps / e2e_s / 1e6
+    same = bool(np.array_equal(out_np, d_out.cpu().numpy()))
+
+    line = None
+    if rank == 0:
+        # the filtered levels, for the encoder's operation count (outside any timing)
+        levels_flat = ctx.mip_chain(d_bgra, w, h, opt)
+        torch.cuda.synchronize()
+        chain_ms = dev_ms / args.steps
+        steps_table = ntg.host_transform_tables(ix, ox, 2.2)[3] if ox == 2 else None
+        peaks, peak_src = measured_peaks()
+        clocks = clk.summary()
+        roof = None
+        if fmt == 4 and steps_table is not None:
+            nsplits = split_counts(ctx, levels_flat, spec, steps_table)
+            ops = nsplits * OPS_PER_SPLIT
+            sm_mhz = clocks["sm_mhz"] or 2070.0
+            peak_tops = 152 * 128 * sm_mhz * 1e6 / 1e12  # one FP32 op per lane per clock (no FMA pairing)
+            achieved = ops / (enc_ms / 1000.0) / 1e12
+            roof = {"bound": "fp32", "achieved": achieved, "peak": peak_tops, "unit": "TFLOP/s",
+                    "frac": achieved / peak_tops, "traffic": None,
+                    "kernel": "k_bc3 (squish weighted cluster fit + DXT5A)",
+                    "note": f"peak = 152 SMs x 128 FP32 lanes x median SM clock {sm_mhz:.0f} MHz (derived from the "
+                            f"clocks seen; the file of measured peaks has no FP32 figure); {nsplits} splits x "
+                            f"{OPS_PER_SPLIT} ops; encoder phase {enc_ms:.3f} ms (one launch over all levels, "
+                            f"CUDA events on the launching stream, mean of the timed steps)"}
+        # mip filter against HBM: algorithmic bytes = read level l-1 + write level l (FP32 planar),
+        # level 0 read as BGRA8, plus the BGRA8 quantised copy each level writes for the encoder
+        mip_bytes = 0
+        lv = ntg.chain_levels(w, h)
+        for i in range(1, len(lv)):
+            src = lv[i - 1][0] * lv[i - 1][1] * (4 if i == 1 else 16)
+            dst = lv[i][0] * lv[i][1] * (16 + (4 if fmt != 1 else 0))
+            mip_bytes += src + dst
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        mip_gbs = mip_bytes / (mips_ms / 1000.0) / 1e9
+        roof_hbm = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
+                    "traffic": None, "kernel": "k_poly (fused separable Kaiser, all levels)",
+                    "algorithmic_bytes": mip_bytes, "ms": mips_ms, "peak_source": peak_src}
+        cpu = None
+        if not args.no_cpu and world == 1:
+            try:
+                cpu = cpu_sample(name, bgra, os.cpu_count() or 1)
+            except Exception as e:  # reported, not fatal
+                cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": desc, "texels_per_step": texels, "blocks_per_step": ntg.chain_bytes(w, h, opt) // 16
+                           if fmt != 1 else ntg.chain_bytes(w, h, opt) // 8, "l2": "flushed (256 MiB write) between steps",
+                           "method": "plain (non-learned) cluster fit", "replicas": world},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(bgra.nbytes),
+                        "d2h_bytes_per_step": int(d_out.numel()), "matches_device_path": same},
+                "gpu_launches": launches_per_step * args.steps,
+                "clocks": clocks, "roofline": roof, "roofline_mips": roof_hbm,
+                "split_ms": {"mips": mips_ms, "encode": enc_ms, "chain": chain_ms},
+                "wall_s_timed": wall, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ntg", choices=["ntg", "reference"])
+    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warmup raised to 3")
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

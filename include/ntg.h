@@ -1,0 +1,165 @@
+/* ntg.h -- C ABI of the GB300 (sm_103a) texture hot path.
+ *
+ * Drop-in boundary for NVTT 2.1.2's mip-chain + BC1/BC3/BC5 path. Plain C types only: device
+ * pointers are caller-owned CUDA allocations, host pointers are plain memory, every call takes an
+ * explicit CUDA stream (cudaStream_t passed as void *; NULL = the legacy default stream) and
+ * returns an int status:
+ *     NTG_OK (0), or an nvtt::Error value (src/nvtt/nvtt.h:345-364):
+ *     1 InvalidInput, 2 UnsupportedFeature, 3 CudaError, 6 UnsupportedOutputFormat;
+ *     NTG_ERROR_UNKNOWN (100) stands in for nvtt's Error_Unknown (0).
+ * ntg_last_error_string() describes the last failure on the calling thread.
+ * Calls that take device pointers only enqueue work; they never synchronise. Calls that take host
+ * pointers (the *_host variants) copy in, run and copy out on the given stream and return after
+ * it has drained.
+ *
+ * Enum values are nvtt's own: Format (src/nvtt/nvtt.h:77-129), Quality (:145-151), WrapMode
+ * (:217-222), MipmapFilter (:253-258), AlphaMode (:279-284).
+ */
+#ifndef NTG_H
+#define NTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NTG_VERSION 20102      /* the NVTT release whose behaviour this reproduces */
+
+#define NTG_OK 0
+#define NTG_ERROR_INVALID_INPUT 1
+#define NTG_ERROR_UNSUPPORTED_FEATURE 2
+#define NTG_ERROR_CUDA 3
+#define NTG_ERROR_UNSUPPORTED_OUTPUT_FORMAT 6
+#define NTG_ERROR_UNKNOWN 100
+
+/* nvtt::Format subset */
+#define NTG_FORMAT_BC1 1   /* Format_DXT1 */
+#define NTG_FORMAT_BC3 4   /* Format_DXT5 */
+#define NTG_FORMAT_BC5 7   /* Format_BC5 */
+/* nvtt::Quality */
+#define NTG_QUALITY_FASTEST 0
+#define NTG_QUALITY_NORMAL 1
+#define NTG_QUALITY_PRODUCTION 2
+#define NTG_QUALITY_HIGHEST 3
+/* nvtt::WrapMode */
+#define NTG_WRAP_CLAMP 0
+#define NTG_WRAP_REPEAT 1
+#define NTG_WRAP_MIRROR 2
+/* nvtt::MipmapFilter */
+#define NTG_FILTER_BOX 0
+#define NTG_FILTER_TRIANGLE 1
+#define NTG_FILTER_KAISER 2
+/* nvtt::AlphaMode */
+#define NTG_ALPHA_NONE 0
+#define NTG_ALPHA_TRANSPARENCY 1
+/* colour transforms applied around the mip chain */
+#define NTG_XFORM_NONE 0   /* linear data */
+#define NTG_XFORM_GAMMA 1  /* Surface::toLinear(gamma) / toGamma(gamma) (src/nvtt/Surface.cpp:1470-1488) */
+#define NTG_XFORM_SRGB 2   /* Surface::toLinearFromSrgb / toSrgb (src/nvtt/Surface.cpp:1512-1592) */
+
+typedef struct ntg_context ntg_context;
+
+/* Per-device state: constant tables, a grow-only scratch workspace and staging buffers.
+ * Replaces the reference's CudaContext (src/nvtt/Context.cpp:81-98). */
+int ntg_create(int device, ntg_context **out);
+int ntg_destroy(ntg_context *ctx);
+const char *ntg_last_error_string(void);
+int ntg_version(void);
+
+/* ---- single steps on device buffers ---- */
+
+/* Surface::setImage(InputFormat_BGRA_8UB) (src/nvtt/Surface.cpp:728-760) followed by the input
+ * transform of RGB. bgra: w*h BGRA8 texels. rgba: 4*w*h floats, planar. */
+int ntg_set_image_bgra8(ntg_context *ctx, const void *d_bgra, int w, int h, int in_xform, float gamma,
+                        float *d_rgba, void *stream);
+
+/* Surface::buildNextMipmap (src/nvtt/Surface.cpp:1344-1406): one level down from a planar FP32
+ * level to max(1, w/2) x max(1, h/2). params = {kaiser alpha, kaiser stretch} (ignored otherwise).
+ * weighted != 0 selects the alpha-weighted kernels of FloatImage::applyKernelX/Y
+ * (src/nvimage/FloatImage.cpp:1212-1281), which the reference defines but does not call. */
+int ntg_mip_level(ntg_context *ctx, const float *d_src, int w, int h, float *d_dst, int filter, float width,
+                  const float *params, int wrap, int alpha_mode, int weighted, void *stream);
+
+/* CompressorInterface::compress (src/nvtt/Compressor.h:34-38) for one planar FP32 level, as
+ * CompressorDXT1 / CompressorDXT5 / FastCompressorBC5 etc. encode it (chooseCpuCompressor,
+ * src/nvtt/Context.cpp:1038-1163). out_xform / gamma apply the output transform to RGB first
+ * (Compressor::Private::compress's toGamma step, src/nvtt/Context.cpp:283-289); cw = colour
+ * weights (CompressionOptions::setColorWeights). Output: ((w+3)/4)*((h+3)/4) blocks of 8 (BC1)
+ * or 16 (BC3, BC5) bytes in row-major block order. */
+int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,
+               int out_xform, float gamma, const float *cw, void *d_blocks, void *stream);
+
+/* ---- whole chains ---- */
+
+typedef struct ntg_chain_options {
+    int format;          /* NTG_FORMAT_* */
+    int quality;         /* NTG_QUALITY_* */
+    int filter;          /* NTG_FILTER_* */
+    float filter_width;  /* 0 = nvtt default for the filter (box 0.5, triangle 1, kaiser 3) */
+    float params[2];     /* kaiser alpha, stretch (defaults 4, 1 when filter_width is 0) */
+    int wrap;            /* NTG_WRAP_* */
+    int alpha_mode;      /* NTG_ALPHA_* */
+    int in_xform;        /* NTG_XFORM_* applied after setImage */
+    int out_xform;       /* NTG_XFORM_* applied to a copy of each level before encoding */
+    float gamma;         /* for NTG_XFORM_GAMMA */
+    int max_levels;      /* 0 = full chain down to 1x1 */
+    int weighted;        /* alpha-weighted polyphase kernels (opt-in) */
+    float cw[3];         /* colour weights; zeros mean 1,1,1 */
+} ntg_chain_options;
+
+/* Number of levels and encoded bytes of a chain (nvtt::countMipmaps, src/nvtt/Surface.cpp:181). */
+int ntg_chain_levels(int w, int h, int max_levels);
+size_t ntg_chain_bytes(int w, int h, const ntg_chain_options *opt);
+
+/* The Surface-API loop of the reference (setImage -> input transform -> per level: copy, output
+ * transform, Compressor::compress -> buildNextMipmap), src/nvtt/tests/imperativeapi.cpp:32-86 and
+ * Compressor::Private::compress (src/nvtt/Context.cpp:217-346), for one BGRA8 image. All levels'
+ * blocks are written back to back, largest level first. */
+int ntg_compress_chain(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
+                       void *d_blocks, void *stream);
+/* Same from host memory: copies the image in, encodes, copies the blocks out, drains the stream. */
+int ntg_compress_chain_host(ntg_context *ctx, const void *h_bgra, int w, int h, const ntg_chain_options *opt,
+                            void *h_blocks, void *stream);
+
+/* Mip chain only: writes every level, planar FP32 (linear, before the output transform),
+ * back to back into d_levels (sum of 4*w_l*h_l floats). */
+int ntg_mip_chain(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
+                  float *d_levels, void *stream);
+
+/* Phase timing of chain calls: when enabled, ntg_compress_chain records CUDA events on its stream
+ * around the mip phase and the encode phase; ntg_profile_read waits for the last call's events and
+ * returns the two durations in milliseconds. */
+int ntg_profile_enable(ntg_context *ctx, int enable);
+int ntg_profile_read(ntg_context *ctx, float *mips_ms, float *encode_ms);
+
+/* ---- decode and error ---- */
+
+/* Surface::setImage2D(format, Decoder_D3D10, ...) (src/nvtt/Surface.cpp:908-1116): blocks to a
+ * planar FP32 image of w x h. */
+int ntg_decode(ntg_context *ctx, int format, const void *d_blocks, int w, int h, float *d_rgba, void *stream);
+/* nv::rmsColorError / rmsAlphaError (src/nvimage/ErrorMetric.cpp:13-71) sums in double:
+ * d_sums[0] = colour squared error (alpha-weighted when alpha_mode is Transparency),
+ * d_sums[1] = alpha squared error. rms = sqrt(sum / (w*h)). */
+int ntg_error_sums(ntg_context *ctx, const float *d_ref, const float *d_img, int w, int h, int alpha_mode,
+                   double *d_sums, void *stream);
+
+/* ---- host-side tables (no GPU needed) ---- */
+
+/* PolyphaseKernel weights (src/nvimage/Filter.cpp:520-566) and the window offsets
+ * FloatImage::applyKernelX/Y start from (src/nvimage/FloatImage.cpp:1124-1131), as the kernels
+ * receive them. Returns the window size; fills weights (dst_len * window) and lefts (dst_len)
+ * when capacity allows. */
+int ntg_host_polyphase(int filter, float width, const float *params, int src_len, int dst_len, float *weights,
+                       int *lefts, int capacity);
+/* The 8-bit transform tables of a chain: lut_in[256] = input transform of v/255; lut_composed[256]
+ * = output(input(v/255)); lut8[512] = ColorBlock quantisation of lut_composed, then of v/255
+ * (alpha); srgb_steps[256] = smallest float whose toSrgb code reaches k. Any pointer may be NULL. */
+int ntg_host_transform_tables(int in_xform, int out_xform, float gamma, float *lut_in, float *lut_composed,
+                              unsigned char *lut8, float *srgb_steps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NTG_H */

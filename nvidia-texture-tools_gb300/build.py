@@ -1,0 +1,79 @@
+"""Builds libntg.so, the GB300 texture path (CUDA kernels for sm_103a + the C ABI of include/ntg.h).
+
+Compiles in-tree into nvidia-texture-tools_gb300/_build/ with nvcc (kernels) and g++ (host code),
+translation units in parallel, one -gencode. Kernels use --fmad=false and host code
+-ffp-contract=off: results must match the reference's CPU arithmetic bit for bit.
+
+    python nvidia-texture-tools_gb300/build.py          # incremental
+    python nvidia-texture-tools_gb300/build.py --force  # rebuild everything
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libntg.so")
+CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA, "bin", "nvcc") if os.path.exists(os.path.join(CUDA, "bin", "nvcc")) else "nvcc"
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+CU_SOURCES = ["ntg_bc1.cu", "ntg_bc3.cu", "ntg_mip.cu", "ntg_decode.cu"]
+CPP_SOURCES = ["ntg_api.cpp", "ntg_host_tables.cpp"]
+HEADERS = ["ntg_device.cuh", "ntg_internal.h", "ntg_host_tables.h"]
+
+NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
+             "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + os.path.join(CUDA, "include")]
+
+
+def _newer(src_paths, target):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(p) > t for p in src_paths)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    headers = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "ntg.h")]
+    jobs, objs = [], []
+    for s in CU_SOURCES:
+        src, obj = os.path.join(CSRC, s), os.path.join(OUT, s + ".o")
+        objs.append(obj)
+        if force or _newer([src] + headers, obj):
+            jobs.append([NVCC] + NVCC_FLAGS + ["-c", src, "-o", obj])
+    cxx = shutil.which("g++") or "g++"
+    for s in CPP_SOURCES:
+        src, obj = os.path.join(CSRC, s), os.path.join(OUT, s + ".o")
+        objs.append(obj)
+        if force or _newer([src] + headers, obj):
+            jobs.append([cxx] + CXX_FLAGS + ["-c", src, "-o", obj])
+    if jobs:
+        with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+            for out in ex.map(_run, jobs):
+                if verbose and out.strip():
+                    print(out)
+    if force or jobs or _newer(objs, LIB):
+        _run([cxx, "-shared", "-o", LIB] + objs +
+             ["-L" + os.path.join(CUDA, "lib64"), "-lcudart_static", "-lrt", "-lpthread", "-ldl",
+              "-Wl,--no-undefined"])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

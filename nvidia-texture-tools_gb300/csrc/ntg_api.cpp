@@ -1,0 +1,633 @@
+// C ABI of the GB300 texture path (include/ntg.h): contexts, table caches, chain planning and the
+// launch sequences. Host code only; kernels live in the .cu translation units.
+#include "ntg.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "ntg_host_tables.h"
+#include "ntg_internal.h"
+
+using namespace ntg;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string &msg) {
+    g_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(NTG_ERROR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Maps a launcher status (ntg_internal.h) to an nvtt error code with a message.
+int launched(int status, const char *what) {
+    if (status == 0) return NTG_OK;
+    if (status >= kLaunchErrorBase) return cuda_fail((cudaError_t)(status - kLaunchErrorBase), what);
+    return fail(status, what);
+}
+
+#define NTG_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+#define NTG_TRY(call)                         \
+    do {                                      \
+        int r_ = (call);                      \
+        if (r_ != NTG_OK) {                   \
+            if (g_error.empty()) g_error = #call; \
+            return r_;                        \
+        }                                     \
+    } while (0)
+
+inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+struct Level { int w, h; };
+
+std::vector<Level> chain_levels(int w, int h, int max_levels) {
+    std::vector<Level> v;
+    for (;;) {
+        v.push_back({w, h});
+        if ((max_levels > 0 && (int)v.size() >= max_levels) || (w == 1 && h == 1)) break;
+        w = std::max(1, w / 2);
+        h = std::max(1, h / 2);
+    }
+    return v;
+}
+
+int block_bytes(int format) { return format == NTG_FORMAT_BC1 ? 8 : 16; }
+long long blocks_of(int w, int h) { return (long long)((w + 3) / 4) * ((h + 3) / 4); }
+
+// Filter defaults of Surface::buildNextMipmap (getDefaultFilterWidthAndParams,
+// src/nvtt/Surface.cpp:1121-1141).
+void filter_defaults(const ntg_chain_options &o, float &width, float p[2]) {
+    width = o.filter_width;
+    p[0] = o.params[0];
+    p[1] = o.params[1];
+    if (width > 0) return;
+    if (o.filter == NTG_FILTER_BOX) width = 0.5f;
+    else if (o.filter == NTG_FILTER_TRIANGLE) width = 1.0f;
+    else { width = 3.0f; p[0] = 4.0f; p[1] = 1.0f; }
+}
+
+// True when buildNextMipmap takes FloatImage::fastDownSample (src/nvtt/Surface.cpp:1382-1386).
+bool uses_fast_box(const ntg_chain_options &o, float width) {
+    return o.alpha_mode != NTG_ALPHA_TRANSPARENCY && o.filter == NTG_FILTER_BOX && width == 0.5f;
+}
+
+// Device copy of one axis' polyphase table.
+struct AxisTable {
+    int ws = 0;
+    float *d_w = nullptr;
+    int *d_left = nullptr;
+    std::vector<int> left;
+};
+
+// Device copy of one 256-entry table set for an (in, out, gamma) transform combination.
+struct XformTables {
+    float *d_in = nullptr;       // input transform of 8-bit values
+    float *d_comp = nullptr;     // output(input(v/255)) for the BC1 level-0 path
+    uint8_t *d_comp8 = nullptr;  // quantised composition (RGB) + alpha quantiser, 512 bytes
+    float *d_steps = nullptr;    // sRGB quantiser steps
+};
+
+}  // namespace
+
+struct ntg_context {
+    int device = 0;
+    HostTables tables;
+    std::mutex mu;
+    std::map<std::tuple<int, float, float, float, int, int>, AxisTable> axes;
+    std::map<std::tuple<int, int, float>, XformTables> xforms;
+    std::vector<void *> owned;  // every cudaMalloc of the caches
+    uint8_t *ws = nullptr;      // grow-only workspace (stream-ordered)
+    size_t ws_bytes = 0;
+    EncJob *d_jobs = nullptr;   // job list of chain encodes
+    int d_jobs_cap = 0;
+    bool profile = false;       // record phase events in chain calls
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+
+    ~ntg_context() {
+        cudaSetDevice(device);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+        for (void *p : owned) cudaFree(p);
+        if (ws) cudaFree(ws);
+        if (d_jobs) cudaFree(d_jobs);
+    }
+
+    int alloc(void **p, size_t bytes) {
+        NTG_CUDA(cudaMalloc(p, bytes));
+        owned.push_back(*p);
+        return NTG_OK;
+    }
+
+    int workspace(size_t bytes, cudaStream_t s, uint8_t **out) {
+        if (bytes > ws_bytes) {
+            if (ws) NTG_CUDA(cudaFreeAsync(ws, s));
+            ws = nullptr;
+            ws_bytes = 0;
+            const size_t want = std::max(bytes, ws_bytes + ws_bytes / 4);
+            NTG_CUDA(cudaMallocAsync((void **)&ws, want, s));
+            ws_bytes = want;
+        }
+        *out = ws;
+        return NTG_OK;
+    }
+
+    const AxisTable *axis(int filter, float width, float p0, float p1, int src, int dst) {
+        auto key = std::make_tuple(filter, width, p0, p1, src, dst);
+        auto it = axes.find(key);
+        if (it != axes.end()) return &it->second;
+        AxisTable t;
+        t.ws = polyphase_window(width, src, dst);
+        std::vector<float> w((size_t)t.ws * dst);
+        t.left.resize(dst);
+        build_polyphase(filter, width, p0, p1, src, dst, w.data(), t.left.data());
+        if (alloc((void **)&t.d_w, w.size() * sizeof(float)) != NTG_OK) return nullptr;
+        if (alloc((void **)&t.d_left, t.left.size() * sizeof(int)) != NTG_OK) return nullptr;
+        if (cudaMemcpy(t.d_w, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+        if (cudaMemcpy(t.d_left, t.left.data(), t.left.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+            return nullptr;
+        return &(axes[key] = t);
+    }
+
+    const XformTables *xform(int in_x, int out_x, float gamma) {
+        auto key = std::make_tuple(in_x, out_x, gamma);
+        auto it = xforms.find(key);
+        if (it != xforms.end()) return &it->second;
+        XformTables t;
+        float lin[256], comp[256], steps[256];
+        uint8_t comp8[512];
+        build_input_lut(in_x, gamma, tables, lin);
+        build_composed_lut(in_x, out_x, gamma, tables, comp);
+        build_composed_lut8(in_x, out_x, gamma, tables, comp8);
+        build_srgb_steps(steps);
+        if (alloc((void **)&t.d_in, sizeof lin) || alloc((void **)&t.d_comp, sizeof comp) ||
+            alloc((void **)&t.d_comp8, sizeof comp8) || alloc((void **)&t.d_steps, sizeof steps))
+            return nullptr;
+        if (cudaMemcpy(t.d_in, lin, sizeof lin, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(t.d_comp, comp, sizeof comp, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(t.d_comp8, comp8, sizeof comp8, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(t.d_steps, steps, sizeof steps, cudaMemcpyHostToDevice) != cudaSuccess)
+            return nullptr;
+        return &(xforms[key] = t);
+    }
+};
+
+namespace {
+
+// Largest source window (columns) any PTW-wide run of outputs of this axis can touch.
+int max_window(const AxisTable &t, int tile) {
+    int m = 0;
+    const int n = (int)t.left.size();
+    for (int i0 = 0; i0 < n; i0 += tile) {
+        const int i1 = std::min(n, i0 + tile) - 1;
+        m = std::max(m, t.left[i1] + t.ws - t.left[i0]);
+    }
+    return m;
+}
+
+int check_opts(const ntg_chain_options *opt) {
+    if (!opt) return fail(NTG_ERROR_INVALID_INPUT, "null options");
+    if (opt->format != NTG_FORMAT_BC1 && opt->format != NTG_FORMAT_BC3 && opt->format != NTG_FORMAT_BC5)
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "format not supported (BC1, BC3, BC5)");
+    if (opt->quality < 0 || opt->quality > 3) return fail(NTG_ERROR_INVALID_INPUT, "bad quality");
+    if (opt->filter < 0 || opt->filter > 2) return fail(NTG_ERROR_INVALID_INPUT, "bad filter");
+    if (opt->wrap < 0 || opt->wrap > 2) return fail(NTG_ERROR_INVALID_INPUT, "bad wrap mode");
+    if (opt->in_xform < 0 || opt->in_xform > 2 || opt->out_xform < 0 || opt->out_xform > 2)
+        return fail(NTG_ERROR_INVALID_INPUT, "bad colour transform");
+    return NTG_OK;
+}
+
+void colour_weights(const ntg_chain_options &o, float cw[3]) {
+    if (o.cw[0] == 0 && o.cw[1] == 0 && o.cw[2] == 0) { cw[0] = cw[1] = cw[2] = 1.0f; return; }
+    cw[0] = o.cw[0]; cw[1] = o.cw[1]; cw[2] = o.cw[2];
+}
+
+// Workspace plan of one chain.
+struct ChainPlan {
+    std::vector<Level> lv;
+    std::vector<size_t> f_off;   // float level offsets (bytes) in the workspace, SIZE_MAX = none
+    std::vector<size_t> q_off;   // quantised BGRA8 level offsets, SIZE_MAX = none
+    size_t bytes = 0;
+    bool fast_box = false;
+    float width = 0, p[2] = {0, 0};
+};
+
+const size_t NONE = (size_t)-1;
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+ChainPlan plan_chain(int w, int h, const ntg_chain_options &o, bool keep_level0_float) {
+    ChainPlan P;
+    P.lv = chain_levels(w, h, o.max_levels);
+    filter_defaults(o, P.width, P.p);
+    P.fast_box = uses_fast_box(o, P.width);
+    const bool need_q = o.format != NTG_FORMAT_BC1;
+    size_t off = 0;
+    for (size_t l = 0; l < P.lv.size(); l++) {
+        const size_t n = (size_t)P.lv[l].w * P.lv[l].h;
+        if (l > 0 || P.fast_box || keep_level0_float) { P.f_off.push_back(off); off = align256(off + 16 * n); }
+        else P.f_off.push_back(NONE);
+        if (l > 0 && need_q) { P.q_off.push_back(off); off = align256(off + 4 * n); }
+        else P.q_off.push_back(NONE);
+    }
+    P.bytes = off;
+    return P;
+}
+
+// Builds the levels of a chain into the workspace. Level 0 comes straight from the BGRA8 input:
+// the fast box path materialises it as FP32, the polyphase path reads the bytes through the input
+// transform table.
+int build_levels(ntg_context *ctx, const ChainPlan &P, const uint32_t *d_bgra, const ntg_chain_options &o,
+                 const XformTables *xt, uint8_t *ws, cudaStream_t s) {
+    const int L = (int)P.lv.size();
+    if (P.f_off[0] != NONE) {
+        NTG_TRY(launched(launch_set_image(d_bgra, (size_t)P.lv[0].w * P.lv[0].h, xt->d_in, (float *)(ws + P.f_off[0]), s), "set image"));
+    }
+    for (int l = 1; l < L; l++) {
+        const Level &S = P.lv[l - 1], &D = P.lv[l];
+        float *dst = (float *)(ws + P.f_off[l]);
+        uint32_t *q = P.q_off[l] != NONE ? (uint32_t *)(ws + P.q_off[l]) : nullptr;
+        if (P.fast_box) {
+            NTG_TRY(launched(launch_fast_down((const float *)(ws + P.f_off[l - 1]), S.w, S.h, dst, q, o.out_xform, xt->d_steps, s), "box downsample"));
+            continue;
+        }
+        const AxisTable *ax = ctx->axis(o.filter, P.width, P.p[0], P.p[1], S.w, D.w);
+        const AxisTable *ay = ctx->axis(o.filter, P.width, P.p[0], P.p[1], S.h, D.h);
+        if (!ax || !ay) return fail(NTG_ERROR_CUDA, "polyphase table upload failed");
+        PolyArgs a;
+        a.src = P.f_off[l - 1] != NONE ? (const float *)(ws + P.f_off[l - 1]) : nullptr;
+        a.bgra8 = a.src ? nullptr : d_bgra;
+        a.lut = xt->d_in;
+        a.W = S.w; a.H = S.h; a.w = D.w; a.h = D.h;
+        a.wsx = ax->ws; a.wsy = ay->ws;
+        a.kx = ax->d_w; a.ky = ay->d_w; a.lx = ax->d_left; a.ly = ay->d_left;
+        a.wrap = o.wrap;
+        a.dst = dst;
+        a.q_out = q;
+        a.xform = o.out_xform;
+        a.steps = xt->d_steps;
+        a.weighted = o.weighted != 0;
+        a.rx_max = max_window(*ax, poly_tile_w());
+        a.ry_max = max_window(*ay, poly_tile_h());
+        NTG_TRY(launched(launch_poly(a, s), "polyphase filter (windows wider than 32 taps are not supported)"));
+    }
+    return NTG_OK;
+}
+
+int upload_jobs(ntg_context *ctx, const std::vector<EncJob> &jobs, cudaStream_t s) {
+    if ((int)jobs.size() > ctx->d_jobs_cap) {
+        if (ctx->d_jobs) NTG_CUDA(cudaFreeAsync(ctx->d_jobs, s));
+        ctx->d_jobs = nullptr;
+        NTG_CUDA(cudaMallocAsync((void **)&ctx->d_jobs, jobs.size() * sizeof(EncJob), s));
+        ctx->d_jobs_cap = (int)jobs.size();
+    }
+    // pageable source: the copy is staged before the call returns, so `jobs` may go away
+    NTG_CUDA(cudaMemcpyAsync(ctx->d_jobs, jobs.data(), jobs.size() * sizeof(EncJob), cudaMemcpyHostToDevice, s));
+    return NTG_OK;
+}
+
+int launch_encode(int format, const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s) {
+    int r = format == NTG_FORMAT_BC1 ? launch_bc1(d_jobs, njobs, nblocks, quality, s)
+            : format == NTG_FORMAT_BC3 ? launch_bc3(d_jobs, njobs, nblocks, quality, s)
+                                       : launch_bc5(d_jobs, njobs, nblocks, quality, s);
+    return launched(r, "encoder launch");
+}
+
+// Encode jobs of a chain: level 0 from the input bytes (through the composed transform tables),
+// the other levels from the workspace.
+void chain_jobs(const ChainPlan &P, const uint32_t *d_bgra, const ntg_chain_options &o, const XformTables *xt,
+                uint8_t *ws, uint8_t *d_blocks, std::vector<EncJob> &jobs, long long &nblocks) {
+    float cw[3];
+    colour_weights(o, cw);
+    size_t out_off = 0;
+    for (size_t l = 0; l < P.lv.size(); l++) {
+        const Level &L = P.lv[l];
+        EncJob j;
+        std::memset(&j, 0, sizeof j);
+        j.w = L.w; j.h = L.h; j.bw = (L.w + 3) / 4;
+        j.alpha_mode = o.alpha_mode;
+        j.out_xform = o.out_xform;
+        std::memcpy(j.cw, cw, sizeof cw);
+        j.out = d_blocks + out_off;
+        j.first_block = nblocks;
+        if (o.format == NTG_FORMAT_BC1) {
+            if (l == 0) { j.bgra = d_bgra; j.lut_f = xt->d_comp; }
+            else j.rgba = (const float *)(ws + P.f_off[l]);
+        } else {
+            if (l == 0) { j.bgra = d_bgra; j.lut8 = xt->d_comp8; }
+            else j.bgra = (const uint32_t *)(ws + P.q_off[l]);
+        }
+        jobs.push_back(j);
+        nblocks += blocks_of(L.w, L.h);
+        out_off += (size_t)block_bytes(o.format) * blocks_of(L.w, L.h);
+    }
+}
+
+// Surface::toLinear/toGamma return early for gamma == 1 (nv::equal, src/nvtt/Surface.cpp:1470-1488).
+ntg_chain_options normalized(const ntg_chain_options &o) {
+    ntg_chain_options n = o;
+    const float g = o.gamma;
+    const bool unit = std::fabs(g - 1.0f) <= 0.0001f * std::max(1.0f, std::max(std::fabs(g), 1.0f));
+    if (unit && n.in_xform == NTG_XFORM_GAMMA) n.in_xform = NTG_XFORM_NONE;
+    if (unit && n.out_xform == NTG_XFORM_GAMMA) n.out_xform = NTG_XFORM_NONE;
+    return n;
+}
+
+int ensure_device(ntg_context *ctx) {
+    int cur = -1;
+    NTG_CUDA(cudaGetDevice(&cur));
+    if (cur != ctx->device) NTG_CUDA(cudaSetDevice(ctx->device));
+    return NTG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ntg_version(void) { return NTG_VERSION; }
+
+const char *ntg_last_error_string(void) { return g_error.c_str(); }
+
+int ntg_create(int device, ntg_context **out) {
+    g_error.clear();
+    if (!out) return fail(NTG_ERROR_INVALID_INPUT, "null output");
+    int count = 0;
+    NTG_CUDA(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count) return fail(NTG_ERROR_INVALID_INPUT, "no such CUDA device");
+    NTG_CUDA(cudaSetDevice(device));
+    std::unique_ptr<ntg_context> ctx(new ntg_context);
+    ctx->device = device;
+    build_device_tables(ctx->tables);
+    NTG_TRY(upload_tables_bc1(ctx->tables));
+    NTG_TRY(upload_tables_bc3(ctx->tables));
+    NTG_TRY(upload_tables_mip(ctx->tables));
+    NTG_TRY(upload_tables_decode(ctx->tables));
+    *out = ctx.release();
+    return NTG_OK;
+}
+
+int ntg_destroy(ntg_context *ctx) {
+    if (!ctx) return NTG_OK;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    delete ctx;
+    return NTG_OK;
+}
+
+int ntg_chain_levels(int w, int h, int max_levels) {
+    if (w <= 0 || h <= 0) return 0;
+    return (int)chain_levels(w, h, max_levels).size();
+}
+
+size_t ntg_chain_bytes(int w, int h, const ntg_chain_options *opt) {
+    if (!opt || w <= 0 || h <= 0) return 0;
+    size_t b = 0;
+    for (const Level &L : chain_levels(w, h, opt->max_levels)) b += (size_t)block_bytes(opt->format) * blocks_of(L.w, L.h);
+    return b;
+}
+
+int ntg_set_image_bgra8(ntg_context *ctx, const void *d_bgra, int w, int h, int in_xform, float gamma, float *d_rgba,
+                        void *stream) {
+    g_error.clear();
+    if (!ctx || !d_bgra || !d_rgba || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    const XformTables *xt = ctx->xform(in_xform, NTG_XFORM_NONE, gamma);
+    if (!xt) return fail(NTG_ERROR_CUDA, "table upload failed");
+    return launched(launch_set_image((const uint32_t *)d_bgra, (size_t)w * h, xt->d_in, d_rgba, S(stream)), "set image");
+}
+
+int ntg_mip_level(ntg_context *ctx, const float *d_src, int w, int h, float *d_dst, int filter, float width,
+                  const float *params, int wrap, int alpha_mode, int weighted, void *stream) {
+    g_error.clear();
+    if (!ctx || !d_src || !d_dst || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    if (w == 1 && h == 1) return fail(NTG_ERROR_INVALID_INPUT, "no smaller level (canMakeNextMipmap)");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    ntg_chain_options o;
+    std::memset(&o, 0, sizeof o);
+    o.filter = filter; o.filter_width = width;
+    if (params) { o.params[0] = params[0]; o.params[1] = params[1]; }
+    o.wrap = wrap; o.alpha_mode = alpha_mode; o.weighted = weighted;
+    float fw, p[2];
+    filter_defaults(o, fw, p);
+    const int dw = std::max(1, w / 2), dh = std::max(1, h / 2);
+    if (uses_fast_box(o, fw) && !weighted)
+        return launched(launch_fast_down(d_src, w, h, d_dst, nullptr, 0, nullptr, S(stream)), "box downsample");
+    const AxisTable *ax = ctx->axis(filter, fw, p[0], p[1], w, dw);
+    const AxisTable *ay = ctx->axis(filter, fw, p[0], p[1], h, dh);
+    if (!ax || !ay) return fail(NTG_ERROR_CUDA, "polyphase table upload failed");
+    PolyArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.src = d_src; a.W = w; a.H = h; a.w = dw; a.h = dh;
+    a.wsx = ax->ws; a.wsy = ay->ws; a.kx = ax->d_w; a.ky = ay->d_w; a.lx = ax->d_left; a.ly = ay->d_left;
+    a.wrap = wrap; a.dst = d_dst; a.weighted = weighted != 0;
+    a.rx_max = max_window(*ax, poly_tile_w());
+    a.ry_max = max_window(*ay, poly_tile_h());
+    return launched(launch_poly(a, S(stream)), "polyphase filter (windows wider than 32 taps are not supported)");
+}
+
+int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,
+               int out_xform, float gamma, const float *cw, void *d_blocks, void *stream) {
+    g_error.clear();
+    if (!ctx || !d_rgba || !d_blocks || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    ntg_chain_options o0;
+    std::memset(&o0, 0, sizeof o0);
+    o0.format = format; o0.quality = quality; o0.out_xform = out_xform; o0.gamma = gamma; o0.alpha_mode = alpha_mode;
+    NTG_TRY(check_opts(&o0));
+    const ntg_chain_options o = normalized(o0);
+    out_xform = o.out_xform;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    cudaStream_t s = S(stream);
+    uint32_t *q = nullptr;
+    if (format != NTG_FORMAT_BC1 && out_xform != NTG_XFORM_NONE) {
+        // BC3/BC5 quantise the transformed level first (ColorBlock::init on the toGamma'd copy)
+        const XformTables *xt = ctx->xform(NTG_XFORM_NONE, out_xform, gamma);
+        if (!xt) return fail(NTG_ERROR_CUDA, "table upload failed");
+        if (out_xform == NTG_XFORM_GAMMA && gamma != 2.2f)
+            return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "power-law gamma other than 2.2 is not supported on the GPU");
+        uint8_t *ws = nullptr;
+        NTG_TRY(ctx->workspace((size_t)w * h * 4, s, &ws));
+        q = (uint32_t *)ws;
+        NTG_TRY(launched(launch_quantize(d_rgba, (size_t)w * h, out_xform, xt->d_steps, q, s), "quantise level"));
+    } else if (format == NTG_FORMAT_BC1 && out_xform == NTG_XFORM_GAMMA && gamma != 2.2f) {
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "power-law gamma other than 2.2 is not supported on the GPU");
+    }
+    EncJob j;
+    std::memset(&j, 0, sizeof j);
+    j.w = w; j.h = h; j.bw = (w + 3) / 4;
+    j.alpha_mode = alpha_mode;
+    j.out_xform = format == NTG_FORMAT_BC1 ? out_xform : NTG_XFORM_NONE;
+    if (format == NTG_FORMAT_BC1) j.rgba = d_rgba;
+    else if (q) j.bgra = q;
+    else j.rgba = d_rgba;
+    if (cw) { j.cw[0] = cw[0]; j.cw[1] = cw[1]; j.cw[2] = cw[2]; }
+    else { j.cw[0] = j.cw[1] = j.cw[2] = 1.0f; }
+    j.out = (uint8_t *)d_blocks;
+    j.first_block = 0;
+    std::vector<EncJob> jobs(1, j);
+    NTG_TRY(upload_jobs(ctx, jobs, s));
+    return launch_encode(format, ctx->d_jobs, 1, blocks_of(w, h), quality, s);
+}
+
+static int chain_common(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt_in,
+                        void *d_blocks, float *d_levels, void *stream) {
+    NTG_TRY(check_opts(opt_in));
+    const ntg_chain_options norm = normalized(*opt_in);
+    const ntg_chain_options *opt = &norm;
+    if (!ctx || !d_bgra || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    if ((opt->in_xform == NTG_XFORM_GAMMA || opt->out_xform == NTG_XFORM_GAMMA) && opt->gamma != 2.2f &&
+        std::fabs(opt->gamma - 1.0f) > 0.0001f * std::max(1.0f, std::fabs(opt->gamma)))
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "power-law gamma other than 2.2 is not supported on the GPU");
+    NTG_TRY(ensure_device(ctx));
+    cudaStream_t s = S(stream);
+    const ChainPlan P = plan_chain(w, h, *opt, d_levels != nullptr);
+    const XformTables *xt = ctx->xform(opt->in_xform, opt->out_xform, opt->gamma);
+    if (!xt) return fail(NTG_ERROR_CUDA, "table upload failed");
+    uint8_t *ws = nullptr;
+    NTG_TRY(ctx->workspace(std::max<size_t>(P.bytes, 256), s, &ws));
+    if (d_levels && P.f_off[0] != NONE && !P.fast_box) {
+        NTG_TRY(launched(launch_set_image((const uint32_t *)d_bgra, (size_t)w * h, xt->d_in, (float *)(ws + P.f_off[0]), s), "set image"));
+    }
+    if (ctx->profile) NTG_CUDA(cudaEventRecord(ctx->ev[0], s));
+    NTG_TRY(build_levels(ctx, P, (const uint32_t *)d_bgra, *opt, xt, ws, s));
+    if (ctx->profile) NTG_CUDA(cudaEventRecord(ctx->ev[1], s));
+    if (d_levels) {
+        size_t off = 0;
+        for (size_t l = 0; l < P.lv.size(); l++) {
+            const size_t n = 4 * (size_t)P.lv[l].w * P.lv[l].h;
+            NTG_CUDA(cudaMemcpyAsync(d_levels + off, ws + P.f_off[l], n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            off += n;
+        }
+    }
+    if (d_blocks) {
+        std::vector<EncJob> jobs;
+        long long nblocks = 0;
+        chain_jobs(P, (const uint32_t *)d_bgra, *opt, xt, ws, (uint8_t *)d_blocks, jobs, nblocks);
+        NTG_TRY(upload_jobs(ctx, jobs, s));
+        NTG_TRY(launch_encode(opt->format, ctx->d_jobs, (int)jobs.size(), nblocks, opt->quality, s));
+    }
+    if (ctx->profile) NTG_CUDA(cudaEventRecord(ctx->ev[2], s));
+    return NTG_OK;
+}
+
+int ntg_compress_chain(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt, void *d_blocks,
+                       void *stream) {
+    g_error.clear();
+    if (!d_blocks) return fail(NTG_ERROR_INVALID_INPUT, "null output");
+    if (!ctx) return fail(NTG_ERROR_INVALID_INPUT, "null context");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return chain_common(ctx, d_bgra, w, h, opt, d_blocks, nullptr, stream);
+}
+
+int ntg_mip_chain(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt, float *d_levels,
+                  void *stream) {
+    g_error.clear();
+    if (!d_levels) return fail(NTG_ERROR_INVALID_INPUT, "null output");
+    if (!ctx) return fail(NTG_ERROR_INVALID_INPUT, "null context");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return chain_common(ctx, d_bgra, w, h, opt, nullptr, d_levels, stream);
+}
+
+int ntg_compress_chain_host(ntg_context *ctx, const void *h_bgra, int w, int h, const ntg_chain_options *opt,
+                            void *h_blocks, void *stream) {
+    g_error.clear();
+    if (!ctx || !h_bgra || !h_blocks || !opt || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    NTG_TRY(check_opts(opt));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    cudaStream_t s = S(stream);
+    const size_t in_bytes = (size_t)w * h * 4, out_bytes = ntg_chain_bytes(w, h, opt);
+    uint8_t *io = nullptr;
+    NTG_CUDA(cudaMallocAsync((void **)&io, align256(in_bytes) + out_bytes, s));
+    int r = NTG_OK;
+    if (cudaMemcpyAsync(io, h_bgra, in_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "copy in");
+    if (r == NTG_OK) r = chain_common(ctx, io, w, h, opt, io + align256(in_bytes), nullptr, stream);
+    if (r == NTG_OK && cudaMemcpyAsync(h_blocks, io + align256(in_bytes), out_bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        r = cuda_fail(cudaGetLastError(), "copy out");
+    cudaFreeAsync(io, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (r == NTG_OK && e != cudaSuccess) r = cuda_fail(e, "stream");
+    return r;
+}
+
+int ntg_host_polyphase(int filter, float width, const float *params, int src_len, int dst_len, float *weights,
+                       int *lefts, int capacity) {
+    const int ws = polyphase_window(width, src_len, dst_len);
+    if (weights && lefts && (long long)ws * dst_len <= capacity)
+        build_polyphase(filter, width, params ? params[0] : 0.0f, params ? params[1] : 0.0f, src_len, dst_len, weights, lefts);
+    return ws;
+}
+
+int ntg_host_transform_tables(int in_xform, int out_xform, float gamma, float *lut_in, float *lut_composed,
+                              unsigned char *lut8, float *srgb_steps) {
+    HostTables t;
+    build_device_tables(t);
+    if (lut_in) build_input_lut(in_xform, gamma, t, lut_in);
+    if (lut_composed) build_composed_lut(in_xform, out_xform, gamma, t, lut_composed);
+    if (lut8) build_composed_lut8(in_xform, out_xform, gamma, t, lut8);
+    if (srgb_steps) build_srgb_steps(srgb_steps);
+    return NTG_OK;
+}
+
+int ntg_profile_enable(ntg_context *ctx, int enable) {
+    g_error.clear();
+    if (!ctx) return fail(NTG_ERROR_INVALID_INPUT, "null context");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    for (cudaEvent_t &e : ctx->ev)
+        if (!e) NTG_CUDA(cudaEventCreate(&e));
+    ctx->profile = enable != 0;
+    return NTG_OK;
+}
+
+int ntg_profile_read(ntg_context *ctx, float *mips_ms, float *encode_ms) {
+    g_error.clear();
+    if (!ctx || !ctx->ev[2]) return fail(NTG_ERROR_INVALID_INPUT, "profiling not enabled");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_CUDA(cudaEventSynchronize(ctx->ev[2]));
+    float a = 0, b = 0;
+    NTG_CUDA(cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
+    NTG_CUDA(cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]));
+    if (mips_ms) *mips_ms = a;
+    if (encode_ms) *encode_ms = b;
+    return NTG_OK;
+}
+
+int ntg_decode(ntg_context *ctx, int format, const void *d_blocks, int w, int h, float *d_rgba, void *stream) {
+    g_error.clear();
+    if (!ctx || !d_blocks || !d_rgba || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    if (format != NTG_FORMAT_BC1 && format != NTG_FORMAT_BC3 && format != NTG_FORMAT_BC5)
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "format not supported");
+    NTG_TRY(ensure_device(ctx));
+    return launched(launch_decode(format, (const uint8_t *)d_blocks, w, h, d_rgba, S(stream)), "decode");
+}
+
+int ntg_error_sums(ntg_context *ctx, const float *d_ref, const float *d_img, int w, int h, int alpha_mode, double *d_sums,
+                   void *stream) {
+    g_error.clear();
+    if (!ctx || !d_ref || !d_img || !d_sums || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    NTG_TRY(ensure_device(ctx));
+    return launched(launch_rms(d_ref, d_img, w, h, alpha_mode, d_sums, S(stream)), "error sums");
+}
+
+}  // extern "C"

@@ -1,0 +1,536 @@
+// BC1 encoder for sm_103a: the icbc 1.05 fits NVTT's CompressorDXT1 uses
+// (src/nvtt/BlockCompressor.cpp:211-222 -> icbc::compress_dxt1, src/nvtt/icbc.h:3485-3559):
+//   Quality_Fastest    -> icbc Level1: box fit + least squares
+//   Quality_Normal     -> icbc Level8: 4- and 3-colour cluster fit over all orderings
+//   Quality_Production -> icbc Level9: Level8 + endpoint refinement
+// One thread encodes one 4x4 block. The block's texels, its reduced colour set and its summed-area
+// table live in shared memory laid out [element][thread], so the data-dependent element indices of
+// the cluster-fit search never conflict on banks. The ordering index of the search loop is the
+// same in every thread of a warp, so ordering records are read as constant-cache broadcasts.
+// Built with --fmad=false: results are bit-identical to the reference's scalar build.
+#include "ntg_device.cuh"
+#include "ntg_internal.h"
+
+namespace ntg {
+
+template <typename T>
+struct Lane {  // one thread's view of a [k][thread] shared-memory array
+    T *base;
+    int stride;
+    __device__ __forceinline__ T &operator[](int k) const { return base[k * stride]; }
+};
+
+__device__ __forceinline__ float to_srgb(float f) {
+    // toSrgb (src/nvtt/Surface.cpp:1512-1519)
+    if (isnan(f)) return 0.0f;
+    if (f <= 0.0f) return 0.0f;
+    if (f <= 0.0031308f) return 12.92f * f;
+    if (f <= 1.0f) return (powf(f, 0.41666f) * 1.055f) - 0.055f;
+    return 1.0f;
+}
+
+__device__ __forceinline__ unsigned to565(f3 v) {
+    // vector3_to_color16 (src/nvtt/icbc.h:1580-1595)
+    unsigned r = (unsigned)ic_clamp(v.x * 31.0f, 0.0f, 31.0f);
+    unsigned g = (unsigned)ic_clamp(v.y * 63.0f, 0.0f, 63.0f);
+    unsigned b = (unsigned)ic_clamp(v.z * 31.0f, 0.0f, 31.0f);
+    r += (v.x > c_tab.mid5[r]);
+    g += (v.y > c_tab.mid6[g]);
+    b += (v.z > c_tab.mid5[b]);
+    return (r << 11) | (g << 5) | b;
+}
+
+__device__ __forceinline__ float round5(float x) { return (float)(int)(x * 31.0f + 0.5f) * (1.0f / 31.0f); }
+__device__ __forceinline__ float round6(float x) { return (float)(int)(x * 63.0f + 0.5f) * (1.0f / 63.0f); }
+__device__ __forceinline__ f3 round_ept(f3 v) { return mk3(round5(ic_sat(v.x)), round6(ic_sat(v.y)), round5(ic_sat(v.z))); }
+__device__ __forceinline__ bool is_black(f3 c) { return c.x < 1.0f / 8 && c.y < 1.0f / 8 && c.z < 1.0f / 8; }
+__device__ __forceinline__ f3 xyz(float4 v) { return mk3(v.x, v.y, v.z); }
+
+struct Pal3 { f3 p[4]; };
+__device__ __forceinline__ void palette_f(unsigned c0, unsigned c1, Pal3 &pf) {
+    Pal8 p;
+    palette_d3d10(c0, c1, p);
+#pragma unroll
+    for (int i = 0; i < 4; i++) pf.p[i] = mk3(p.r[i] / 255.0f, p.g[i] / 255.0f, p.b[i] / 255.0f);
+}
+
+// compute_indices4 (src/nvtt/icbc.h:2803-2835)
+__device__ uint32_t indices4(const Lane<float4> &in, f3 cw, const Pal3 &pal) {
+    f3 p0 = pal.p[0] * cw, p1 = pal.p[1] * cw, p2 = pal.p[2] * cw, p3 = pal.p[3] * cw;
+    uint32_t idx = 0;
+#pragma unroll 4
+    for (int i = 0; i < 16; i++) {
+        f3 c = xyz(in[i]) * cw;
+        f3 t;
+        t = c - p0; float d0 = dot(t, t);
+        t = c - p1; float d1 = dot(t, t);
+        t = c - p2; float d2 = dot(t, t);
+        t = c - p3; float d3 = dot(t, t);
+        unsigned hi = ((d1 > d2) & (d0 > d2)) | ((d0 > d3) & (d1 > d3));
+        unsigned lo = (d0 > d3) & (d2 > d3);
+        idx |= ((hi << 1) | lo) << (2 * i);
+    }
+    return idx;
+}
+
+// compute_indices3 (src/nvtt/icbc.h:2837-2882)
+__device__ uint32_t indices3(const Lane<float4> &in, f3 cw, bool allow_black, const Pal3 &pal) {
+    f3 p0 = pal.p[0] * cw, p1 = pal.p[1] * cw, p2 = pal.p[2] * cw;
+    uint32_t idx = 0;
+#pragma unroll 4
+    for (int i = 0; i < 16; i++) {
+        f3 c = xyz(in[i]) * cw;
+        f3 t;
+        unsigned hi, lo;
+        if (allow_black) {
+            t = p0 - c; float d0 = dot(t, t);
+            t = p1 - c; float d1 = dot(t, t);
+            t = p2 - c; float d2 = dot(t, t);
+            float d3 = dot(c, c);
+            unsigned i1 = d1 < d2, i2 = (d2 <= d0) & (d2 <= d1), i3 = (d3 <= d0) & (d3 <= d1) & (d3 <= d2);
+            hi = i2 | i3; lo = i1 | i3;
+        } else {
+            t = c - p0; float d0 = dot(t, t);
+            t = c - p1; float d1 = dot(t, t);
+            t = c - p2; float d2 = dot(t, t);
+            hi = (d2 <= d0) & (d2 <= d1); lo = d1 < d2;
+        }
+        idx |= ((hi << 1) | lo) << (2 * i);
+    }
+    return idx;
+}
+
+// compute_indices, live branch (src/nvtt/icbc.h:2885-2941)
+__device__ uint32_t indices_any(const Lane<float4> &in, f3 cw, const Pal3 &pal) {
+    f3 p0 = pal.p[0] * cw, p1 = pal.p[1] * cw, p2 = pal.p[2] * cw, p3 = pal.p[3] * cw;
+    uint32_t idx = 0;
+#pragma unroll 4
+    for (int i = 0; i < 16; i++) {
+        f3 c = xyz(in[i]) * cw;
+        f3 t;
+        t = c - p0; float d0 = dot(t, t);
+        t = c - p1; float d1 = dot(t, t);
+        t = c - p2; float d2 = dot(t, t);
+        t = c - p3; float d3 = dot(t, t);
+        unsigned i1 = (d1 <= d0) & (d1 < d2) & (d1 < d3);
+        unsigned i2 = (d2 <= d0) & (d2 <= d1) & (d2 < d3);
+        unsigned i3 = (d3 <= d0) & (d3 <= d1) & (d3 <= d2);
+        idx |= (((i2 | i3) << 1) | (i1 | i3)) << (2 * i);
+    }
+    return idx;
+}
+
+// evaluate_mse over the input texels (src/nvtt/icbc.h:2733-2756)
+__device__ float block_mse(const Lane<float4> &in, const Lane<float> &wi, f3 cw, const Pal3 &pal, uint32_t idx) {
+    float err = 0.0f;
+#pragma unroll 4
+    for (int i = 0; i < 16; i++) {
+        int k = (idx >> (2 * i)) & 3;
+        f3 p = k == 0 ? pal.p[0] : (k == 1 ? pal.p[1] : (k == 2 ? pal.p[2] : pal.p[3]));
+        f3 d = ((p - xyz(in[i])) * cw) * 255.0f;
+        err += wi[i] * dot(d, d);
+    }
+    return err;
+}
+
+struct Block1 { unsigned c0, c1; uint32_t idx; };
+
+__device__ float output_block4(const Lane<float4> &in, const Lane<float> &wi, f3 cw, f3 v0, f3 v1, Block1 &o) {
+    unsigned c0 = to565(v0), c1 = to565(v1);
+    if (c0 < c1) { unsigned t = c0; c0 = c1; c1 = t; }
+    Pal3 pal;
+    palette_f(c0, c1, pal);
+    o.c0 = c0; o.c1 = c1;
+    o.idx = indices4(in, cw, pal);
+    return block_mse(in, wi, cw, pal, o.idx);
+}
+
+__device__ float output_block3(const Lane<float4> &in, const Lane<float> &wi, f3 cw, bool allow_black, f3 v0, f3 v1, Block1 &o) {
+    unsigned c0 = to565(v0), c1 = to565(v1);
+    if (c0 > c1) { unsigned t = c0; c0 = c1; c1 = t; }
+    Pal3 pal;
+    palette_f(c0, c1, pal);
+    o.c0 = c0; o.c1 = c1;
+    o.idx = indices3(in, cw, allow_black, pal);
+    return block_mse(in, wi, cw, pal, o.idx);
+}
+
+__device__ __forceinline__ float mse_of(const Lane<float4> &in, const Lane<float> &wi, f3 cw, const Block1 &o) {
+    Pal3 pal;
+    palette_f(o.c0, o.c1, pal);
+    return block_mse(in, wi, cw, pal, o.idx);
+}
+
+// compute_sat (src/nvtt/icbc.h:1812-1882) from n colours (xyz) and weights (w) in `col`.
+// Writes the prefix sums in principal-axis order to `sat`. Returns n.
+__device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &sat) {
+    // computeCentroid / computeCovariance (src/nvtt/icbc.h:1700-1741)
+    f3 c = mk3(0, 0, 0);
+    float total = 0.0f;
+    for (int i = 0; i < n; i++) { float4 p = col[i]; total += p.w; c = c + xyz(p) * p.w; }
+    c = c * (1.0f / total);
+    float m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0;
+    for (int i = 0; i < n; i++) {
+        float4 p = col[i];
+        f3 a = xyz(p) - c;
+        f3 b = a * p.w;
+        m0 += a.x * b.x; m1 += a.x * b.y; m2 += a.x * b.z;
+        m3 += a.y * b.y; m4 += a.y * b.z; m5 += a.z * b.z;
+    }
+    // firstEigenVector_PowerMethod (src/nvtt/icbc.h:1760-1790)
+    f3 v;
+    if (m0 == 0 && m3 == 0 && m5 == 0) {
+        v = mk3(0, 0, 0);
+    } else {
+        f3 r0 = mk3(m0, m1, m2), r1 = mk3(m1, m3, m4), r2 = mk3(m2, m4, m5);
+        float l0 = dot(r0, r0), l1 = dot(r1, r1), l2 = dot(r2, r2);
+        v = (l0 > l1 && l0 > l2) ? r0 : (l1 > l2 ? r1 : r2);
+#pragma unroll
+        for (int it = 0; it < 8; it++) {
+            float x = v.x * m0 + v.y * m1 + v.z * m2;
+            float y = v.x * m1 + v.y * m3 + v.z * m4;
+            float z = v.x * m2 + v.y * m4 + v.z * m5;
+            float norm = ic_max(ic_max(x, y), z);
+            v = mk3(x, y, z) * (1.0f / norm);
+        }
+    }
+    // project and stable insertion sort of (dps, order), packed order in a 64-bit word
+    float dps[16];
+    uint64_t order = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        dps[i] = i < n ? dot(xyz(col[i]), v) : 0.0f;
+        order |= (uint64_t)i << (4 * i);
+    }
+#pragma unroll
+    for (int i = 1; i < 16; i++) {
+        bool moving = i < n;
+#pragma unroll
+        for (int j = i; j > 0; --j) {
+            moving = moving && (dps[j] < dps[j - 1]);
+            if (moving) {
+                float t = dps[j]; dps[j] = dps[j - 1]; dps[j - 1] = t;
+                uint64_t a = (order >> (4 * j)) & 15, b = (order >> (4 * (j - 1))) & 15;
+                order &= ~((uint64_t)0xFF << (4 * (j - 1)));
+                order |= (a << (4 * (j - 1))) | (b << (4 * j));
+            }
+        }
+    }
+    float4 acc = col[(int)(order & 15)];
+    acc = make_float4(acc.x * acc.w, acc.y * acc.w, acc.z * acc.w, acc.w);
+    sat[0] = acc;
+    for (int i = 1; i < n; i++) {
+        float4 p = col[(int)((order >> (4 * i)) & 15)];
+        acc = make_float4(acc.x + p.x * p.w, acc.y + p.y * p.w, acc.z + p.z * p.w, acc.w + p.w);
+        sat[i] = acc;
+    }
+    return n;
+}
+
+// Shared solve / snap / residual of cluster_fit_three and cluster_fit_four
+// (src/nvtt/icbc.h:2200-2240, 2501-2540).
+__device__ __forceinline__ float cf_eval(f3 ax, f3 sum, float a2, float b2, float ab, f3 metric, f3 &pa, f3 &pb) {
+    float factor = 1.0f / (a2 * b2 - ab * ab);
+    f3 bx = sum - ax;
+    f3 a = ((ax * b2) - (bx * ab)) * factor;
+    f3 b = ((bx * a2) - (ax * ab)) * factor;
+    a = round_ept(a);
+    b = round_ept(b);
+    f3 e2 = ((a * ((b * ab) - ax)) - (b * bx)) * 2.0f;
+    f3 e1 = ((a * a) * a2) + (((b * b) * b2) + e2);
+    pa = a; pb = b;
+    return dot(e1, metric);
+}
+
+// cluster_fit_four (src/nvtt/icbc.h:2250-2549): all orderings of n points; the first strict
+// minimum wins, as in the scalar build.
+__device__ void cluster_fit_four(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
+    float4 s = sat[n - 1];
+    f3 sum = xyz(s);
+    float wsum = s.w;
+    float best = FLT_MAX;
+    f3 bs = mk3(0, 0, 0), be = mk3(0, 0, 0);
+    const int total = c_tab.four_total[n - 1];
+    for (int i = 0; i < total; i++) {
+        uint32_t o = c_tab.four[i];
+        int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1, c2 = (int)((o >> 16) & 255) - 1;
+        float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
+        float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
+        float4 v2 = c2 >= 0 ? sat[c2] : make_float4(0, 0, 0, 0);
+        float w0 = v0.w, w1 = v1.w, w2 = v2.w;
+        float w3 = wsum - w2;
+        f3 x0 = xyz(v0), x1 = xyz(v1) - x0, x2 = xyz(v2) - xyz(v1);
+        w2 = w2 - w1;
+        w1 = w1 - w0;
+        float a2 = w2 * (1.0f / 9.0f) + (w1 * (4.0f / 9.0f) + w0);
+        float b2 = w1 * (1.0f / 9.0f) + (w2 * (4.0f / 9.0f) + w3);
+        float ab = (w1 + w2) * (2.0f / 9.0f);
+        f3 ax = (x2 * (1.0f / 3.0f)) + ((x1 * (2.0f / 3.0f)) + x0);
+        f3 a, b;
+        float e = cf_eval(ax, sum, a2, b2, ab, metric, a, b);
+        if (e < best) { best = e; bs = a; be = b; }
+    }
+    start = bs; end = be;
+}
+
+// cluster_fit_three (src/nvtt/icbc.h:2016-2247)
+__device__ void cluster_fit_three(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
+    float4 s = sat[n - 1];
+    f3 sum = xyz(s);
+    float wsum = s.w;
+    float best = FLT_MAX;
+    f3 bs = mk3(0, 0, 0), be = mk3(0, 0, 0);
+    const int total = c_tab.three_total[n - 1];
+    for (int i = 0; i < total; i++) {
+        uint32_t o = c_tab.three[i];
+        int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1;
+        float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
+        float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
+        float w0 = v0.w, w1 = v1.w;
+        float w2 = wsum - w1;
+        f3 x0 = xyz(v0), x1 = xyz(v1) - x0;
+        w1 = w1 - w0;
+        float ab = w1 * 0.25f;
+        float a2 = w0 + ab;
+        float b2 = w2 + ab;
+        f3 ax = x0 + (x1 * 0.5f);
+        f3 a, b;
+        float e = cf_eval(ax, sum, a2, b2, ab, metric, a, b);
+        if (e < best) { best = e; bs = a; be = b; }
+    }
+    start = bs; end = be;
+}
+
+// refine_endpoints (src/nvtt/icbc.h:3329-3406), including the reference's use of the current
+// output's palette (not the candidate's) for index selection.
+__device__ float refine_endpoints(const Lane<float4> &in, const Lane<float> &wi, f3 cw, float err, Block1 &o) {
+    const int8_t deltas[16][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1},
+                                  {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {-1, -1, 0}, {-1, 0, -1}, {0, -1, -1},
+                                  {-1, 1, 0}, {1, -1, 0}, {0, -1, 1}, {0, 1, -1}};
+    float best = err;
+    int last = 0;
+    for (int i = 0; i < 256; i++) {
+        Block1 r = o;
+        const int8_t *d = deltas[i % 16];
+        unsigned c = ((i / 16) & 1) ? r.c0 : r.c1;
+        unsigned cr = ((c >> 11) + d[0]) & 31, cg = (((c >> 5) & 63) + d[1]) & 63, cb = ((c & 31) + d[2]) & 31;
+        c = (cr << 11) | (cg << 5) | cb;
+        if ((i / 16) & 1) r.c0 = c; else r.c1 = c;
+        Pal3 pal;
+        palette_f(o.c0, o.c1, pal);
+        r.idx = indices_any(in, cw, pal);
+        float e = mse_of(in, wi, cw, r);
+        if (e < best) { best = e; o = r; last = i; }
+        if (i - last > 32) break;
+    }
+    return best;
+}
+
+__device__ __forceinline__ void store_block(uint8_t *dst, const Block1 &o) {
+    uint2 v;
+    v.x = (o.c0 & 0xFFFF) | (o.c1 << 16);
+    v.y = o.idx;
+    *reinterpret_cast<uint2 *>(dst) = v;
+}
+
+// compress_dxt1 with NVTT's arguments: three-colour mode and transparent black enabled
+// (src/nvtt/icbc.h:3485-3559, src/nvtt/BlockCompressor.cpp:219-222).
+__device__ __forceinline__ int find_job(const EncJob *jobs, int njobs, long long blk) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].first_block <= blk) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int LEVEL>  // 0: icbc Level1, 7: Level8, 8: Level9
+__global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x;
+    const int t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    Lane<float4> in{smem + t, T};
+    Lane<float4> col{smem + 16 * T + t, T};
+    Lane<float4> sat{smem + 32 * T + t, T};
+    Lane<float> wi{reinterpret_cast<float *>(smem + 48 * T) + t, T};
+    const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
+    uint8_t *const out = J.out + 8 * (size_t)blk;
+
+    // FloatColorCompressorTask gather (src/nvtt/BlockCompressor.cpp:116-166)
+    const int bx = blk % J.bw, by = blk / J.bw;
+    const size_t n = (size_t)J.w * J.h;
+    const int vw = min(J.w - bx * 4, 4), vh = min(J.h - by * 4, 4);
+#pragma unroll
+    for (int y = 0; y < 4; y++)
+#pragma unroll
+        for (int x = 0; x < 4; x++) {
+            const int k = 4 * y + x;
+            if (x < vw && y < vh) {
+                const size_t s = (size_t)(by * 4 + y) * J.w + (bx * 4 + x);
+                float r, g, b, al;
+                if (J.bgra) {
+                    // 8-bit source through the composed input/output transform table
+                    const uint32_t p = J.bgra[s];
+                    r = J.lut_f[(p >> 16) & 255]; g = J.lut_f[(p >> 8) & 255]; b = J.lut_f[p & 255];
+                    al = (float)(p >> 24) / 255.0f;
+                } else {
+                    r = J.rgba[s]; g = J.rgba[n + s]; b = J.rgba[2 * n + s]; al = J.rgba[3 * n + s];
+                    if (J.out_xform == 1) { r = powf_5_11(r); g = powf_5_11(g); b = powf_5_11(b); }
+                    else if (J.out_xform == 2) { r = to_srgb(r); g = to_srgb(g); b = to_srgb(b); }
+                }
+                in[k] = make_float4(r, g, b, al);
+                wi[k] = J.alpha_mode == 1 ? ic_clamp(al, 0.0f, 1.0f) : 1.0f;
+            } else {
+                in[k] = make_float4(0, 0, 0, 0);
+                wi[k] = 0.0f;
+            }
+        }
+
+    Block1 o{0, 0, 0};
+    float err = FLT_MAX;
+
+    if (LEVEL == 0) {
+        // Level1: box fit of all 16 texels, inset, diagonal, then least squares
+        // (src/nvtt/icbc.h:3096-3151, 2984-3016)
+        f3 c0 = mk3(0, 0, 0), c1 = mk3(1, 1, 1);
+        for (int i = 0; i < 16; i++) {
+            f3 p = xyz(in[i]);
+            c0 = mk3(ic_max(c0.x, p.x), ic_max(c0.y, p.y), ic_max(c0.z, p.z));
+            c1 = mk3(ic_min(c1.x, p.x), ic_min(c1.y, p.y), ic_min(c1.z, p.z));
+        }
+        const float bias = (8.0f / 255.0f) / 16.0f;
+        f3 d = c0 - c1;
+        f3 inset = mk3(d.x / 16.0f, d.y / 16.0f, d.z / 16.0f) - mk3(bias, bias, bias);
+        c0 = sat3(c0 - inset);
+        c1 = sat3(c1 + inset);
+        f3 center = (c0 + c1) * 0.5f;
+        float cxz = 0.0f, cyz = 0.0f;
+        for (int i = 0; i < 16; i++) { f3 tt = xyz(in[i]) - center; cxz += tt.x * tt.z; cyz += tt.y * tt.z; }
+        float x0 = c0.x, y0 = c0.y, x1 = c1.x, y1 = c1.y;
+        if (cxz < 0) { float tt = x0; x0 = x1; x1 = tt; }
+        if (cyz < 0) { float tt = y0; y0 = y1; y1 = tt; }
+        c0 = mk3(x0, y0, c0.z); c1 = mk3(x1, y1, c1.z);
+        err = output_block4(in, wi, cw, c0, c1, o);
+        // optimize_end_points4 on the 16 input texels
+        float a2 = 0, b2 = 0, ab = 0;
+        f3 ax = mk3(0, 0, 0), bxs = mk3(0, 0, 0);
+        for (int i = 0; i < 16; i++) {
+            unsigned bits = o.idx >> (2 * i);
+            float beta = (float)(bits & 1);
+            if (bits & 2) beta = (1 + beta) / 3.0f;
+            float alpha = 1.0f - beta;
+            f3 p = xyz(in[i]);
+            a2 += alpha * alpha; b2 += beta * beta; ab += alpha * beta;
+            ax = ax + p * alpha; bxs = bxs + p * beta;
+        }
+        float den = a2 * b2 - ab * ab;
+        if (!(fabsf(den - 0.0f) < 0.0001f)) {
+            float f = 1.0f / den;
+            f3 na = sat3(((ax * b2) - (bxs * ab)) * f);
+            f3 nb = sat3(((bxs * a2) - (ax * ab)) * f);
+            Block1 t2;
+            float e2 = output_block4(in, wi, cw, na, nb, t2);
+            if (e2 < err) { err = e2; o = t2; }
+        }
+        store_block(out, o);
+        return;
+    }
+
+    // reduce_colors (src/nvtt/icbc.h:1638-1683), threshold 1/256
+    const float thr = 1.0f / 256;
+    int cnt = 0;
+    bool any_black = false;
+    for (int i = 0; i < 16; i++) {
+        float wt = wi[i];
+        if (wt > 0) {
+            f3 c = xyz(in[i]);
+            int j;
+            for (j = 0; j < cnt; j++) {
+                float4 q = col[j];
+                if (fabsf(q.x - c.x) < thr && fabsf(q.y - c.y) < thr && fabsf(q.z - c.z) < thr) {
+                    float den = q.w + wt;
+                    f3 s = (xyz(q) * q.w) + (c * wt);
+                    col[j] = make_float4(s.x / den, s.y / den, s.z / den, q.w + wt);
+                    break;
+                }
+            }
+            if (j == cnt) { col[cnt] = make_float4(c.x, c.y, c.z, wt); cnt++; }
+            if (is_black(c)) any_black = true;
+        }
+    }
+
+    if (cnt == 0) {
+        store_block(out, Block1{0, 0, 0});
+        return;
+    }
+    if (cnt == 1) {
+        // compress_dxt1_single_color_optimal (src/nvtt/icbc.h:3274-3289)
+        float4 c = col[0];
+        int r = (int)(uint8_t)(ic_sat(c.x) * 255 + 0.5f);
+        int g = (int)(uint8_t)(ic_sat(c.y) * 255 + 0.5f);
+        int b = (int)(uint8_t)(ic_sat(c.z) * 255 + 0.5f);
+        o.c0 = ((unsigned)c_tab.icbc_match5[r][0] << 11) | ((unsigned)c_tab.icbc_match6[g][0] << 5) | c_tab.icbc_match5[b][0];
+        o.c1 = ((unsigned)c_tab.icbc_match5[r][1] << 11) | ((unsigned)c_tab.icbc_match6[g][1] << 5) | c_tab.icbc_match5[b][1];
+        o.idx = 0xaaaaaaaau;
+        if (o.c0 < o.c1) { unsigned tt = o.c0; o.c0 = o.c1; o.c1 = tt; o.idx ^= 0x55555555u; }
+        store_block(out, o);
+        return;
+    }
+
+    // compress_dxt1_cluster_fit (src/nvtt/icbc.h:3292-3325)
+    const f3 metric = cw * cw;
+    int sn = compute_sat(col, cnt, sat);
+    f3 s0, s1;
+    cluster_fit_four(sat, sn, metric, s0, s1);
+    Block1 cf;
+    float cerr = output_block4(in, wi, cw, s0, s1, cf);
+    bool run3 = true;
+    if (any_black) {
+        // skip_blacks in place: compact the non-black colours to the front of `col`
+        int m = 0;
+        for (int i = 0; i < cnt; i++) {
+            float4 q = col[i];
+            if (is_black(xyz(q))) continue;
+            col[m++] = q;
+        }
+        if (m == 0) run3 = false;
+        else sn = compute_sat(col, m, sat);
+    }
+    if (run3) {
+        cluster_fit_three(sat, sn, metric, s0, s1);
+        Block1 c3;
+        float e3 = output_block3(in, wi, cw, true, s0, s1, c3);
+        if (e3 < cerr) { cerr = e3; cf = c3; }
+    }
+    // taken only when its error compares below FLT_MAX: a NaN error leaves the block as the
+    // reference leaves it unwritten (this build writes zeros there)
+    if (cerr < err) { o = cf; err = cerr; }
+    if (LEVEL == 8) err = refine_endpoints(in, wi, cw, err, o);
+    store_block(out, o);
+}
+
+int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t stream) {
+    if (nblocks == 0) return 0;
+    const int T = 64;
+    const size_t sm = (size_t)T * (48 * sizeof(float4) + 16 * sizeof(float));
+    const unsigned grid = (unsigned)((nblocks + T - 1) / T);
+    static bool attrs = false;
+    if (!attrs) {  // the per-thread arrays exceed the 48 KB default of dynamic shared memory
+        cudaFuncSetAttribute(k_bc1<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_bc1<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_bc1<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        attrs = true;
+    }
+    if (quality == 0) k_bc1<0><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks);
+    else if (quality == 2) k_bc1<8><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks);
+    else k_bc1<7><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks);
+    return launch_status();
+}
+
+NTG_DEFINE_TABLE_UPLOAD(upload_tables_bc1)
+
+}  // namespace ntg

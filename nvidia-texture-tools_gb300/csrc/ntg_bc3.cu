@@ -1,0 +1,540 @@
+// BC3 and BC5 encoders for sm_103a.
+//
+// BC3 = CompressorDXT5::compressBlock (src/nvtt/CompressorDX9.cpp:145-176):
+//   alpha : QuickCompress::compressDXT5A (Normal/Production) or OptimalCompress::compressDXT5A
+//           (Highest); colour: OptimalCompress::compressDXT1 for single-colour blocks, otherwise
+//           squish's WeightedClusterFit::Compress4 over all 969 cluster splits (scalar build).
+//   Fastest uses FastCompressorDXT5 = QuickCompress::compressDXT1 + compressDXT5A.
+// BC5 = FastCompressorBC5 / ProductionCompressorBC5 (src/nvtt/CompressorDX10.cpp:51-85): the
+//   red and green channels as two interpolated-alpha blocks.
+//
+// One thread encodes one block. The 16 texels stay in registers; the principal-axis sort is a
+// fully unrolled stable insertion network, and the weighted points it produces are staged in
+// shared memory as [element][thread] because the cluster-split loops index them by running
+// counts. Blocks with 16 distinct colours (the common case) all run the same 969-split schedule,
+// so those warps do not diverge in the search. Built with --fmad=false.
+#include "ntg_device.cuh"
+#include "ntg_internal.h"
+
+namespace ntg {
+
+struct AlphaBlk { int a0, a1; uint64_t idx; };  // idx: 16 x 3-bit, texel i at bits 3i
+
+__device__ __forceinline__ void pack_alpha(const AlphaBlk &b, uint8_t *dst) {
+    uint64_t u = (uint64_t)(b.a0 & 255) | ((uint64_t)(b.a1 & 255) << 8) | (b.idx << 16);
+    *reinterpret_cast<uint2 *>(dst) = make_uint2((uint32_t)u, (uint32_t)(u >> 32));
+}
+
+// computeAlphaIndices of QuickCompress (src/nvtt/QuickCompressDXT.cpp:505-536)
+__device__ __forceinline__ unsigned quick_alpha_indices(const int a[16], AlphaBlk &b) {
+    int pal[8];
+    alpha_palette(b.a0, b.a1, pal);
+    unsigned total = 0;
+    uint64_t idx = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        unsigned besterr = 256 * 256;
+        int best = 8;
+#pragma unroll
+        for (int p = 0; p < 8; p++) {
+            int d = pal[p] - a[i];
+            unsigned e = (unsigned)(d * d);
+            if (e < besterr) { besterr = e; best = p; }
+        }
+        total += besterr;
+        idx |= (uint64_t)best << (3 * i);
+    }
+    b.idx = idx;
+    return total;
+}
+
+// optimizeAlpha8 (src/nvtt/QuickCompressDXT.cpp:538-592)
+__device__ __forceinline__ void quick_alpha_refit(const int a[16], AlphaBlk &b) {
+    float a2 = 0, b2 = 0, ab = 0, ax = 0, bx = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        unsigned k = (unsigned)(b.idx >> (3 * i)) & 7;
+        float alpha = k < 2 ? 1.0f - k : (8.0f - k) / 7.0f;
+        float beta = 1 - alpha;
+        a2 += alpha * alpha; b2 += beta * beta; ab += alpha * beta;
+        ax += alpha * a[i]; bx += beta * a[i];
+    }
+    const float f = 1.0f / (a2 * b2 - ab * ab);
+    float fa = (ax * b2 - bx * ab) * f;
+    float fb = (bx * a2 - ax * ab) * f;
+    unsigned v0 = (unsigned)ic_min(ic_max(fa, 0.0f), 255.0f);
+    unsigned v1 = (unsigned)ic_min(ic_max(fb, 0.0f), 255.0f);
+    if (v0 < v1) {
+        unsigned t = v0; v0 = v1; v1 = t;
+        uint64_t n = 0;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            unsigned k = (unsigned)(b.idx >> (3 * i)) & 7;
+            n |= (uint64_t)(k < 2 ? 1 - k : 9 - k) << (3 * i);
+        }
+        b.idx = n;
+    } else if (v0 == v1) {
+        b.idx = 0;
+    }
+    b.a0 = (int)v0; b.a1 = (int)v1;
+}
+
+// QuickCompress::compressDXT5A (src/nvtt/QuickCompressDXT.cpp:779-821); its sameIndices()
+// compares the endpoint bytes only, kept as is.
+__device__ AlphaBlk dxt5a_quick(const int a[16]) {
+    int hi = 0, lo = 255;
+#pragma unroll
+    for (int i = 0; i < 16; i++) { hi = max(hi, a[i]); lo = min(lo, a[i]); }
+    AlphaBlk b;
+    b.a0 = (uint8_t)(hi - (hi - lo) / 34);
+    b.a1 = (uint8_t)(lo + (hi - lo) / 34);
+    unsigned best = quick_alpha_indices(a, b);
+    AlphaBlk bestb = b;
+    for (int it = 0; it < 8; it++) {
+        quick_alpha_refit(a, b);
+        unsigned e = quick_alpha_indices(a, b);
+        if (e >= best) break;
+        if (b.a0 == bestb.a0 && b.a1 == bestb.a1) { bestb = b; break; }
+        best = e;
+        bestb = b;
+    }
+    return bestb;
+}
+
+// computeAlphaError (src/nvtt/OptimalCompressDXT.cpp:189-217), unit weights, early out.
+__device__ __forceinline__ float opt_alpha_error(const int a[16], int a0, int a1, float bound) {
+    int pal[8];
+    alpha_palette(a0, a1, pal);
+    float total = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        int md = 0x7fffffff;
+#pragma unroll
+        for (int p = 0; p < 8; p++) { int d = a[i] - pal[p]; d = d * d; md = d < md ? d : md; }
+        total += md * 1.0f;
+        if (total > bound) return total;
+    }
+    return total;
+}
+
+// OptimalCompress::compressDXT5A (src/nvtt/OptimalCompressDXT.cpp:512-607), starting from a zeroed
+// destination block (the reference starts from whatever the destination held).
+__device__ AlphaBlk dxt5a_optimal(const int a[16]) {
+    int mina = 255, maxa = 0, mina01 = 255, maxa01 = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        int v = a[i];
+        mina = min(mina, v); maxa = max(maxa, v);
+        if (v != 0 && v != 255) { mina01 = min(mina01, v); maxa01 = max(maxa01, v); }
+    }
+    AlphaBlk b;
+    if (maxa - mina < 8) { b.a0 = maxa; b.a1 = mina; }
+    else if (maxa01 - mina01 < 6) { b.a0 = mina01; b.a1 = maxa01; }
+    else {
+        float besterr = opt_alpha_error(a, 0, 0, FLT_MAX);
+        int ba0 = maxa, ba1 = mina;
+        int lo = mina <= 8 ? 0 : mina - 8, hi = maxa >= 255 - 8 ? 255 : maxa + 8;
+        for (int a0 = lo + 9; a0 < hi; a0++)
+            for (int a1 = lo; a1 < a0 - 8; a1++) {
+                float e = opt_alpha_error(a, a0, a1, besterr);
+                if (e < besterr) { besterr = e; ba0 = a0; ba1 = a1; }
+            }
+        lo = mina01 <= 6 ? 0 : mina01 - 6;
+        hi = maxa01 >= 255 - 6 ? 255 : maxa01 + 6;
+        for (int a0 = lo + 9; a0 < hi; a0++)
+            for (int a1 = lo; a1 < a0 - 8; a1++) {
+                float e = opt_alpha_error(a, a1, a0, besterr);
+                if (e < besterr) { besterr = e; ba0 = a1; ba1 = a0; }
+            }
+        b.a0 = ba0; b.a1 = ba1;
+    }
+    int pal[8];
+    alpha_palette(b.a0, b.a1, pal);
+    uint64_t idx = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        int md = 0x7fffffff, bi = 8;
+#pragma unroll
+        for (int p = 0; p < 8; p++) { int d = a[i] - pal[p]; d = d * d; if (d < md) { md = d; bi = p; } }
+        idx |= (uint64_t)bi << (3 * i);
+    }
+    b.idx = idx;
+    return b;
+}
+
+// OptimalCompress::compressDXT1(Color32) (src/nvtt/OptimalCompressDXT.cpp:254-269)
+__device__ __forceinline__ uint2 dxt1_single_color(int r, int g, int b) {
+    unsigned c0 = ((unsigned)c_tab.opt_match5[r][0] << 11) | ((unsigned)c_tab.opt_match6[g][0] << 5) | c_tab.opt_match5[b][0];
+    unsigned c1 = ((unsigned)c_tab.opt_match5[r][1] << 11) | ((unsigned)c_tab.opt_match6[g][1] << 5) | c_tab.opt_match5[b][1];
+    uint32_t idx = 0xaaaaaaaau;
+    if (c0 < c1) { unsigned t = c0; c0 = c1; c1 = t; idx ^= 0x55555555u; }
+    return make_uint2(c0 | (c1 << 16), idx);
+}
+
+__device__ __forceinline__ int float_to_int(float a, int limit) {
+    int i = (int)(a + 0.5f);
+    return i < 0 ? 0 : (i > limit ? limit : i);
+}
+
+// squish WeightedClusterFit, scalar build: ColourSet with the header's default
+// createMinimalSet = true (src/nvtt/squish/colourset.h:40, colourset.cpp:44-90), SetColourSet
+// (src/nvtt/squish/weightedclusterfit.cpp:39-105), ComputeWeightedCovariance /
+// ComputePrincipleComponent (src/nvtt/squish/maths.cpp:32-135), Compress4
+// (src/nvtt/squish/weightedclusterfit.cpp:476-589), WriteColourBlock4
+// (src/nvtt/squish/colourblock.cpp:108-139).
+//
+// The minimal set is kept in texel slots instead of being compacted: a slot is live when its
+// texel is the first with that RGB, and its weight collects the weights of the later duplicates
+// in texel order. Live slots in slot order are exactly the reference's points in order, so the
+// sums run in the same order; dead slots sort last behind +inf keys. Everything stays in
+// registers with static indices; `wp` is this thread's [17][thread] float4 staging for the
+// split loops, which index points by running counts.
+template <typename Arr>
+__device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f3 metric, Arr wp) {
+    float X[16], Y[16], Z[16], W[16];
+    uint32_t live = 0;        // bit i: slot i holds a point
+    uint64_t first = 0;       // 4 bits per texel: slot of its point
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        X[i] = (float)((px[i] >> 16) & 255) / 255.0f;
+        Y[i] = (float)((px[i] >> 8) & 255) / 255.0f;
+        Z[i] = (float)(px[i] & 255) / 255.0f;
+        W[i] = weight_by_alpha ? (float)((px[i] >> 24) + 1) / 256.0f : 1.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        bool found = false;
+        int slot = i;
+#pragma unroll
+        for (int j = 0; j < i; j++) {
+            const bool m = !found && ((px[i] & 0xFFFFFF) == (px[j] & 0xFFFFFF));
+            if (m) { W[j] += W[i]; slot = j; }
+            found = found || m;
+        }
+        if (!found) live |= 1u << i;
+        first |= (uint64_t)slot << (4 * i);
+    }
+    const int count = __popc(live);
+    float total = 0.0f;
+    f3 cen = mk3(0, 0, 0);
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+        if (live & (1u << i)) { total += W[i]; cen = cen + mk3(X[i], Y[i], Z[i]) * W[i]; }
+    cen = cen * (1.0f / total);
+    float m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        if (!(live & (1u << i))) continue;
+        f3 a = (mk3(X[i], Y[i], Z[i]) - cen) * metric;
+        f3 b = a * W[i];
+        m0 += a.x * b.x; m1 += a.x * b.y; m2 += a.x * b.z;
+        m3 += a.y * b.y; m4 += a.y * b.z; m5 += a.z * b.z;
+    }
+    f3 r0 = mk3(m0, m1, m2), r1 = mk3(m1, m3, m4), r2 = mk3(m2, m4, m5);
+    float l0 = dot(r0, r0), l1 = dot(r1, r1), l2 = dot(r2, r2);
+    f3 v = (l0 > l1 && l0 > l2) ? r0 : (l1 > l2 ? r1 : r2);
+#pragma unroll
+    for (int it = 0; it < 8; it++) {
+        float x = v.x * m0 + v.y * m1 + v.z * m2;
+        float y = v.x * m1 + v.y * m3 + v.z * m4;
+        float z = v.x * m2 + v.y * m4 + v.z * m5;
+        float norm = sq_max(sq_max(x, y), z);
+        float iv = 1.0f / norm;
+        if (norm == 0.0f) { v = mk3(0, 0, 0); break; }
+        v = mk3(x * iv, y * iv, z * iv);
+    }
+    // stable insertion sort along the axis; slot numbers carried in a packed 64-bit word
+    float dps[16];
+    uint64_t order = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        dps[i] = (live & (1u << i)) ? dot(mk3(X[i], Y[i], Z[i]), v) : __int_as_float(0x7f800000);
+        order |= (uint64_t)i << (4 * i);
+    }
+#pragma unroll
+    for (int i = 1; i < 16; i++) {
+        bool moving = true;
+#pragma unroll
+        for (int j = i; j > 0; --j) {
+            moving = moving && (dps[j] < dps[j - 1]);
+            if (moving) {
+                float t;
+                t = dps[j]; dps[j] = dps[j - 1]; dps[j - 1] = t;
+                t = X[j]; X[j] = X[j - 1]; X[j - 1] = t;
+                t = Y[j]; Y[j] = Y[j - 1]; Y[j - 1] = t;
+                t = Z[j]; Z[j] = Z[j - 1]; Z[j - 1] = t;
+                t = W[j]; W[j] = W[j - 1]; W[j - 1] = t;
+                uint64_t a = (order >> (4 * j)) & 15, b = (order >> (4 * (j - 1))) & 15;
+                order &= ~((uint64_t)0xFF << (4 * (j - 1)));
+                order |= (a << (4 * (j - 1))) | (b << (4 * j));
+            }
+        }
+    }
+    f3 xsum = mk3(0, 0, 0);
+    float wsum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        f3 p = mk3(X[i], Y[i], Z[i]) * W[i];
+        wp[i] = make_float4(p.x, p.y, p.z, W[i]);
+        if (i < count) { xsum = xsum + p; wsum += W[i]; }
+    }
+    wp[16] = make_float4(0, 0, 0, 0);
+    const f3 msq = metric * metric;
+
+    float besterr = FLT_MAX;
+    f3 bs = mk3(0, 0, 0), be = mk3(0, 0, 0);
+    int b0 = 0, b1 = 0, b2 = 0;
+    f3 x0 = mk3(0, 0, 0);
+    float w0 = 0.0f;
+    for (int c0 = 0; c0 <= count; c0++) {
+        f3 x1 = mk3(0, 0, 0);
+        float w1 = 0.0f;
+        for (int c1 = 0; c1 <= count - c0; c1++) {
+            f3 x2 = mk3(0, 0, 0);
+            float w2 = 0.0f;
+            for (int c2 = 0; c2 <= count - c0 - c1; c2++) {
+                float w3 = wsum - w0 - w1 - w2;
+                float a2 = w0 + w1 * (4.0f / 9.0f) + w2 * (1.0f / 9.0f);
+                float b2s = w3 + w2 * (4.0f / 9.0f) + w1 * (1.0f / 9.0f);
+                float ab = (w1 + w2) * (2.0f / 9.0f);
+                float f = 1.0f / (a2 * b2s - ab * ab);
+                f3 ax = (x0 + (x1 * (2.0f / 3.0f))) + (x2 * (1.0f / 3.0f));
+                f3 bx = xsum - ax;
+                f3 a = ((ax * b2s) - (bx * ab)) * f;
+                f3 b = ((bx * a2) - (ax * ab)) * f;
+                a = mk3(sq_min(1.0f, sq_max(0.0f, a.x)), sq_min(1.0f, sq_max(0.0f, a.y)), sq_min(1.0f, sq_max(0.0f, a.z)));
+                b = mk3(sq_min(1.0f, sq_max(0.0f, b.x)), sq_min(1.0f, sq_max(0.0f, b.y)), sq_min(1.0f, sq_max(0.0f, b.z)));
+                a = mk3(floorf(31.0f * a.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * a.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * a.z + 0.5f) * (1.0f / 31.0f));
+                b = mk3(floorf(31.0f * b.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * b.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * b.z + 0.5f) * (1.0f / 31.0f));
+                f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
+                f3 e1 = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
+                float err = dot(e1, msq);
+                if (err < besterr) { besterr = err; bs = a; be = b; b0 = c0; b1 = c1; b2 = c2; }
+                float4 q = wp[c0 + c1 + c2];
+                x2 = x2 + mk3(q.x, q.y, q.z);
+                w2 += q.w;
+            }
+            float4 q = wp[c0 + c1];
+            x1 = x1 + mk3(q.x, q.y, q.z);
+            w1 += q.w;
+        }
+        float4 q = wp[c0];
+        x0 = x0 + mk3(q.x, q.y, q.z);
+        w0 += q.w;
+    }
+    if (!(besterr < FLT_MAX)) return make_uint2(0, 0);
+    // cluster sizes -> point (slot) indices -> texel indices (ColourSet::RemapIndices)
+    uint32_t slot_idx = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        const uint32_t c = i < b0 ? 0u : (i < b0 + b1 ? 2u : (i < b0 + b1 + b2 ? 3u : 1u));
+        if (i < count) slot_idx |= c << (2 * (int)((order >> (4 * i)) & 15));
+    }
+    uint32_t idx = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) idx |= ((slot_idx >> (2 * (int)((first >> (4 * i)) & 15))) & 3u) << (2 * i);
+    int ea = (float_to_int(31.0f * bs.x, 31) << 11) | (float_to_int(63.0f * bs.y, 63) << 5) | float_to_int(31.0f * bs.z, 31);
+    int eb = (float_to_int(31.0f * be.x, 31) << 11) | (float_to_int(63.0f * be.y, 63) << 5) | float_to_int(31.0f * be.z, 31);
+    if (ea < eb) { int t = ea; ea = eb; eb = t; idx ^= 0x55555555u; }
+    else if (ea == eb) idx = 0;
+    return make_uint2((uint32_t)ea | ((uint32_t)eb << 16), idx);
+}
+
+// QuickCompress::compressDXT1 (src/nvtt/QuickCompressDXT.cpp:653-713) with roundAndExpand
+// (:122-149), computeIndices4 (:195-227) and optimizeEndPoints4 (:406-452).
+__device__ __forceinline__ unsigned quick_round_expand(f3 &v) {
+    unsigned r = (unsigned)floorf(ic_clamp(v.x * (31.0f / 255.0f), 0.0f, 31.0f));
+    unsigned g = (unsigned)floorf(ic_clamp(v.y * (63.0f / 255.0f), 0.0f, 63.0f));
+    unsigned b = (unsigned)floorf(ic_clamp(v.z * (31.0f / 255.0f), 0.0f, 31.0f));
+    if (fabsf(v.x - (float)ex5(r + 1)) < fabsf(v.x - (float)ex5(r))) r = min(r + 1, 31u);
+    if (fabsf(v.y - (float)ex6(g + 1)) < fabsf(v.y - (float)ex6(g))) g = min(g + 1, 63u);
+    if (fabsf(v.z - (float)ex5(b + 1)) < fabsf(v.z - (float)ex5(b))) b = min(b + 1, 31u);
+    unsigned w = (r << 11) | (g << 5) | b;
+    v = mk3((float)ex5(r), (float)ex6(g), (float)ex5(b));
+    return w;
+}
+
+__device__ __forceinline__ uint32_t quick_indices4(const f3 blk[16], f3 mx, f3 mn) {
+    const float s1 = 1.0f - 1.0f / 3.0f, s2 = 1.0f - 2.0f / 3.0f;
+    f3 p2 = mk3(mx.x * s1 + (1.0f / 3.0f) * mn.x, mx.y * s1 + (1.0f / 3.0f) * mn.y, mx.z * s1 + (1.0f / 3.0f) * mn.z);
+    f3 p3 = mk3(mx.x * s2 + (2.0f / 3.0f) * mn.x, mx.y * s2 + (2.0f / 3.0f) * mn.y, mx.z * s2 + (2.0f / 3.0f) * mn.z);
+    uint32_t idx = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        f3 t;
+        t = mx - blk[i]; float d0 = dot(t, t);
+        t = mn - blk[i]; float d1 = dot(t, t);
+        t = p2 - blk[i]; float d2 = dot(t, t);
+        t = p3 - blk[i]; float d3 = dot(t, t);
+        unsigned q0 = d0 > d3, q1 = d1 > d2, q2 = d0 > d2, q3 = d1 > d3, q4 = d2 > d3;
+        unsigned x0 = q1 & q2, x1 = q0 & q3, x2 = q0 & q4;
+        idx |= (x2 | ((x0 | x1) << 1)) << (2 * i);
+    }
+    return idx;
+}
+
+__device__ uint2 quick_dxt1(const uint32_t px[16]) {
+    f3 blk[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) blk[i] = mk3((float)((px[i] >> 16) & 255), (float)((px[i] >> 8) & 255), (float)(px[i] & 255));
+    f3 mx = mk3(0, 0, 0), mn = mk3(255, 255, 255);
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        mx = mk3(ic_max(mx.x, blk[i].x), ic_max(mx.y, blk[i].y), ic_max(mx.z, blk[i].z));
+        mn = mk3(ic_min(mn.x, blk[i].x), ic_min(mn.y, blk[i].y), ic_min(mn.z, blk[i].z));
+    }
+    f3 center = (mx + mn) * 0.5f;
+    float cx = 0.0f, cy = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 16; i++) { f3 t = blk[i] - center; cx += t.x * t.z; cy += t.y * t.z; }
+    float x0 = mx.x, y0 = mx.y, x1 = mn.x, y1 = mn.y;
+    if (cx < 0) { float t = x0; x0 = x1; x1 = t; }
+    if (cy < 0) { float t = y0; y0 = y1; y1 = t; }
+    mx = mk3(x0, y0, mx.z); mn = mk3(x1, y1, mn.z);
+    f3 d = mx - mn;
+    const float bias = (8.0f / 255.0f) / 16.0f;
+    f3 inset = mk3(d.x / 16.0f - bias, d.y / 16.0f - bias, d.z / 16.0f - bias);
+    f3 t = mx - inset;
+    mx = mk3(ic_clamp(t.x, 0.0f, 255.0f), ic_clamp(t.y, 0.0f, 255.0f), ic_clamp(t.z, 0.0f, 255.0f));
+    t = mn + inset;
+    mn = mk3(ic_clamp(t.x, 0.0f, 255.0f), ic_clamp(t.y, 0.0f, 255.0f), ic_clamp(t.z, 0.0f, 255.0f));
+    unsigned c0 = quick_round_expand(mx), c1 = quick_round_expand(mn);
+    if (c0 < c1) { f3 tv = mx; mx = mn; mn = tv; unsigned tc = c0; c0 = c1; c1 = tc; }
+    uint32_t idx = quick_indices4(blk, mx, mn);
+    float a2 = 0, b2 = 0, ab = 0;
+    f3 ax = mk3(0, 0, 0), bx = mk3(0, 0, 0);
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        unsigned bits = idx >> (2 * i);
+        float beta = (float)(bits & 1);
+        if (bits & 2) beta = (1 + beta) / 3.0f;
+        float alpha = 1.0f - beta;
+        a2 += alpha * alpha; b2 += beta * beta; ab += alpha * beta;
+        ax = ax + blk[i] * alpha; bx = bx + blk[i] * beta;
+    }
+    float den = a2 * b2 - ab * ab;
+    if (!(fabsf(den - 0.0f) <= 0.0001f * ic_max(ic_max(1.0f, fabsf(den)), 0.0f))) {
+        float f = 1.0f / den;
+        f3 a = ((ax * b2) - (bx * ab)) * f;
+        f3 b = ((bx * a2) - (ax * ab)) * f;
+        a = mk3(ic_clamp(a.x, 0.0f, 255.0f), ic_clamp(a.y, 0.0f, 255.0f), ic_clamp(a.z, 0.0f, 255.0f));
+        b = mk3(ic_clamp(b.x, 0.0f, 255.0f), ic_clamp(b.y, 0.0f, 255.0f), ic_clamp(b.z, 0.0f, 255.0f));
+        unsigned e0 = quick_round_expand(a), e1 = quick_round_expand(b);
+        if (e0 < e1) { f3 tv = a; a = b; b = tv; unsigned tc = e0; e0 = e1; e1 = tc; }
+        c0 = e0; c1 = e1;
+        idx = quick_indices4(blk, a, b);
+    }
+    return make_uint2(c0 | (c1 << 16), idx);
+}
+
+__device__ __forceinline__ int find_job(const EncJob *jobs, int njobs, long long blk) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].first_block <= blk) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Loads a block's 16 texels as BGRA words (b | g << 8 | r << 16 | a << 24), with ColorBlock's
+// edge repetition (src/nvimage/ColorBlock.cpp:57-110):
+//  - from BGRA8 words, optionally remapped through 8-bit tables (the composed transform +
+//    quantiser of an 8-bit source level), or
+//  - from a planar FP32 level with ColorBlock::init(float)'s clamp-and-truncate.
+__device__ __forceinline__ void load_block(const EncJob &J, int x, int y, uint32_t px[16]) {
+    const unsigned bw = min(J.w - x, 4), bh = min(J.h - y, 4);
+    const size_t n = (size_t)J.w * J.h;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const unsigned yy = (unsigned)i % bh;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const unsigned xx = (unsigned)e % bw;
+            const size_t idx = (size_t)(y + yy) * J.w + x + xx;
+            uint32_t p;
+            if (J.bgra) {
+                p = J.bgra[idx];
+                if (J.lut8)
+                    p = (uint32_t)J.lut8[p & 255] | ((uint32_t)J.lut8[(p >> 8) & 255] << 8) |
+                        ((uint32_t)J.lut8[(p >> 16) & 255] << 16) | ((uint32_t)J.lut8[256 + (p >> 24)] << 24);
+            } else {
+                p = quant_u8(J.rgba[idx + 2 * n]) | (quant_u8(J.rgba[idx + n]) << 8) | (quant_u8(J.rgba[idx]) << 16) |
+                    (quant_u8(J.rgba[idx + 3 * n]) << 24);
+            }
+            px[4 * i + e] = p;
+        }
+    }
+}
+
+template <int QUALITY>
+__global__ void __launch_bounds__(128) k_bc3(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    uint32_t px[16];
+    load_block(J, 4 * (blk % J.bw), 4 * (blk / J.bw), px);
+    int al[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) al[i] = (int)(px[i] >> 24);
+    AlphaBlk ab = QUALITY == 3 ? dxt5a_optimal(al) : dxt5a_quick(al);
+    uint8_t *dst = J.out + 16 * (size_t)blk;
+    pack_alpha(ab, dst);
+    bool single = true;
+#pragma unroll
+    for (int i = 1; i < 16; i++) single = single && ((px[i] & 0xFFFFFF) == (px[0] & 0xFFFFFF));
+    uint2 col;
+    if (single) col = dxt1_single_color((px[0] >> 16) & 255, (px[0] >> 8) & 255, px[0] & 255);
+    else if (QUALITY == 0) col = quick_dxt1(px);
+    else {
+        struct { float4 *b; int s; __device__ float4 &operator[](int k) const { return b[k * s]; } } wp{smem + t, T};
+        col = squish_compress4(px, J.alpha_mode == 1, mk3(J.cw[0], J.cw[1], J.cw[2]), wp);
+    }
+    *reinterpret_cast<uint2 *>(dst + 8) = col;
+}
+
+template <int QUALITY>
+__global__ void __launch_bounds__(128) k_bc5(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
+    const long long gblk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    uint32_t px[16];
+    load_block(J, 4 * (blk % J.bw), 4 * (blk / J.bw), px);
+    int ch[16];
+    uint8_t *dst = J.out + 16 * (size_t)blk;
+#pragma unroll
+    for (int i = 0; i < 16; i++) ch[i] = (int)((px[i] >> 16) & 255);
+    pack_alpha(QUALITY >= 2 ? dxt5a_optimal(ch) : dxt5a_quick(ch), dst);
+#pragma unroll
+    for (int i = 0; i < 16; i++) ch[i] = (int)((px[i] >> 8) & 255);
+    pack_alpha(QUALITY >= 2 ? dxt5a_optimal(ch) : dxt5a_quick(ch), dst + 8);
+}
+
+int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t stream) {
+    if (nblocks == 0) return 0;
+    const int T = 128;
+    const size_t sm = (size_t)T * 17 * sizeof(float4);
+    const unsigned grid = (unsigned)((nblocks + T - 1) / T);
+    switch (quality) {
+        case 0: k_bc3<0><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks); break;
+        case 3: k_bc3<3><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks); break;
+        default: k_bc3<1><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks); break;
+    }
+    return launch_status();
+}
+
+int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t stream) {
+    if (nblocks == 0) return 0;
+    const int T = 128;
+    const unsigned grid = (unsigned)((nblocks + T - 1) / T);
+    if (quality >= 2) k_bc5<2><<<grid, T, 0, stream>>>(d_jobs, njobs, nblocks);
+    else k_bc5<1><<<grid, T, 0, stream>>>(d_jobs, njobs, nblocks);
+    return launch_status();
+}
+
+NTG_DEFINE_TABLE_UPLOAD(upload_tables_bc3)
+
+}  // namespace ntg

@@ -1,0 +1,92 @@
+// Device-side building blocks shared by the sm_103a kernels.
+//
+// Every kernel translation unit is compiled with --fmad=false: each product and each sum is
+// rounded on its own, as in the reference's scalar CPU code, which is what makes the encoders
+// bit-exact. Division and square root use the IEEE-rounded forms (no fast-math).
+#pragma once
+
+#include <cstdint>
+#include <cfloat>
+#include <cuda_runtime.h>
+
+#include "ntg_host_tables.h"
+
+namespace ntg {
+
+// Min/max in the two comparison forms the reference uses; they differ on NaN.
+//   ic_*: icbc::max/min and nv::max/min   (src/nvtt/icbc.h:180-190, src/nvcore/Utils.h:159-187)
+//   sq_*: std::max/std::min as squish calls them (src/nvtt/squish/maths.h)
+__device__ __forceinline__ float ic_max(float a, float b) { return (b < a) ? a : b; }
+__device__ __forceinline__ float ic_min(float a, float b) { return (a < b) ? a : b; }
+__device__ __forceinline__ float ic_clamp(float x, float a, float b) { return ic_min(ic_max(x, a), b); }
+__device__ __forceinline__ float ic_sat(float x) { return ic_clamp(x, 0.0f, 1.0f); }
+__device__ __forceinline__ float sq_max(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float sq_min(float a, float b) { return (b < a) ? b : a; }
+
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return f3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return f3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 sat3(f3 a) { return f3{ic_sat(a.x), ic_sat(a.y), ic_sat(a.z)}; }
+
+__device__ __forceinline__ int ex5(int v) { return (v << 3) | (v >> 2); }
+__device__ __forceinline__ int ex6(int v) { return (v << 2) | (v >> 4); }
+
+// Tables built on the host (ntg_host_tables.cpp) and uploaded once per device: cluster orderings,
+// 565 midpoints, single-colour tables, gamma exponent tables.
+// Each translation unit holds its own copy (no relocatable device code) and exports an uploader.
+using DeviceTables = HostTables;
+static __constant__ DeviceTables c_tab;
+#define NTG_DEFINE_TABLE_UPLOAD(fn) \
+    int fn(const HostTables &t) { return cudaMemcpyToSymbol(c_tab, &t, sizeof(t)) == cudaSuccess ? 0 : 3; }
+
+__device__ __forceinline__ void put_u16(uint8_t *p, unsigned v) { p[0] = (uint8_t)v; p[1] = (uint8_t)(v >> 8); }
+
+// D3D10 BC1 palette (src/nvtt/icbc.h:2558-2585; src/nvimage/BlockDXT.cpp:43-99).
+struct Pal8 { int r[4], g[4], b[4]; };
+__device__ __forceinline__ void palette_d3d10(unsigned c0, unsigned c1, Pal8 &p) {
+    p.r[0] = ex5((c0 >> 11) & 31); p.g[0] = ex6((c0 >> 5) & 63); p.b[0] = ex5(c0 & 31);
+    p.r[1] = ex5((c1 >> 11) & 31); p.g[1] = ex6((c1 >> 5) & 63); p.b[1] = ex5(c1 & 31);
+    if (c0 > c1) {
+        p.r[2] = (2 * p.r[0] + p.r[1]) / 3; p.g[2] = (2 * p.g[0] + p.g[1]) / 3; p.b[2] = (2 * p.b[0] + p.b[1]) / 3;
+        p.r[3] = (2 * p.r[1] + p.r[0]) / 3; p.g[3] = (2 * p.g[1] + p.g[0]) / 3; p.b[3] = (2 * p.b[1] + p.b[0]) / 3;
+    } else {
+        p.r[2] = (p.r[0] + p.r[1]) / 2; p.g[2] = (p.g[0] + p.g[1]) / 2; p.b[2] = (p.b[0] + p.b[1]) / 2;
+        p.r[3] = 0; p.g[3] = 0; p.b[3] = 0;
+    }
+}
+
+// AlphaBlockDXT5::evaluatePalette, D3D10 (src/nvimage/BlockDXT.cpp:336-378).
+__device__ __forceinline__ void alpha_palette(int a0, int a1, int pal[8]) {
+    pal[0] = a0; pal[1] = a1;
+    if (a0 > a1) {
+#pragma unroll
+        for (int k = 1; k <= 6; k++) pal[k + 1] = ((7 - k) * a0 + k * a1) / 7;
+    } else {
+#pragma unroll
+        for (int k = 1; k <= 4; k++) pal[k + 1] = ((5 - k) * a0 + k * a1) / 5;
+        pal[6] = 0; pal[7] = 255;
+    }
+}
+
+// _powf_11_5 / _powf_5_11 of src/nvmath/Gamma.cpp:311-357 (exponent table times a quartic).
+__device__ __forceinline__ float powf_11_5(float x) {
+    uint32_t u = __float_as_uint(x);
+    float m = __uint_as_float((u & 0x7FFFFFu) | (127u << 23));
+    float pm = (((-0.00916587552f * m + 0.119315466f) * m + 1.01847068f) * m - 0.158338739f) * m + 0.0297184721f;
+    return c_tab.pow_11_5[u >> 23] * pm;
+}
+__device__ __forceinline__ float powf_5_11(float x) {
+    uint32_t u = __float_as_uint(x);
+    float m = __uint_as_float((u & 0x7FFFFFu) | (127u << 23));
+    float pm = (((-0.0110083047f * m + 0.0905038750f) * m - 0.324697506f) * m + 0.876040946f) * m + 0.369160989f;
+    return c_tab.pow_5_11[u >> 23] * pm;
+}
+
+// ColorBlock::init(float) quantiser (src/nvimage/ColorBlock.cpp:103-106).
+__device__ __forceinline__ uint32_t quant_u8(float x) { return (uint32_t)(uint8_t)(255 * ic_clamp(x, 0.0f, 1.0f)); }
+
+}  // namespace ntg

@@ -1,0 +1,42 @@
+// Host-computed tables shared with the kernels (see ntg_host_tables.cpp).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+namespace ntg {
+
+// Uploaded verbatim to __constant__ memory on each device.
+struct HostTables {
+    uint32_t four[968];            // icbc 4-cluster orderings, bytes (a, b, c) = cumulative cluster ends
+    uint32_t three[152];           // icbc 3-cluster orderings, bytes (a, b)
+    int four_total[16];            // orderings available for 1..16 points
+    int three_total[16];
+    float mid5[32];                // 565 rounding midpoints
+    float mid6[64];
+    uint8_t icbc_match5[256][2];   // icbc single-colour tables (D3D10 decoder)
+    uint8_t icbc_match6[256][2];
+    uint8_t opt_match5[256][2];    // OptimalCompress single-colour tables
+    uint8_t opt_match6[256][2];
+    float pow_5_11[512];           // exponent tables of the gamma-2.2 helpers
+    float pow_11_5[512];
+};
+
+void build_device_tables(HostTables &t);
+
+// Colour transforms, 0 none / 1 power-law gamma / 2 sRGB.
+float host_to_srgb(float f);
+float host_from_srgb(float f);
+float host_xform_in(float v, int xform, float gamma, const HostTables &t);
+float host_xform_out(float v, int xform, float gamma, const HostTables &t);
+void build_input_lut(int xform, float gamma, const HostTables &t, float lut[256]);
+void build_composed_lut(int in_xform, int out_xform, float gamma, const HostTables &t, float lut[256]);
+void build_composed_lut8(int in_xform, int out_xform, float gamma, const HostTables &t, uint8_t lut8[512]);
+void build_srgb_steps(float steps[256]);
+
+// Polyphase filtering: 0 box, 1 triangle, 2 kaiser (params: alpha, stretch).
+float filter_evaluate(int filter, float width, float p0, float p1, float x);
+int polyphase_window(float width, int src_len, int dst_len);
+int build_polyphase(int filter, float width, float p0, float p1, int src_len, int dst_len, float *weights, int *lefts);
+
+}  // namespace ntg

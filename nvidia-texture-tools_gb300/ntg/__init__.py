@@ -1,0 +1,249 @@
+"""Python binding of the GB300 texture path (libntg.so, C ABI in include/ntg.h).
+
+ctypes over the C ABI; torch supplies device memory and streams. Every compute call goes to the
+CUDA kernels in libntg.so: there is no CPU fallback, and a missing or unbuildable library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "_build", "libntg.so")
+
+FORMAT_BC1, FORMAT_BC3, FORMAT_BC5 = 1, 4, 7
+QUALITY_FASTEST, QUALITY_NORMAL, QUALITY_PRODUCTION, QUALITY_HIGHEST = 0, 1, 2, 3
+WRAP_CLAMP, WRAP_REPEAT, WRAP_MIRROR = 0, 1, 2
+FILTER_BOX, FILTER_TRIANGLE, FILTER_KAISER = 0, 1, 2
+ALPHA_NONE, ALPHA_TRANSPARENCY = 0, 1
+XFORM_NONE, XFORM_GAMMA, XFORM_SRGB = 0, 1, 2
+
+BLOCK_BYTES = {FORMAT_BC1: 8, FORMAT_BC3: 16, FORMAT_BC5: 16}
+
+_vp, _i, _f, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_size_t
+
+
+class NtgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ntg error {code}: {msg}")
+        self.code = code
+
+
+class ChainOptions(ctypes.Structure):
+    """Mirror of ntg_chain_options."""
+    _fields_ = [("format", _i), ("quality", _i), ("filter", _i), ("filter_width", _f), ("params", _f * 2),
+                ("wrap", _i), ("alpha_mode", _i), ("in_xform", _i), ("out_xform", _i), ("gamma", _f),
+                ("max_levels", _i), ("weighted", _i), ("cw", _f * 3)]
+
+    @classmethod
+    def make(cls, format=FORMAT_BC1, quality=QUALITY_NORMAL, filter=FILTER_BOX, filter_width=0.0, params=(0.0, 0.0),
+             wrap=WRAP_MIRROR, alpha_mode=ALPHA_NONE, in_xform=XFORM_NONE, out_xform=XFORM_NONE, gamma=2.2,
+             max_levels=0, weighted=0, cw=(1.0, 1.0, 1.0)):
+        o = cls()
+        o.format, o.quality, o.filter, o.filter_width = format, quality, filter, filter_width
+        o.params[0], o.params[1] = params
+        o.wrap, o.alpha_mode, o.in_xform, o.out_xform, o.gamma = wrap, alpha_mode, in_xform, out_xform, gamma
+        o.max_levels, o.weighted = max_levels, weighted
+        o.cw[0], o.cw[1], o.cw[2] = cw
+        return o
+
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("ntg_build", os.path.join(PKG, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib():
+    """Loads libntg.so (building it first when absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "ntg_version": (_i, []),
+        "ntg_last_error_string": (ctypes.c_char_p, []),
+        "ntg_create": (_i, [_i, ctypes.POINTER(_vp)]),
+        "ntg_destroy": (_i, [_vp]),
+        "ntg_set_image_bgra8": (_i, [_vp, _vp, _i, _i, _i, _f, _vp, _vp]),
+        "ntg_mip_level": (_i, [_vp, _vp, _i, _i, _vp, _i, _f, _vp, _i, _i, _i, _vp]),
+        "ntg_encode": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
+        "ntg_chain_levels": (_i, [_i, _i, _i]),
+        "ntg_chain_bytes": (_sz, [_i, _i, ctypes.POINTER(ChainOptions)]),
+        "ntg_compress_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
+        "ntg_compress_chain_host": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
+        "ntg_mip_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
+        "ntg_decode": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
+        "ntg_profile_enable": (_i, [_vp, _i]),
+        "ntg_profile_read": (_i, [_vp, ctypes.POINTER(_f), ctypes.POINTER(_f)]),
+        "ntg_error_sums": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp]),
+        "ntg_host_polyphase": (_i, [_i, _f, _vp, _i, _i, _vp, _vp, _i]),
+        "ntg_host_transform_tables": (_i, [_i, _i, _f, _vp, _vp, _vp, _vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype, fn.argtypes = res, args
+    _lib = L
+    return L
+
+
+def _check(code: int):
+    if code != 0:
+        raise NtgError(code, lib().ntg_last_error_string().decode())
+
+
+def _stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def chain_levels(w: int, h: int, max_levels: int = 0):
+    out = []
+    while True:
+        out.append((w, h))
+        if (max_levels > 0 and len(out) >= max_levels) or (w == 1 and h == 1):
+            break
+        w, h = max(1, w // 2), max(1, h // 2)
+    return out
+
+
+def chain_bytes(w: int, h: int, opt: ChainOptions) -> int:
+    return int(lib().ntg_chain_bytes(w, h, ctypes.byref(opt)))
+
+
+def nblocks(w: int, h: int) -> int:
+    return ((w + 3) // 4) * ((h + 3) // 4)
+
+
+class Context:
+    """One device's tables and workspace (ntg_context)."""
+
+    def __init__(self, device: int = 0):
+        self.h = ctypes.c_void_p()
+        _check(lib().ntg_create(device, ctypes.byref(self.h)))
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib().ntg_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- device-buffer calls (torch tensors on this device) --
+    def set_image(self, bgra, w, h, in_xform=XFORM_NONE, gamma=2.2, out=None, stream=None):
+        import torch
+        out = out if out is not None else torch.empty(4 * w * h, dtype=torch.float32, device=bgra.device)
+        _check(lib().ntg_set_image_bgra8(self.h, bgra.data_ptr(), w, h, in_xform, gamma, out.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def mip_level(self, src, w, h, filter=FILTER_BOX, width=0.0, params=(0.0, 0.0), wrap=WRAP_MIRROR,
+                  alpha_mode=ALPHA_NONE, weighted=0, out=None, stream=None):
+        import torch
+        dw, dh = max(1, w // 2), max(1, h // 2)
+        out = out if out is not None else torch.empty(4 * dw * dh, dtype=torch.float32, device=src.device)
+        p = (ctypes.c_float * 2)(*params)
+        _check(lib().ntg_mip_level(self.h, src.data_ptr(), w, h, out.data_ptr(), filter, width, ctypes.cast(p, _vp),
+                                   wrap, alpha_mode, weighted, _stream_ptr(stream)))
+        return out
+
+    def encode(self, fmt, rgba, w, h, quality=QUALITY_NORMAL, alpha_mode=ALPHA_NONE, out_xform=XFORM_NONE, gamma=2.2,
+               cw=(1.0, 1.0, 1.0), out=None, stream=None):
+        import torch
+        out = out if out is not None else torch.empty(BLOCK_BYTES[fmt] * nblocks(w, h), dtype=torch.uint8, device=rgba.device)
+        c = (ctypes.c_float * 3)(*cw)
+        _check(lib().ntg_encode(self.h, fmt, rgba.data_ptr(), w, h, quality, alpha_mode, out_xform, gamma,
+                                ctypes.cast(c, _vp), out.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def compress_chain(self, bgra, w, h, opt: ChainOptions, out=None, stream=None):
+        import torch
+        out = out if out is not None else torch.empty(chain_bytes(w, h, opt), dtype=torch.uint8, device=bgra.device)
+        _check(lib().ntg_compress_chain(self.h, bgra.data_ptr(), w, h, ctypes.byref(opt), out.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def compress_chain_host(self, bgra: np.ndarray, w, h, opt: ChainOptions, out: np.ndarray | None = None, stream=None):
+        out = out if out is not None else np.empty(chain_bytes(w, h, opt), np.uint8)
+        _check(lib().ntg_compress_chain_host(self.h, bgra.ctypes.data, w, h, ctypes.byref(opt), out.ctypes.data,
+                                             _stream_ptr(stream)))
+        return out
+
+    def mip_chain(self, bgra, w, h, opt: ChainOptions, out=None, stream=None):
+        import torch
+        total = sum(4 * lw * lh for lw, lh in chain_levels(w, h, opt.max_levels))
+        out = out if out is not None else torch.empty(total, dtype=torch.float32, device=bgra.device)
+        _check(lib().ntg_mip_chain(self.h, bgra.data_ptr(), w, h, ctypes.byref(opt), out.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def profile(self, enable: bool = True):
+        _check(lib().ntg_profile_enable(self.h, int(enable)))
+
+    def profile_read(self):
+        """(mips_ms, encode_ms) of the last chain call, from events on its stream."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(lib().ntg_profile_read(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def decode(self, fmt, blocks, w, h, out=None, stream=None):
+        import torch
+        out = out if out is not None else torch.empty(4 * w * h, dtype=torch.float32, device=blocks.device)
+        _check(lib().ntg_decode(self.h, fmt, blocks.data_ptr(), w, h, out.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def error_sums(self, ref, img, w, h, alpha_mode=ALPHA_NONE, out=None, stream=None):
+        import torch
+        out = out if out is not None else torch.empty(2, dtype=torch.float64, device=ref.device)
+        _check(lib().ntg_error_sums(self.h, ref.data_ptr(), img.data_ptr(), w, h, alpha_mode, out.data_ptr(),
+                                    _stream_ptr(stream)))
+        return out
+
+
+def split_levels(flat, w, h, max_levels=0):
+    """Splits back-to-back planar levels into a list of (4, h_l, w_l) arrays/tensors."""
+    out, off = [], 0
+    for lw, lh in chain_levels(w, h, max_levels):
+        out.append(flat[off: off + 4 * lw * lh].reshape(4, lh, lw))
+        off += 4 * lw * lh
+    return out
+
+
+def split_blocks(flat, w, h, fmt, max_levels=0):
+    out, off = [], 0
+    for lw, lh in chain_levels(w, h, max_levels):
+        n = BLOCK_BYTES[fmt] * nblocks(lw, lh)
+        out.append(flat[off: off + n])
+        off += n
+    return out
+
+
+def host_polyphase(filter, width, params, src, dst):
+    ws = lib().ntg_host_polyphase(filter, width, None, src, dst, None, None, 0)
+    w = np.zeros(ws * dst, np.float32)
+    left = np.zeros(dst, np.int32)
+    p = (ctypes.c_float * 2)(*params)
+    lib().ntg_host_polyphase(filter, width, ctypes.cast(p, _vp), src, dst, w.ctypes.data, left.ctypes.data, w.size)
+    return w.reshape(dst, ws), left
+
+
+def host_transform_tables(in_xform, out_xform, gamma=2.2):
+    lut_in = np.zeros(256, np.float32)
+    comp = np.zeros(256, np.float32)
+    lut8 = np.zeros(512, np.uint8)
+    steps = np.zeros(256, np.float32)
+    lib().ntg_host_transform_tables(in_xform, out_xform, gamma, lut_in.ctypes.data, comp.ctypes.data, lut8.ctypes.data,
+                                    steps.ctypes.data)
+    return lut_in, comp, lut8, steps

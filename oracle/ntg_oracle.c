@@ -836,7 +836,7 @@ void ora_dxt1_single_color(int r, int g, int b, uint8_t *out8) {
 }
 
 /* ------------------------------------------------------------------------------------------ */
-/* squish weighted cluster fit (BC3 colour), scalar build                                      */
+/* squish weighted cluster fit (BC3 colour), scalar build                                       */
 
 /* ColourSet (src/nvtt/squish/colourset.cpp:35-139, no minimal set), WeightedClusterFit::
  * SetColourSet (src/nvtt/squish/weightedclusterfit.cpp:39-105), ComputeWeightedCovariance /
@@ -853,19 +853,38 @@ static int float_to_565(v3 c) {
 }
 
 static void squish_compress4(const uint8_t *bgra, int weight_by_alpha, v3 metric, uint8_t *out8) {
+    /* ColourSet with the header's default createMinimalSet = true
+     * (src/nvtt/squish/colourset.h:40, src/nvtt/squish/colourset.cpp:44-90): texels with equal RGB
+     * bytes share one point whose weight is the sum of theirs, points in first-occurrence order. */
     v3 pts[16];
     float wts[16];
+    int remap[16];
+    int count = 0;
     for (int i = 0; i < 16; i++) {
-        pts[i] = mk3((float)bgra[4 * i + 2] / 255.0f, (float)bgra[4 * i + 1] / 255.0f, (float)bgra[4 * i + 0] / 255.0f);
-        wts[i] = weight_by_alpha ? (float)(bgra[4 * i + 3] + 1) / 256.0f : 1.0f;
+        const float wi = weight_by_alpha ? (float)(bgra[4 * i + 3] + 1) / 256.0f : 1.0f;
+        for (int j = 0;; ++j) {
+            if (j == i) {
+                pts[count] = mk3((float)bgra[4 * i + 2] / 255.0f, (float)bgra[4 * i + 1] / 255.0f, (float)bgra[4 * i + 0] / 255.0f);
+                wts[count] = wi;
+                remap[i] = count;
+                ++count;
+                break;
+            }
+            if (bgra[4 * i] == bgra[4 * j] && bgra[4 * i + 1] == bgra[4 * j + 1] && bgra[4 * i + 2] == bgra[4 * j + 2]) {
+                const int index = remap[j];
+                wts[index] += wi;
+                remap[i] = index;
+                break;
+            }
+        }
     }
     /* weighted covariance */
     float total = 0.0f;
     v3 cen = mk3(0, 0, 0);
-    for (int i = 0; i < 16; i++) { total += wts[i]; cen = add3(cen, scl3(pts[i], wts[i])); }
+    for (int i = 0; i < count; i++) { total += wts[i]; cen = add3(cen, scl3(pts[i], wts[i])); }
     cen = scl3(cen, 1.0f / total);
     float m[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < count; i++) {
         v3 a = mul3(sub3(pts[i], cen), metric);
         v3 b = scl3(a, wts[i]);
         m[0] += a.x * b.x; m[1] += a.x * b.y; m[2] += a.x * b.z;
@@ -887,8 +906,8 @@ static void squish_compress4(const uint8_t *bgra, int weight_by_alpha, v3 metric
     /* order along the axis (stable) */
     int order[16];
     float dps[16];
-    for (int i = 0; i < 16; i++) { dps[i] = dot3(pts[i], v); order[i] = i; }
-    for (int i = 0; i < 16; i++)
+    for (int i = 0; i < count; i++) { dps[i] = dot3(pts[i], v); order[i] = i; }
+    for (int i = 0; i < count; i++)
         for (int j = i; j > 0 && dps[j] < dps[j - 1]; --j) {
             float t = dps[j]; dps[j] = dps[j - 1]; dps[j - 1] = t;
             int o = order[j]; order[j] = order[j - 1]; order[j - 1] = o;
@@ -897,20 +916,19 @@ static void squish_compress4(const uint8_t *bgra, int weight_by_alpha, v3 metric
     float ww[17];
     v3 xsum = mk3(0, 0, 0);
     float wsum = 0.0f;
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < count; i++) {
         int p = order[i];
         wp[i] = scl3(pts[p], wts[p]);
         xsum = add3(xsum, wp[i]);
         ww[i] = wts[p];
         wsum += ww[i];
     }
-    wp[16] = mk3(0, 0, 0); ww[16] = 0.0f; /* read past the end by the loop tails, never used */
+    for (int i = count; i < 17; i++) { wp[i] = mk3(0, 0, 0); ww[i] = 0.0f; } /* read by loop tails, never used */
     v3 msq = mul3(metric, metric);
 
     float besterr = FLT_MAX;
     v3 bs = mk3(0, 0, 0), be = mk3(0, 0, 0);
     int b0 = 0, b1 = 0, b2 = 0;
-    const int count = 16;
     v3 x0 = mk3(0, 0, 0);
     float w0 = 0.0f;
     for (int c0 = 0; c0 <= count; c0++) {
@@ -946,11 +964,12 @@ static void squish_compress4(const uint8_t *bgra, int weight_by_alpha, v3 metric
         x0 = add3(x0, wp[c0]);
         w0 += ww[c0];
     }
-    uint8_t sorted_idx[16], idx[16];
+    uint8_t point_idx[16], idx[16];
     if (!(besterr < FLT_MAX)) { memset(out8, 0, 8); return; }
-    for (int i = 0; i < 16; i++)
-        sorted_idx[i] = i < b0 ? 0 : (i < b0 + b1 ? 2 : (i < b0 + b1 + b2 ? 3 : 1));
-    for (int i = 0; i < 16; i++) idx[order[i]] = sorted_idx[i];
+    /* cluster sizes -> point indices -> texel indices (ColourSet::RemapIndices) */
+    for (int i = 0; i < count; i++)
+        point_idx[order[i]] = i < b0 ? 0 : (i < b0 + b1 ? 2 : (i < b0 + b1 + b2 ? 3 : 1));
+    for (int i = 0; i < 16; i++) idx[i] = point_idx[remap[i]];
     int a = float_to_565(bs), b = float_to_565(be);
     uint8_t rem[16];
     if (a < b) { int t = a; a = b; b = t; for (int i = 0; i < 16; i++) rem[i] = (idx[i] ^ 1) & 3; }
@@ -1607,4 +1626,44 @@ int ora_rms(int format, const float *ref, const uint8_t *blocks, int w, int h, i
     *rms_alpha = (float)sqrt(msa / n);
     free(dec);
     return 0;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Check of a toSrgb quantiser step table: counts the floats in [0, 2] whose 8-bit code by
+ * counting steps differs from uint8(255 * clamp(toSrgb(x), 0, 1)) computed directly. */
+typedef struct { const float *steps; uint32_t lo, hi; long long bad; } srgb_scan_t;
+
+static int srgb_code(float x) {
+    float s;
+    ora_to_srgb(&x, &s, 1);
+    return (int)(uint8_t)(255 * ic_clamp(s, 0.0f, 1.0f));
+}
+
+static void *srgb_scan(void *p) {
+    srgb_scan_t *t = (srgb_scan_t *)p;
+    for (uint32_t b = t->lo; b < t->hi; b++) {
+        const float x = u2f(b);
+        int k = 0;
+        while (k < 255 && t->steps[k + 1] <= x) k++;
+        if (k != srgb_code(x)) t->bad++;
+    }
+    return NULL;
+}
+
+long long ora_count_srgb_step_mismatches(const float *steps, int threads) {
+    const uint32_t hi = f2u(2.0f) + 1;
+    if (threads < 1) threads = 1;
+    if (threads > 64) threads = 64;
+    pthread_t th[64];
+    srgb_scan_t jobs[64];
+    for (int i = 0; i < threads; i++) {
+        jobs[i].steps = steps;
+        jobs[i].lo = (uint32_t)((uint64_t)hi * i / threads);
+        jobs[i].hi = (uint32_t)((uint64_t)hi * (i + 1) / threads);
+        jobs[i].bad = 0;
+        pthread_create(&th[i], NULL, srgb_scan, &jobs[i]);
+    }
+    long long bad = 0;
+    for (int i = 0; i < threads; i++) { pthread_join(th[i], NULL); bad += jobs[i].bad; }
+    return bad;
 }

@@ -80,6 +80,9 @@ int ora_decode(int format, const uint8_t *blocks, int w, int h, float *rgba);
 int ora_rms(int format, const float *rgba, const uint8_t *blocks, int w, int h, int alpha_mode,
             float *rms_color, float *rms_alpha);
 
+/* Number of floats in [0, 2] where counting `steps` disagrees with toSrgb + ColorBlock quantiser. */
+long long ora_count_srgb_step_mismatches(const float *steps, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,11 @@ class Oracle:
         self._from_srgb = _bind(lib, "ora_from_srgb", None, [_vp, _vp, _i])
         self._decode = _bind(lib, "ora_decode", _i, [_i, _vp, _i, _i, _vp])
         self._rms = _bind(lib, "ora_rms", _i, [_i, _vp, _vp, _i, _i, _i, _vp, _vp])
+        self._srgb_check = _bind(lib, "ora_count_srgb_step_mismatches", _ll, [_vp, _i])
+
+    def count_srgb_step_mismatches(self, steps, threads=8):
+        s = np.ascontiguousarray(steps, np.float32)
+        return self._srgb_check(_ptr(s), threads)
 
     # -- blocks --
     def bc1_block(self, level, colors, weights, cw=(1, 1, 1), three=1, black=1):

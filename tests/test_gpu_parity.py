@@ -1,0 +1,231 @@
+"""GPU parity: every kernel of libntg.so, called through its C ABI, against the oracle (the C
+restatement pinned to the reference) on the same seeded inputs. Bit-exact everywhere except
+where noted (sRGB output transform on float BC1 levels uses the device's powf)."""
+import numpy as np
+import pytest
+
+import ntg
+import ntg.synth as synth
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def float_image(w, h, seed, lo=0.0, hi=1.0, alpha_zero_frac=0.0):
+    rng = np.random.default_rng(seed)
+    img = (rng.random(4 * w * h) * (hi - lo) + lo).astype(np.float32)
+    if alpha_zero_frac:
+        a = img[3 * w * h:]
+        a[rng.random(w * h) < alpha_zero_frac] = 0.0
+    return img
+
+
+def blocky_image(w, h, seed):
+    """A float image tiled from the synthetic 4x4 block kinds (flat, few-colour, gradients, noise)."""
+    bw, bh = (w + 3) // 4, (h + 3) // 4
+    blocks = synth.random_blocks(bw * bh, seed).reshape(bh, bw, 4, 4, 4).astype(np.float32) / 255.0
+    img = blocks.transpose(0, 2, 1, 3, 4).reshape(bh * 4, bw * 4, 4)[:h, :w]
+    bgra_planar = img.transpose(2, 0, 1)  # b, g, r, a planes
+    return np.concatenate([bgra_planar[2].ravel(), bgra_planar[1].ravel(), bgra_planar[0].ravel(),
+                           bgra_planar[3].ravel()]).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------------------------
+# block encoders
+
+@pytest.mark.parametrize("quality", [0, 1, 2])
+@pytest.mark.parametrize("alpha_mode", [0, 1])
+def test_bc1_encode_matches_oracle(ctx, oracle, quality, alpha_mode):
+    for (w, h, seed) in [(64, 64, 1), (37, 23, 2), (4, 4, 3), (1, 1, 4), (2, 7, 5)]:
+        for img in (float_image(w, h, seed, alpha_zero_frac=0.2), blocky_image(w, h, seed + 50),
+                    float_image(w, h, seed + 9, lo=-0.2, hi=1.3)):
+            ours = host(ctx.encode(ntg.FORMAT_BC1, dev(img), w, h, quality=quality, alpha_mode=alpha_mode))
+            ref = oracle.bc1_image(img, w, h, alpha_mode, quality, threads=4)
+            assert np.array_equal(ours, ref), (w, h, seed)
+
+
+def test_bc1_colour_weights_and_nan(ctx, oracle):
+    w, h = 32, 16
+    img = float_image(w, h, 77)
+    img[5] = np.nan
+    img[w * h + 40] = np.inf
+    for cw in [(1.0, 1.0, 1.0), (0.3, 0.59, 0.11), (2.0, 0.5, 1.0)]:
+        ours = host(ctx.encode(ntg.FORMAT_BC1, dev(img), w, h, quality=1, cw=cw))
+        assert np.array_equal(ours, oracle.bc1_image(img, w, h, 0, 1, cw=cw, threads=4))
+
+
+@pytest.mark.parametrize("quality", [0, 1, 2, 3])
+@pytest.mark.parametrize("alpha_mode", [0, 1])
+def test_bc3_encode_matches_oracle(ctx, oracle, quality, alpha_mode):
+    for (w, h, seed) in [(64, 32, 1), (13, 7, 2), (3, 5, 3), (1, 1, 4)]:
+        for img in (float_image(w, h, seed, alpha_zero_frac=0.3), blocky_image(w, h, seed + 20),
+                    float_image(w, h, seed + 5, lo=-0.3, hi=1.4)):
+            ours = host(ctx.encode(ntg.FORMAT_BC3, dev(img), w, h, quality=quality, alpha_mode=alpha_mode))
+            ref = oracle.bc3_image(img, w, h, alpha_mode, quality, threads=4)
+            assert np.array_equal(ours, ref), (w, h, seed)
+
+
+@pytest.mark.parametrize("quality", [1, 2])
+def test_bc5_encode_matches_oracle(ctx, oracle, quality):
+    for (w, h, seed) in [(64, 32, 1), (13, 7, 2), (1, 3, 3)]:
+        for img in (float_image(w, h, seed), blocky_image(w, h, seed + 7)):
+            ours = host(ctx.encode(ntg.FORMAT_BC5, dev(img), w, h, quality=quality))
+            assert np.array_equal(ours, oracle.bc5_image(img, w, h, quality, threads=4))
+
+
+@pytest.mark.parametrize("fmt", [ntg.FORMAT_BC1, ntg.FORMAT_BC3])
+@pytest.mark.parametrize("out_xform", [ntg.XFORM_GAMMA, ntg.XFORM_SRGB])
+def test_encode_with_output_transform(ctx, oracle, fmt, out_xform):
+    """Compressor::compress after toGamma(2.2) / toSrgb of the level (BC3: exact via the quantiser
+    tables; BC1 sRGB: the device powf, compared by decoded error)."""
+    w, h = 48, 24
+    img = float_image(w, h, 31)
+    enc = img.copy()
+    n = w * h
+    enc[:3 * n] = oracle.powf_5_11(img[:3 * n]) if out_xform == ntg.XFORM_GAMMA else oracle.to_srgb(img[:3 * n])
+    ours = host(ctx.encode(fmt, dev(img), w, h, quality=1, out_xform=out_xform, gamma=2.2))
+    ref = oracle.bc1_image(enc, w, h, 0, 1, threads=4) if fmt == 1 else oracle.bc3_image(enc, w, h, 0, 1, threads=4)
+    if fmt == ntg.FORMAT_BC1 and out_xform == ntg.XFORM_SRGB:
+        rc, _ = oracle.rms(fmt, enc, ref, w, h)
+        oc, _ = oracle.rms(fmt, enc, ours, w, h)
+        assert oc <= rc * 1.005 + 1e-7
+    else:
+        assert np.array_equal(ours, ref)
+
+
+# ---------------------------------------------------------------------------------------------
+# mip filtering
+
+@pytest.mark.parametrize("size", [(64, 64), (33, 17), (1, 9), (9, 1), (2, 2), (5, 7), (128, 32)])
+@pytest.mark.parametrize("filt", [ntg.FILTER_BOX, ntg.FILTER_TRIANGLE, ntg.FILTER_KAISER])
+def test_mip_level_matches_oracle(ctx, oracle, size, filt):
+    w, h = size
+    params = (4.0, 1.0)
+    for wrap in (0, 1, 2):
+        for am in (0, 1):
+            img = float_image(w, h, w * 7 + h + wrap, lo=-0.1, hi=1.1)
+            ours = host(ctx.mip_level(dev(img), w, h, filter=filt, params=params, wrap=wrap, alpha_mode=am))
+            dw, dh = max(1, w // 2), max(1, h // 2)
+            width = {0: 0.5, 1: 1.0, 2: 3.0}[filt]
+            if filt == 0 and am == 0:
+                ref = oracle.fast_downsample(img, w, h)
+            else:
+                ref = oracle.resize(img, w, h, dw, dh, filt, width, 4.0, 1.0, wrap)
+            assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), (size, filt, wrap, am)
+
+
+@pytest.mark.parametrize("filt", [ntg.FILTER_TRIANGLE, ntg.FILTER_KAISER])
+def test_weighted_mip_level_matches_oracle(ctx, oracle, filt):
+    for (w, h) in [(32, 32), (17, 9), (64, 16)]:
+        img = float_image(w, h, 3 + w, alpha_zero_frac=0.3)
+        width = 1.0 if filt == 1 else 3.0
+        ours = host(ctx.mip_level(dev(img), w, h, filter=filt, params=(4.0, 1.0), wrap=2, weighted=1))
+        ref = oracle.resize_weighted(img, w, h, max(1, w // 2), max(1, h // 2), filt, width, 4.0, 1.0, 2)
+        assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
+CHAINS = [
+    # (w, h, format, quality, filter, alpha_mode, in_xform, out_xform, wrap)
+    (128, 128, 1, 1, 0, 0, 0, 0, 2),    # the box/BC1/linear workload at reduced size
+    (256, 256, 4, 1, 2, 1, 2, 2, 2),    # the Kaiser/sRGB/BC3/transparency workload at reduced size
+    (64, 32, 7, 1, 1, 0, 0, 0, 1),      # BC5 normal map, triangle
+    (96, 40, 4, 1, 1, 1, 1, 1, 0),      # gamma 2.2, triangle, clamp
+    (37, 19, 1, 1, 2, 0, 1, 1, 2),      # odd sizes, Kaiser, BC1 + gamma
+    (1, 64, 4, 1, 0, 1, 0, 0, 2),       # 1-D, box polyphase (transparency)
+    (64, 1, 1, 0, 0, 0, 0, 0, 2),       # 1-D fast box, range fit
+    (31, 31, 4, 3, 2, 0, 2, 2, 1),      # odd, Highest quality alpha
+]
+
+
+def oracle_chain(oracle, bgra, w, h, fmt, quality, filt, am, ix, ox, wrap):
+    width = {0: 0.5, 1: 1.0, 2: 3.0}[filt]
+    lin, enc = oracle.mip_chain(bgra, w, h, filt, width, 4.0, 1.0, wrap, am, ix, ox, 2.2)
+    out = []
+    for l in enc:
+        lw, lh = l.shape[2], l.shape[1]
+        flat = l.reshape(-1)
+        if fmt == 1:
+            out.append(oracle.bc1_image(flat, lw, lh, am, quality, threads=8))
+        elif fmt == 4:
+            out.append(oracle.bc3_image(flat, lw, lh, am, quality, threads=8))
+        else:
+            out.append(oracle.bc5_image(flat, lw, lh, quality, threads=8))
+    return lin, np.concatenate(out)
+
+
+@pytest.mark.parametrize("case", CHAINS)
+def test_chain_matches_oracle(ctx, oracle, case):
+    w, h, fmt, quality, filt, am, ix, ox, wrap = case
+    if fmt == 7:
+        bgra = synth.normal_map(w, h, 5)
+    else:
+        bgra = synth.colour_texture(w, h, 11, scale=max(1.0, w / 512),
+                                    alpha=synth.alpha_field(w, h, 11) if am else None)
+    opt = ntg.ChainOptions.make(format=fmt, quality=quality, filter=filt, wrap=wrap, alpha_mode=am, in_xform=ix,
+                                out_xform=ox, gamma=2.2)
+    d_bgra = dev(bgra)
+    levels = host(ctx.mip_chain(d_bgra, w, h, opt))
+    blocks = host(ctx.compress_chain(d_bgra, w, h, opt))
+    lin, ref_blocks = oracle_chain(oracle, bgra, w, h, fmt, quality, filt, am, ix, ox, wrap)
+    ref_levels = np.concatenate([l.reshape(-1) for l in lin])
+    assert np.array_equal(levels.view(np.uint32), ref_levels.view(np.uint32))
+    assert np.array_equal(blocks, ref_blocks)
+
+
+def test_chain_host_variant_matches_device_variant(ctx):
+    w, h = 200, 120
+    bgra = synth.colour_texture(w, h, 3, alpha=synth.alpha_field(w, h, 3))
+    opt = ntg.ChainOptions.make(format=4, quality=1, filter=2, alpha_mode=1, in_xform=2, out_xform=2)
+    a = host(ctx.compress_chain(dev(bgra), w, h, opt))
+    b = ctx.compress_chain_host(bgra, w, h, opt)
+    assert np.array_equal(a, b)
+
+
+def test_chain_golden_fixture(ctx):
+    """The GPU chain against the reference's own bytes (tests/golden/chain_c0.npz)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "chain_c0.npz"))
+    w, h = int(g["w"]), int(g["h"])
+    opt = ntg.ChainOptions.make(format=1, quality=1, filter=0)
+    out = host(ctx.compress_chain(dev(g["image"]), w, h, opt))
+    assert np.array_equal(out, g["blocks"])
+
+
+# ---------------------------------------------------------------------------------------------
+# decode and error
+
+@pytest.mark.parametrize("fmt", [1, 4, 7])
+def test_decode_and_error_sums(ctx, oracle, fmt):
+    w, h = 45, 27
+    img = float_image(w, h, fmt)
+    blocks = oracle.bc1_image(img, w, h) if fmt == 1 else (oracle.bc3_image(img, w, h, 1) if fmt == 4 else oracle.bc5_image(img, w, h))
+    dec = host(ctx.decode(fmt, dev(blocks), w, h))
+    assert np.array_equal(dec.view(np.uint32), oracle.decode(fmt, blocks, w, h).view(np.uint32))
+    am = 1 if fmt == 4 else 0
+    sums = host(ctx.error_sums(dev(img), dev(dec), w, h, alpha_mode=am))
+    rc, ra = oracle.rms(fmt, img, blocks, w, h, am)
+    assert abs(np.sqrt(sums[0] / (w * h)) - rc) <= 1e-6 * max(1.0, rc)
+    assert abs(np.sqrt(sums[1] / (w * h)) - ra) <= 1e-6 * max(1.0, ra)
+
+
+# ---------------------------------------------------------------------------------------------
+# errors are reported, not hidden
+
+def test_invalid_arguments_report_errors(ctx):
+    opt = ntg.ChainOptions.make(format=2)  # BC1a is outside the path
+    with pytest.raises(ntg.NtgError) as e:
+        ctx.compress_chain(dev(np.zeros((4, 4, 4), np.uint8)), 4, 4, opt)
+    assert e.value.code == 2
+    with pytest.raises(ntg.NtgError) as e:
+        ctx.mip_level(dev(np.zeros(4, np.float32)), 1, 1)
+    assert e.value.code == 1
