@@ -41,6 +41,9 @@ WORKLOADS = {
     "c1": (4096, 4096, 4, 1, 2, 1, 2, 2,
            "4096x4096 RGBA8 sRGB, Kaiser(w3,a4,s1) mips, transparency, BC3 Normal, 13 levels"),
     "c0": (512, 512, 1, 1, 0, 0, 0, 0, "512x512 RGBA8 linear, box mips, BC1 Normal, 10 levels"),
+    # reduced-size variant of c1 for profiler captures (same kernels, a quarter of the texels)
+    "c1_2k": (2048, 2048, 4, 1, 2, 1, 2, 2,
+              "2048x2048 RGBA8 sRGB, Kaiser(w3,a4,s1) mips, transparency, BC3 Normal, 12 levels"),
 }
 
 # FP32 operations of one cluster-split evaluation of squish's WeightedClusterFit::Compress4
@@ -147,7 +150,7 @@ def max_over_ranks(world, value, device=None):
 def workload_texture(name):
     import ntg.synth as synth
     w, h = WORKLOADS[name][:2]
-    if name == "c1":
+    if name.startswith("c1"):
         return synth.texture_c1(w=w, h=h)
     return synth.texture_c0(w=w, h=h)
 

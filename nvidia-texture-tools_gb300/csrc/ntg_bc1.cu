@@ -242,63 +242,77 @@ __device__ __forceinline__ float cf_eval(f3 ax, f3 sum, float a2, float b2, floa
     return dot(e1, metric);
 }
 
-// cluster_fit_four (src/nvtt/icbc.h:2250-2549): all orderings of n points; the first strict
-// minimum wins, as in the scalar build.
-__device__ void cluster_fit_four(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
-    float4 s = sat[n - 1];
-    f3 sum = xyz(s);
-    float wsum = s.w;
-    float best = FLT_MAX;
-    f3 bs = mk3(0, 0, 0), be = mk3(0, 0, 0);
-    const int total = c_tab.four_total[n - 1];
-    for (int i = 0; i < total; i++) {
-        uint32_t o = c_tab.four[i];
-        int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1, c2 = (int)((o >> 16) & 255) - 1;
-        float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
-        float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
-        float4 v2 = c2 >= 0 ? sat[c2] : make_float4(0, 0, 0, 0);
-        float w0 = v0.w, w1 = v1.w, w2 = v2.w;
-        float w3 = wsum - w2;
-        f3 x0 = xyz(v0), x1 = xyz(v1) - x0, x2 = xyz(v2) - xyz(v1);
-        w2 = w2 - w1;
-        w1 = w1 - w0;
-        float a2 = w2 * (1.0f / 9.0f) + (w1 * (4.0f / 9.0f) + w0);
-        float b2 = w1 * (1.0f / 9.0f) + (w2 * (4.0f / 9.0f) + w3);
-        float ab = (w1 + w2) * (2.0f / 9.0f);
-        f3 ax = (x2 * (1.0f / 3.0f)) + ((x1 * (2.0f / 3.0f)) + x0);
-        f3 a, b;
-        float e = cf_eval(ax, sum, a2, b2, ab, metric, a, b);
-        if (e < best) { best = e; bs = a; be = b; }
-    }
-    start = bs; end = be;
+// One ordering of cluster_fit_four (src/nvtt/icbc.h:2250-2549): cumulative cluster ends from the
+// SAT, solve, snap, residual.
+__device__ __forceinline__ float four_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
+                                           f3 &b) {
+    const int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1, c2 = (int)((o >> 16) & 255) - 1;
+    const float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
+    const float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
+    const float4 v2 = c2 >= 0 ? sat[c2] : make_float4(0, 0, 0, 0);
+    float w0 = v0.w, w1 = v1.w, w2 = v2.w;
+    const float w3 = wsum - w2;
+    const f3 x0 = xyz(v0), x1 = xyz(v1) - x0, x2 = xyz(v2) - xyz(v1);
+    w2 = w2 - w1;
+    w1 = w1 - w0;
+    const float a2 = w2 * (1.0f / 9.0f) + (w1 * (4.0f / 9.0f) + w0);
+    const float b2 = w1 * (1.0f / 9.0f) + (w2 * (4.0f / 9.0f) + w3);
+    const float ab = (w1 + w2) * (2.0f / 9.0f);
+    const f3 ax = (x2 * (1.0f / 3.0f)) + ((x1 * (2.0f / 3.0f)) + x0);
+    return cf_eval(ax, sum, a2, b2, ab, metric, a, b);
 }
 
-// cluster_fit_three (src/nvtt/icbc.h:2016-2247)
-__device__ void cluster_fit_three(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
-    float4 s = sat[n - 1];
-    f3 sum = xyz(s);
-    float wsum = s.w;
+// The first strict minimum over all orderings wins, as in the scalar build. The search keeps the
+// index of the best ordering; its endpoints are recomputed once at the end.
+__device__ void cluster_fit_four(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
+    const float4 s = sat[n - 1];
+    const f3 sum = xyz(s);
+    const float wsum = s.w;
     float best = FLT_MAX;
-    f3 bs = mk3(0, 0, 0), be = mk3(0, 0, 0);
+    int bi = -1;
+    const int total = c_tab.four_total[n - 1];
+    for (int i = 0; i < total; i++) {
+        f3 a, b;
+        const float e = four_eval(sat, c_tab.four[i], sum, wsum, metric, a, b);
+        if (e < best) { best = e; bi = i; }
+    }
+    start = mk3(0, 0, 0);
+    end = mk3(0, 0, 0);
+    if (bi >= 0) four_eval(sat, c_tab.four[bi], sum, wsum, metric, start, end);
+}
+
+// One ordering of cluster_fit_three (src/nvtt/icbc.h:2016-2247).
+__device__ __forceinline__ float three_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
+                                            f3 &b) {
+    const int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1;
+    const float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
+    const float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
+    float w0 = v0.w, w1 = v1.w;
+    const float w2 = wsum - w1;
+    const f3 x0 = xyz(v0), x1 = xyz(v1) - x0;
+    w1 = w1 - w0;
+    const float ab = w1 * 0.25f;
+    const float a2 = w0 + ab;
+    const float b2 = w2 + ab;
+    const f3 ax = x0 + (x1 * 0.5f);
+    return cf_eval(ax, sum, a2, b2, ab, metric, a, b);
+}
+
+__device__ void cluster_fit_three(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
+    const float4 s = sat[n - 1];
+    const f3 sum = xyz(s);
+    const float wsum = s.w;
+    float best = FLT_MAX;
+    int bi = -1;
     const int total = c_tab.three_total[n - 1];
     for (int i = 0; i < total; i++) {
-        uint32_t o = c_tab.three[i];
-        int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1;
-        float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
-        float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
-        float w0 = v0.w, w1 = v1.w;
-        float w2 = wsum - w1;
-        f3 x0 = xyz(v0), x1 = xyz(v1) - x0;
-        w1 = w1 - w0;
-        float ab = w1 * 0.25f;
-        float a2 = w0 + ab;
-        float b2 = w2 + ab;
-        f3 ax = x0 + (x1 * 0.5f);
         f3 a, b;
-        float e = cf_eval(ax, sum, a2, b2, ab, metric, a, b);
-        if (e < best) { best = e; bs = a; be = b; }
+        const float e = three_eval(sat, c_tab.three[i], sum, wsum, metric, a, b);
+        if (e < best) { best = e; bi = i; }
     }
-    start = bs; end = be;
+    start = mk3(0, 0, 0);
+    end = mk3(0, 0, 0);
+    if (bi >= 0) three_eval(sat, c_tab.three[bi], sum, wsum, metric, start, end);
 }
 
 // refine_endpoints (src/nvtt/icbc.h:3329-3406), including the reference's use of the current
@@ -518,12 +532,11 @@ int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, 
     const int T = 64;
     const size_t sm = (size_t)T * (48 * sizeof(float4) + 16 * sizeof(float));
     const unsigned grid = (unsigned)((nblocks + T - 1) / T);
-    static bool attrs = false;
-    if (!attrs) {  // the per-thread arrays exceed the 48 KB default of dynamic shared memory
+    static std::atomic<unsigned long long> configured{0};
+    if (first_use_on_device(configured)) {  // the per-thread arrays exceed the 48 KB default
         cudaFuncSetAttribute(k_bc1<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         cudaFuncSetAttribute(k_bc1<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         cudaFuncSetAttribute(k_bc1<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        attrs = true;
     }
     if (quality == 0) k_bc1<0><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks);
     else if (quality == 2) k_bc1<8><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks);

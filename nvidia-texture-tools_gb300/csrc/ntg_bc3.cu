@@ -281,48 +281,76 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
     wp[16] = make_float4(0, 0, 0, 0);
     const f3 msq = metric * metric;
 
+    // The split search keeps only the best error and its cluster sizes; the endpoints of the
+    // winner are recomputed afterwards with the same sequence of operations.
     float besterr = FLT_MAX;
-    f3 bs = mk3(0, 0, 0), be = mk3(0, 0, 0);
     int b0 = 0, b1 = 0, b2 = 0;
     f3 x0 = mk3(0, 0, 0);
     float w0 = 0.0f;
     for (int c0 = 0; c0 <= count; c0++) {
         f3 x1 = mk3(0, 0, 0);
         float w1 = 0.0f;
+        const float t01 = w0;  // loop invariants of the inner loops, same operands and order
         for (int c1 = 0; c1 <= count - c0; c1++) {
             f3 x2 = mk3(0, 0, 0);
             float w2 = 0.0f;
+            const float wr = wsum - w0 - w1;
+            const float a2p = t01 + w1 * (4.0f / 9.0f);
+            const float w1n = w1 * (1.0f / 9.0f);
+            const f3 axp = x0 + (x1 * (2.0f / 3.0f));
             for (int c2 = 0; c2 <= count - c0 - c1; c2++) {
-                float w3 = wsum - w0 - w1 - w2;
-                float a2 = w0 + w1 * (4.0f / 9.0f) + w2 * (1.0f / 9.0f);
-                float b2s = w3 + w2 * (4.0f / 9.0f) + w1 * (1.0f / 9.0f);
-                float ab = (w1 + w2) * (2.0f / 9.0f);
-                float f = 1.0f / (a2 * b2s - ab * ab);
-                f3 ax = (x0 + (x1 * (2.0f / 3.0f))) + (x2 * (1.0f / 3.0f));
-                f3 bx = xsum - ax;
+                const float w3 = wr - w2;
+                const float a2 = a2p + w2 * (1.0f / 9.0f);
+                const float b2s = w3 + w2 * (4.0f / 9.0f) + w1n;
+                const float ab = (w1 + w2) * (2.0f / 9.0f);
+                const float f = 1.0f / (a2 * b2s - ab * ab);
+                const f3 ax = axp + (x2 * (1.0f / 3.0f));
+                const f3 bx = xsum - ax;
                 f3 a = ((ax * b2s) - (bx * ab)) * f;
                 f3 b = ((bx * a2) - (ax * ab)) * f;
                 a = mk3(sq_min(1.0f, sq_max(0.0f, a.x)), sq_min(1.0f, sq_max(0.0f, a.y)), sq_min(1.0f, sq_max(0.0f, a.z)));
                 b = mk3(sq_min(1.0f, sq_max(0.0f, b.x)), sq_min(1.0f, sq_max(0.0f, b.y)), sq_min(1.0f, sq_max(0.0f, b.z)));
                 a = mk3(floorf(31.0f * a.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * a.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * a.z + 0.5f) * (1.0f / 31.0f));
                 b = mk3(floorf(31.0f * b.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * b.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * b.z + 0.5f) * (1.0f / 31.0f));
-                f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
-                f3 e1 = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
-                float err = dot(e1, msq);
-                if (err < besterr) { besterr = err; bs = a; be = b; b0 = c0; b1 = c1; b2 = c2; }
-                float4 q = wp[c0 + c1 + c2];
+                const f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
+                const f3 e1 = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
+                const float err = dot(e1, msq);
+                if (err < besterr) { besterr = err; b0 = c0; b1 = c1; b2 = c2; }
+                const float4 q = wp[c0 + c1 + c2];
                 x2 = x2 + mk3(q.x, q.y, q.z);
                 w2 += q.w;
             }
-            float4 q = wp[c0 + c1];
+            const float4 q = wp[c0 + c1];
             x1 = x1 + mk3(q.x, q.y, q.z);
             w1 += q.w;
         }
-        float4 q = wp[c0];
+        const float4 q = wp[c0];
         x0 = x0 + mk3(q.x, q.y, q.z);
         w0 += q.w;
     }
     if (!(besterr < FLT_MAX)) return make_uint2(0, 0);
+    f3 bs, be;
+    {
+        // the running sums of the winning split, accumulated exactly as the search did
+        f3 x0b = mk3(0, 0, 0), x1b = mk3(0, 0, 0), x2b = mk3(0, 0, 0);
+        float w0b = 0.0f, w1b = 0.0f, w2b = 0.0f;
+        for (int i = 0; i < b0; i++) { const float4 q = wp[i]; x0b = x0b + mk3(q.x, q.y, q.z); w0b += q.w; }
+        for (int i = b0; i < b0 + b1; i++) { const float4 q = wp[i]; x1b = x1b + mk3(q.x, q.y, q.z); w1b += q.w; }
+        for (int i = b0 + b1; i < b0 + b1 + b2; i++) { const float4 q = wp[i]; x2b = x2b + mk3(q.x, q.y, q.z); w2b += q.w; }
+        const float w3 = wsum - w0b - w1b - w2b;
+        const float a2 = w0b + w1b * (4.0f / 9.0f) + w2b * (1.0f / 9.0f);
+        const float b2s = w3 + w2b * (4.0f / 9.0f) + w1b * (1.0f / 9.0f);
+        const float ab = (w1b + w2b) * (2.0f / 9.0f);
+        const float f = 1.0f / (a2 * b2s - ab * ab);
+        const f3 ax = (x0b + (x1b * (2.0f / 3.0f))) + (x2b * (1.0f / 3.0f));
+        const f3 bx = xsum - ax;
+        f3 a = ((ax * b2s) - (bx * ab)) * f;
+        f3 b = ((bx * a2) - (ax * ab)) * f;
+        a = mk3(sq_min(1.0f, sq_max(0.0f, a.x)), sq_min(1.0f, sq_max(0.0f, a.y)), sq_min(1.0f, sq_max(0.0f, a.z)));
+        b = mk3(sq_min(1.0f, sq_max(0.0f, b.x)), sq_min(1.0f, sq_max(0.0f, b.y)), sq_min(1.0f, sq_max(0.0f, b.z)));
+        bs = mk3(floorf(31.0f * a.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * a.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * a.z + 0.5f) * (1.0f / 31.0f));
+        be = mk3(floorf(31.0f * b.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * b.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * b.z + 0.5f) * (1.0f / 31.0f));
+    }
     // cluster sizes -> point (slot) indices -> texel indices (ColourSet::RemapIndices)
     uint32_t slot_idx = 0;
 #pragma unroll

@@ -1,6 +1,7 @@
 // Internal interfaces between the C-ABI layer (ntg_api.cu) and the kernel translation units.
 #pragma once
 
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -9,6 +10,14 @@ namespace ntg {
 
 // Launcher status: 0 on success, else kLaunchErrorBase + the cudaError_t of the failed launch.
 constexpr int kLaunchErrorBase = 1000;
+// True the first time it is called for the current device (function attributes are per device).
+inline bool first_use_on_device(std::atomic<unsigned long long> &mask) {
+    int d = 0;
+    cudaGetDevice(&d);
+    const unsigned long long bit = 1ull << (d & 63);
+    return (mask.fetch_or(bit) & bit) == 0;
+}
+
 inline int launch_status() {
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? 0 : kLaunchErrorBase + (int)e;

@@ -169,112 +169,122 @@ __device__ __forceinline__ int wrap_index(int x, int w, int wm) {
     return x;
 }
 
-constexpr int PTW = 32;    // output tile width
+constexpr int PTW = 32;    // output tile width (one warp lane per output column)
 constexpr int PTH = 16;    // output tile height
 constexpr int PMAXW = 32;  // widest window handled by the fused kernel
 constexpr int PTHREADS = 256;
-constexpr int PSLOTS = PTW * PTH / PTHREADS;
+constexpr int PWARPS = PTHREADS / 32;
 
-template <bool WEIGHTED>
+// One CTA per PTW x PTH output tile, all four channels at once (RGBA as float4 in shared memory):
+//  1. wrap maps for the tile's source rows and columns (FloatImage::index, one wrap per row/column),
+//  2. the wrapped source window staged once as float4 (from planar FP32 or BGRA8 + input table),
+//  3. X taps for every window row into a (rows x PTW) float4 plane,
+//  4. Y taps, written as four planes and, optionally, the quantised BGRA8 word.
+// Channel arithmetic is the reference's, lane by lane: sum starts at 0 and adds k * v in tap order.
+template <bool WEIGHTED, bool SRC_U8>
 __global__ void __launch_bounds__(PTHREADS) k_poly(PolyLevel L) {
-    extern __shared__ float sm[];
+    extern __shared__ float4 sm4[];
     const int ox0 = blockIdx.x * PTW, oy0 = blockIdx.y * PTH;
     const int tw = min(PTW, L.w - ox0), th = min(PTH, L.h - oy0);
-    // source window of the tile, before wrapping (left offsets are non-decreasing)
     const int xlo = L.lx[ox0], xhi = L.lx[ox0 + tw - 1] + L.wsx - 1;
     const int ylo = L.ly[oy0], yhi = L.ly[oy0 + th - 1] + L.wsy - 1;
     const int rx = xhi - xlo + 1, ry = yhi - ylo + 1;
-    float *s_in = sm;                                 // ry * rx source texels of one channel
-    float *s_tmp = s_in + ry * rx;                    // ry * PTW X-filtered rows
-    float *s_ain = s_tmp + ry * PTW;                  // weighted mode: alpha window
-    float *s_atmp = s_ain + (WEIGHTED ? ry * rx : 0); // weighted mode: X-filtered alpha
+    float4 *s_in = sm4;                 // ry * rx
+    float4 *s_tmp = s_in + ry * rx;     // ry * PTW
+    int *s_col = reinterpret_cast<int *>(s_tmp + ry * PTW);  // rx
+    int *s_row = s_col + rx;                                  // ry
     __shared__ float s_kx[PTW * PMAXW], s_ky[PTH * PMAXW], s_steps[256], s_lut[256];
     __shared__ int s_lx[PTW], s_ly[PTH];
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int i = tid; i < tw * L.wsx; i += PTHREADS) s_kx[i] = L.kx[(size_t)ox0 * L.wsx + i];
     for (int i = tid; i < th * L.wsy; i += PTHREADS) s_ky[i] = L.ky[(size_t)oy0 * L.wsy + i];
     if (tid < tw) s_lx[tid] = L.lx[ox0 + tid] - xlo;
     if (tid < th) s_ly[tid] = L.ly[oy0 + tid] - ylo;
+    for (int i = tid; i < rx; i += PTHREADS) s_col[i] = wrap_index(xlo + i, L.W, L.wrap);
+    for (int i = tid; i < ry; i += PTHREADS) s_row[i] = wrap_index(ylo + i, L.H, L.wrap);
     if (L.q_out && L.q.xform == 2) for (int i = tid; i < 256; i += PTHREADS) s_steps[i] = L.q.steps[i];
-    if (L.bgra8) for (int i = tid; i < 256; i += PTHREADS) s_lut[i] = L.lut[i];
-    const size_t sn = (size_t)L.W * L.H, dn = (size_t)L.w * L.h;
-    uint32_t qword[PSLOTS];
-#pragma unroll
-    for (int s = 0; s < PSLOTS; s++) qword[s] = 0;
+    if (SRC_U8) for (int i = tid; i < 256; i += PTHREADS) s_lut[i] = L.lut[i];
+    __syncthreads();
 
-    // channel order: alpha first (as resize(..., alpha) processes it), then R, G, B
-    for (int ci = 0; ci < 4; ci++) {
-        const int c = ci == 0 ? 3 : ci - 1;
-        __syncthreads();
-        for (int i = tid; i < ry * rx; i += PTHREADS) {
-            const int yy = wrap_index(ylo + i / rx, L.H, L.wrap), xx = wrap_index(xlo + i % rx, L.W, L.wrap);
-            const size_t s = (size_t)yy * L.W + xx;
-            float v;
-            if (L.bgra8) {
+    const size_t sn = (size_t)L.W * L.H;
+    for (int r = warp; r < ry; r += PWARPS) {
+        const size_t rowoff = (size_t)s_row[r] * L.W;
+        float4 *dst = s_in + r * rx;
+        for (int x = lane; x < rx; x += 32) {
+            const size_t s = rowoff + s_col[x];
+            float4 v;
+            if (SRC_U8) {
                 const uint32_t p = L.bgra8[s];
-                v = c == 3 ? (float)(p >> 24) / 255.0f : s_lut[(p >> (c == 0 ? 16 : (c == 1 ? 8 : 0))) & 255];
+                v = make_float4(s_lut[(p >> 16) & 255], s_lut[(p >> 8) & 255], s_lut[p & 255], (float)(p >> 24) / 255.0f);
             } else {
-                v = L.src[c * sn + s];
+                v = make_float4(L.src[s], L.src[sn + s], L.src[2 * sn + s], L.src[3 * sn + s]);
             }
-            s_in[i] = v;
-            if (WEIGHTED && c == 3) s_ain[i] = v;
-        }
-        __syncthreads();
-        // X taps for every source row the tile's Y taps read
-        for (int i = tid; i < ry * tw; i += PTHREADS) {
-            const int r = i / tw, x = i % tw;
-            const float *row = s_in + r * rx + s_lx[x];
-            const float *k = s_kx + x * L.wsx;
-            float sum = 0;
-            if (WEIGHTED && c != 3) {
-                const float *arow = s_ain + r * rx + s_lx[x];
-                float norm = 0;
-                for (int j = 0; j < L.wsx; j++) {
-                    float wgt = k[j] * (arow[j] + (1.0f / 256.0f));
-                    norm += wgt;
-                    sum += wgt * row[j];
-                }
-                sum = sum / norm;
-            } else {
-                for (int j = 0; j < L.wsx; j++) sum += k[j] * row[j];
-            }
-            s_tmp[r * PTW + x] = sum;
-            if (WEIGHTED && c == 3) s_atmp[r * PTW + x] = sum;
-        }
-        __syncthreads();
-        // Y taps
-#pragma unroll
-        for (int s = 0; s < PSLOTS; s++) {
-            const int i = tid + s * PTHREADS;
-            const int y = i / PTW, x = i % PTW;
-            if (y >= th || x >= tw) continue;
-            const float *k = s_ky + y * L.wsy;
-            const int r0 = s_ly[y];
-            float sum = 0;
-            if (WEIGHTED && c != 3) {
-                float norm = 0;
-                for (int j = 0; j < L.wsy; j++) {
-                    float wgt = k[j] * (s_atmp[(r0 + j) * PTW + x] + (1.0f / 256.0f));
-                    norm += wgt;
-                    sum += wgt * s_tmp[(r0 + j) * PTW + x];
-                }
-                sum = sum / norm;
-            } else {
-                for (int j = 0; j < L.wsy; j++) sum += k[j] * s_tmp[(r0 + j) * PTW + x];
-            }
-            L.dst[c * dn + (size_t)(oy0 + y) * L.w + ox0 + x] = sum;
-            if (L.q_out) {
-                const uint32_t qv = c == 3 ? quant_u8(sum) : quantize(sum, L.q.xform, s_steps);
-                qword[s] |= qv << (c == 3 ? 24 : (c == 0 ? 16 : (c == 1 ? 8 : 0)));
-            }
+            dst[x] = v;
         }
     }
-    if (L.q_out) {
-#pragma unroll
-        for (int s = 0; s < PSLOTS; s++) {
-            const int i = tid + s * PTHREADS;
-            const int y = i / PTW, x = i % PTW;
-            if (y < th && x < tw) L.q_out[(size_t)(oy0 + y) * L.w + ox0 + x] = qword[s];
+    __syncthreads();
+
+    // X taps: one lane per output column, warps over the window rows
+    if (lane < tw) {
+        const float *k = s_kx + lane * L.wsx;
+        const int off = s_lx[lane];
+        for (int r = warp; r < ry; r += PWARPS) {
+            const float4 *row = s_in + r * rx + off;
+            float4 sum = make_float4(0, 0, 0, 0);
+            if (WEIGHTED) {
+                float norm = 0;
+                for (int j = 0; j < L.wsx; j++) {
+                    const float4 v = row[j];
+                    const float kj = k[j];
+                    const float wgt = kj * (v.w + (1.0f / 256.0f));
+                    norm += wgt;
+                    sum.x += wgt * v.x; sum.y += wgt * v.y; sum.z += wgt * v.z;
+                    sum.w += kj * v.w;
+                }
+                sum.x = sum.x / norm; sum.y = sum.y / norm; sum.z = sum.z / norm;
+            } else {
+                for (int j = 0; j < L.wsx; j++) {
+                    const float4 v = row[j];
+                    const float kj = k[j];
+                    sum.x += kj * v.x; sum.y += kj * v.y; sum.z += kj * v.z; sum.w += kj * v.w;
+                }
+            }
+            s_tmp[r * PTW + lane] = sum;
+        }
+    }
+    __syncthreads();
+
+    // Y taps: one lane per output column, warps over the output rows
+    if (lane < tw) {
+        const size_t dn = (size_t)L.w * L.h;
+        for (int y = warp; y < th; y += PWARPS) {
+            const float *k = s_ky + y * L.wsy;
+            const float4 *col = s_tmp + s_ly[y] * PTW + lane;
+            float4 sum = make_float4(0, 0, 0, 0);
+            if (WEIGHTED) {
+                float norm = 0;
+                for (int j = 0; j < L.wsy; j++) {
+                    const float4 v = col[j * PTW];
+                    const float kj = k[j];
+                    const float wgt = kj * (v.w + (1.0f / 256.0f));
+                    norm += wgt;
+                    sum.x += wgt * v.x; sum.y += wgt * v.y; sum.z += wgt * v.z;
+                    sum.w += kj * v.w;
+                }
+                sum.x = sum.x / norm; sum.y = sum.y / norm; sum.z = sum.z / norm;
+            } else {
+                for (int j = 0; j < L.wsy; j++) {
+                    const float4 v = col[j * PTW];
+                    const float kj = k[j];
+                    sum.x += kj * v.x; sum.y += kj * v.y; sum.z += kj * v.z; sum.w += kj * v.w;
+                }
+            }
+            const size_t o = (size_t)(oy0 + y) * L.w + ox0 + lane;
+            L.dst[o] = sum.x;
+            L.dst[dn + o] = sum.y;
+            L.dst[2 * dn + o] = sum.z;
+            L.dst[3 * dn + o] = sum.w;
+            if (L.q_out) L.q_out[o] = quantize_bgra(sum.x, sum.y, sum.z, sum.w, L.q.xform, s_steps);
         }
     }
 }
@@ -304,10 +314,19 @@ int launch_fast_down(const float *src, int W, int H, float *dst, uint32_t *q_out
     return launch_status();
 }
 
-size_t poly_smem_bytes(int rx_max, int ry_max, bool weighted) {
-    size_t f = (size_t)ry_max * rx_max + (size_t)ry_max * PTW;
-    if (weighted) f *= 2;
-    return f * sizeof(float);
+size_t poly_smem_bytes(int rx_max, int ry_max, bool) {
+    return (size_t)ry_max * rx_max * sizeof(float4) + (size_t)ry_max * PTW * sizeof(float4) +
+           (size_t)(rx_max + ry_max) * sizeof(int);
+}
+
+template <bool W, bool U8>
+static int launch_poly_t(const PolyLevel &L, size_t sm, cudaStream_t s) {
+    static std::atomic<unsigned long long> configured{0};
+    if (first_use_on_device(configured))
+        cudaFuncSetAttribute(k_poly<W, U8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    dim3 grid((L.w + PTW - 1) / PTW, (L.h + PTH - 1) / PTH);
+    k_poly<W, U8><<<grid, PTHREADS, sm, s>>>(L);
+    return launch_status();
 }
 
 int launch_poly(const PolyArgs &a, cudaStream_t s) {
@@ -317,16 +336,10 @@ int launch_poly(const PolyArgs &a, cudaStream_t s) {
     L.wsx = a.wsx; L.wsy = a.wsy; L.kx = a.kx; L.ky = a.ky; L.lx = a.lx; L.ly = a.ly;
     L.wrap = a.wrap; L.dst = a.dst; L.q_out = a.q_out; L.q = Quant{a.xform, a.steps};
     const size_t sm = poly_smem_bytes(a.rx_max, a.ry_max, a.weighted);
-    if (a.wsx > PMAXW || a.wsy > PMAXW || sm > 180 * 1024) return 2;  // Error_UnsupportedFeature
-    dim3 grid((a.w + PTW - 1) / PTW, (a.h + PTH - 1) / PTH);
-    if (a.weighted) {
-        cudaFuncSetAttribute(k_poly<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_poly<true><<<grid, PTHREADS, sm, s>>>(L);
-    } else {
-        cudaFuncSetAttribute(k_poly<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_poly<false><<<grid, PTHREADS, sm, s>>>(L);
-    }
-    return launch_status();
+    if (a.wsx > PMAXW || a.wsy > PMAXW || sm > 200 * 1024) return 2;  // Error_UnsupportedFeature
+    const bool u8 = a.src == nullptr;
+    if (a.weighted) return u8 ? launch_poly_t<true, true>(L, sm, s) : launch_poly_t<true, false>(L, sm, s);
+    return u8 ? launch_poly_t<false, true>(L, sm, s) : launch_poly_t<false, false>(L, sm, s);
 }
 
 int poly_tile_w() { return PTW; }
