@@ -91,6 +91,20 @@ int ntg_mip_level(ntg_context *ctx, const float *d_src, int w, int h, float *d_d
 int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,
                int out_xform, float gamma, const float *cw, void *d_blocks, void *stream);
 
+/* ntg_encode for callers that cannot allocate device memory (engines that own all GPU memory
+ * through their own pools, frame loops where cudaMalloc's implicit synchronisation would stall):
+ * it calls no cudaMalloc/cudaFree and no allocating library routine. No counterpart in the
+ * reference. Its scratch is a static device array of NTG_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this library holds until exit; levels above NTG_NOALLOC_MAX_TEXELS texels are rejected
+ * with NTG_ERROR_INVALID_INPUT. The first call on a device looks up the array's device address
+ * (make it before any stream capture). All calls share the array: calls that overlap on the GPU
+ * race, so issue them on one stream. The context must come from ntg_create (which allocates nothing
+ * on the device); same arguments and results as ntg_encode. */
+#define NTG_NOALLOC_MAX_TEXELS 1048576
+#define NTG_NOALLOC_SCRATCH_BYTES (4 * NTG_NOALLOC_MAX_TEXELS + 2048)
+int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,
+                       int out_xform, float gamma, const float *cw, void *d_blocks, void *stream);
+
 /* ---- whole chains ---- */
 
 typedef struct ntg_chain_options {

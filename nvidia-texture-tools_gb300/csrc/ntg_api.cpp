@@ -360,6 +360,8 @@ int ensure_device(ntg_context *ctx) {
 
 }  // namespace
 
+void ntg::set_last_error(const std::string &msg) { g_error = msg; }
+
 extern "C" {
 
 int ntg_version(void) { return NTG_VERSION; }

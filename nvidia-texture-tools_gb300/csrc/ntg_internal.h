@@ -4,6 +4,7 @@
 #include <atomic>
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 namespace ntg {
@@ -77,5 +78,8 @@ int upload_tables_bc1(const HostTables &t);
 int upload_tables_bc3(const HostTables &t);
 int upload_tables_mip(const HostTables &t);
 int upload_tables_decode(const HostTables &t);
+
+// Sets the message ntg_last_error_string() returns on this thread.
+void set_last_error(const std::string &msg);
 
 }  // namespace ntg

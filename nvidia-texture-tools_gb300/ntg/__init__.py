@@ -77,6 +77,7 @@ def lib():
         "ntg_set_image_bgra8": (_i, [_vp, _vp, _i, _i, _i, _f, _vp, _vp]),
         "ntg_mip_level": (_i, [_vp, _vp, _i, _i, _vp, _i, _f, _vp, _i, _i, _i, _vp]),
         "ntg_encode": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
+        "ntg_encode_noalloc": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
         "ntg_chain_levels": (_i, [_i, _i, _i]),
         "ntg_chain_bytes": (_sz, [_i, _i, ctypes.POINTER(ChainOptions)]),
         "ntg_compress_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
