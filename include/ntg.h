@@ -105,6 +105,16 @@ int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, 
 int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,
                        int out_xform, float gamma, const float *cw, void *d_blocks, void *stream);
 
+/* Surface::toLinear(gamma) / toGamma(gamma) / toLinearFromSrgb / toSrgb (src/nvtt/Surface.cpp:1470-1592)
+ * on RGB of a planar FP32 level, in place. kind: 0 toLinear, 1 toGamma, 2 toLinearFromSrgb, 3 toSrgb.
+ * Gamma 2.2 is bit-exact (the reference's own table-and-quartic powf); the sRGB curves and other
+ * gammas use the device powf (may differ from the host libm in the last place). */
+#define NTG_TRANSFORM_TO_LINEAR 0
+#define NTG_TRANSFORM_TO_GAMMA 1
+#define NTG_TRANSFORM_FROM_SRGB 2
+#define NTG_TRANSFORM_TO_SRGB 3
+int ntg_transform(ntg_context *ctx, float *d_rgba, int w, int h, int kind, float gamma, void *stream);
+
 /* ---- whole chains ---- */
 
 typedef struct ntg_chain_options {

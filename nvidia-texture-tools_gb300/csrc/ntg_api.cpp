@@ -591,6 +591,20 @@ int ntg_host_transform_tables(int in_xform, int out_xform, float gamma, float *l
     return NTG_OK;
 }
 
+int ntg_transform(ntg_context *ctx, float *d_rgba, int w, int h, int kind, float gamma, void *stream) {
+    g_error.clear();
+    if (!ctx || !d_rgba || w <= 0 || h <= 0 || kind < 0 || kind > 3) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    NTG_TRY(ensure_device(ctx));
+    int k = kind;
+    float p = gamma;
+    if (kind <= 1) {
+        // Surface::toLinear / toGamma return early for gamma == 1 (nv::equal)
+        if (std::fabs(gamma - 1.0f) <= 0.0001f * std::max(1.0f, std::fabs(gamma))) return NTG_OK;
+        if (gamma != 2.2f) { k = 4; p = kind == 0 ? gamma : 1.0f / gamma; }
+    }
+    return launched(launch_transform(d_rgba, (size_t)w * h, k, p, S(stream)), "colour transform");
+}
+
 int ntg_profile_enable(ntg_context *ctx, int enable) {
     g_error.clear();
     if (!ctx) return fail(NTG_ERROR_INVALID_INPUT, "null context");

@@ -63,6 +63,7 @@ struct PolyArgs {
 
 int launch_set_image(const uint32_t *bgra, size_t n, const float *lut, float *out, cudaStream_t s);
 int launch_quantize(const float *rgba, size_t n, int xform, const float *steps, uint32_t *out, cudaStream_t s);
+int launch_transform(float *rgba, size_t n, int kind, float p, cudaStream_t s);
 int launch_fast_down(const float *src, int W, int H, float *dst, uint32_t *q_out, int xform, const float *steps,
                      cudaStream_t s);
 int launch_poly(const PolyArgs &a, cudaStream_t s);

@@ -289,6 +289,42 @@ __global__ void __launch_bounds__(PTHREADS) k_poly(PolyLevel L) {
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Colour transforms of RGB on a planar FP32 level, in place (Surface::toLinear / toGamma /
+// toLinearFromSrgb / toSrgb, src/nvtt/Surface.cpp:1470-1592). Gamma 2.2 uses the reference's own
+// table-and-quartic powf_11_5 / powf_5_11 and is bit-exact; the sRGB curves and other gammas call
+// the device powf, which can differ from the host libm's in the last place.
+__device__ __forceinline__ float dev_to_srgb(float f) {
+    if (isnan(f)) return 0.0f;
+    if (f <= 0.0f) return 0.0f;
+    if (f <= 0.0031308f) return 12.92f * f;
+    if (f <= 1.0f) return (powf(f, 0.41666f) * 1.055f) - 0.055f;
+    return 1.0f;
+}
+
+__device__ __forceinline__ float dev_from_srgb(float f) {
+    if (f < 0.0f) return 0.0f;
+    if (f < 0.04045f) return f / 12.92f;
+    if (f <= 1.0f) return powf((f + 0.055f) / 1.055f, 2.4f);
+    return 1.0f;
+}
+
+// kind: 0 toLinear(2.2), 1 toGamma(2.2), 2 toLinearFromSrgb, 3 toSrgb, 4 pow(max(0, x), p)
+__global__ void k_transform(float *__restrict__ rgb, size_t n3, int kind, float p) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n3; i += (size_t)gridDim.x * blockDim.x) {
+        const float x = rgb[i];
+        float y;
+        switch (kind) {
+            case 0: y = powf_11_5(x); break;
+            case 1: y = powf_5_11(x); break;
+            case 2: y = dev_from_srgb(x); break;
+            case 3: y = dev_to_srgb(x); break;
+            default: y = powf(ic_max(0.0f, x), p); break;
+        }
+        rgb[i] = y;
+    }
+}
+
 static int grid_for(size_t n, int threads) {
     size_t g = (n + threads - 1) / threads;
     const size_t cap = 152 * 64;
@@ -298,6 +334,12 @@ static int grid_for(size_t n, int threads) {
 int launch_set_image(const uint32_t *bgra, size_t n, const float *lut, float *out, cudaStream_t s) {
     if (n == 0) return 0;
     k_set_image<<<grid_for(n, 256), 256, 0, s>>>(bgra, n, lut, out);
+    return launch_status();
+}
+
+int launch_transform(float *rgba, size_t n, int kind, float p, cudaStream_t s) {
+    if (n == 0) return 0;
+    k_transform<<<grid_for(3 * n, 256), 256, 0, s>>>(rgba, 3 * n, kind, p);
     return launch_status();
 }
 

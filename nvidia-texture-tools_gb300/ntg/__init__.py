@@ -85,6 +85,7 @@ def lib():
         "ntg_mip_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
         "ntg_decode": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
         "ntg_profile_enable": (_i, [_vp, _i]),
+        "ntg_transform": (_i, [_vp, _vp, _i, _i, _i, _f, _vp]),
         "ntg_profile_read": (_i, [_vp, ctypes.POINTER(_f), ctypes.POINTER(_f)]),
         "ntg_error_sums": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp]),
         "ntg_host_polyphase": (_i, [_i, _f, _vp, _i, _i, _vp, _vp, _i]),

@@ -274,6 +274,8 @@ class Reference:
         self._decode = _bind(lib, "ref_decode", _i, [_i, _vp, _i, _i, _vp])
         self._rms = _bind(lib, "ref_rms", _i, [_i, _vp, _vp, _i, _i, _i, _vp, _vp])
         self._process = _bind(lib, "ref_process", _ll, [_vp, _i, _i, _i, _i, _i, _i, _i, _f, _f, _i, _i, _vp, _ll])
+        self._process_ex = _bind(lib, "ref_process_ex", _ll,
+                                 [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _vp, _vp, _vp, _ll])
 
     def bc1_block(self, level, colors, weights, cw=(1, 1, 1), three=1, black=1):
         c = np.ascontiguousarray(colors, np.float32).reshape(64)
@@ -390,6 +392,20 @@ class Reference:
                           max_level, int(header), _ptr(out), cap)
         assert n >= 0, n
         return out[:n]
+
+    def process_ex(self, data, w, h, fmt, input_format=0, nsrc_levels=1, quality=1, mip_filter=0, alpha_mode=0,
+                   wrap=2, max_level=-1, header=True, kaiser=(3.0, 4.0, 1.0), gamma=(2.2, 2.2), cw=(1, 1, 1, 1),
+                   container=0, srgb=0, version=0, normal_map=0, normalize_mips=1):
+        """Compressor::process with containers, flags, Kaiser parameters, source mipmaps and float
+        input; returns the bytes, or the negative nvtt::Error - 100 on failure."""
+        b = np.ascontiguousarray(data).view(np.uint8)
+        opts = np.array(list(kaiser) + list(gamma) + list(cw), np.float32)
+        flags = np.array([container, srgb, version, normal_map, normalize_mips], np.int32)
+        cap = 16 * Oracle.nblocks(w, h) * 2 + 4096
+        out = np.zeros(cap, np.uint8)
+        n = self._process_ex(_ptr(b), w, h, input_format, nsrc_levels, fmt, quality, mip_filter, alpha_mode, wrap,
+                             max_level, int(header), _ptr(opts), _ptr(flags), _ptr(out), cap)
+        return out[:n] if n >= 0 else n
 
 
 def level_sizes(w, h, max_levels=64):

@@ -310,4 +310,48 @@ long long ref_process(const unsigned char * bgra, int w, int h, int format, int 
     return copy_out(mem.bytes, out, cap);
 }
 
+// Compressor::process with the rest of the options the GPU drop-in mirrors. `data` holds
+// `nsrc_levels` source levels back to back (largest first) in `input_format` (0 BGRA8, 1 RGBA16F,
+// 2 RGBA32F, interleaved); opts[] = {kaiser width, kaiser alpha, kaiser stretch, in gamma,
+// out gamma, colour weights r, g, b, a}; flags[] = {container, srgb, user version, normal map,
+// normalize mipmaps}.
+long long ref_process_ex(const void * data, int w, int h, int input_format, int nsrc_levels,
+                         int format, int quality, int mip_filter, int alpha_mode, int wrap,
+                         int max_level, int header, const float * opts, const int * flags,
+                         unsigned char * out, long long cap) {
+    InputOptions io;
+    io.setTextureLayout(TextureType_2D, w, h);
+    io.setFormat((InputFormat)input_format);
+    const int bpp = input_format == 0 ? 4 : (input_format == 1 ? 8 : 16);
+    const unsigned char * p = (const unsigned char *)data;
+    int lw = w, lh = h;
+    for (int l = 0; l < nsrc_levels; l++) {
+        io.setMipmapData(p, lw, lh, 1, 0, l);
+        p += (size_t)lw * lh * bpp;
+        lw = lw > 1 ? lw / 2 : 1;
+        lh = lh > 1 ? lh / 2 : 1;
+    }
+    io.setAlphaMode((AlphaMode)alpha_mode);
+    io.setWrapMode((WrapMode)wrap);
+    io.setGamma(opts[3], opts[4]);
+    io.setMipmapFilter((MipmapFilter)mip_filter);
+    io.setKaiserParameters(opts[0], opts[1], opts[2]);
+    io.setMipmapGeneration(max_level != 0, max_level);
+    io.setNormalMap(flags[3] != 0);
+    io.setNormalizeMipmaps(flags[4] != 0);
+    CompressionOptions co;
+    fill_options(co, format, quality, opts + 5);
+    MemoryOutput mem;
+    CountingErrors err;
+    OutputOptions oo;
+    oo.setOutputHandler(&mem);
+    oo.setErrorHandler(&err);
+    oo.setOutputHeader(header != 0);
+    oo.setContainer((Container)flags[0]);
+    oo.setSrgbFlag(flags[1] != 0);
+    oo.setUserVersion(flags[2]);
+    if (!compressor().process(io, co, oo)) return -100 - (err.last < 0 ? 0 : err.last);
+    return copy_out(mem.bytes, out, cap);
+}
+
 } // extern "C"

@@ -7,6 +7,7 @@ Inputs are seeded synthetic blocks and images (ntg.synth); outputs are exactly w
 reference produces for them. The fixtures let the oracle be checked on machines without the
 reference tree."""
 import argparse
+import json
 import os
 import sys
 
@@ -48,11 +49,20 @@ def float_blocks(n, seed):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=pyoracle.REF_SRC)
+    ap.add_argument("--only", choices=["blocks", "dds"], help="write only the block/chain or only the DDS fixtures")
     args = ap.parse_args()
     path = pyoracle.build_reference(args.ref)
     if path is None:
         sys.exit("reference source tree not found")
     R = pyoracle.Reference(path)
+    if args.only != "dds":
+        write_block_fixtures(R)
+    if args.only != "blocks":
+        write_dds_fixtures(R)
+    print("fixtures written to", HERE)
+
+
+def write_block_fixtures(R):
 
     out = {}
     for level in (0, 7, 8):
@@ -93,7 +103,64 @@ def main():
     lin, _ = R.mip_chain(img, w, h, 0, 0.5, 0.0, 0.0, 2, 0, 0, 0)
     blocks = np.concatenate([R.compress(l.reshape(-1), l.shape[2], l.shape[1], 1, 1, 0) for l in lin])
     np.savez_compressed(os.path.join(HERE, "chain_c0.npz"), image=img, w=w, h=h, blocks=blocks)
-    print("fixtures written to", HERE)
+
+
+def write_dds_fixtures(R):
+    out = {}
+    for i, case in enumerate(DDS_CASES):
+        data = dds_input(i, case)
+        res = R.process_ex(data, case["w"], case["h"], case["format"], **{k: v for k, v in case.items()
+                                                                         if k not in ("w", "h", "format")})
+        out[f"params_{i}"] = np.array(json.dumps(case))
+        out[f"input_{i}"] = data
+        out[f"dds_{i}"] = res if isinstance(res, np.ndarray) else np.array([res], np.int64)
+        if case.get("input_format", 0) == 0 and case["format"] in (1, 4, 7):
+            # rmsError / rmsAlphaError of level 0 encoded without transforms, against its input
+            w, h = case["w"], case["h"]
+            bgra = data[:4 * w * h].reshape(h, w, 4)
+            planar = np.stack([bgra[..., c].astype(np.float32) / np.float32(255) for c in (2, 1, 0, 3)])
+            am = case.get("alpha_mode", 0)
+            blocks = R.compress(planar.reshape(-1), w, h, case["format"], case.get("quality", 1), am,
+                                case.get("cw", (1, 1, 1, 1)))
+            out[f"rms_{i}"] = np.array(R.rms(case["format"], planar.reshape(-1), blocks, w, h, am), np.float32)
+    np.savez_compressed(os.path.join(HERE, "dds_process.npz"), **out)
+
+
+# Compressor::process cases for the nvtt:: drop-in API: containers, header flags, filters, gammas,
+# source mipmaps, float input, and one format the DDS container rejects (BC7 -> Error 6).
+DDS_CASES = [
+    dict(w=61, h=37, format=1, quality=1, mip_filter=0),
+    dict(w=64, h=64, format=4, quality=1, mip_filter=2, alpha_mode=1, srgb=1, version=7),
+    dict(w=48, h=40, format=7, quality=2, mip_filter=1, gamma=(1.0, 1.0), container=1, normal_map=1, normalize_mips=0),
+    dict(w=32, h=32, format=1, quality=0, max_level=0, container=1, srgb=1),
+    dict(w=40, h=24, format=4, quality=0, max_level=3, wrap=0, cw=(0.5, 1.0, 0.25, 1.0)),
+    dict(w=32, h=32, format=1, quality=2, nsrc_levels=2),
+    dict(w=24, h=24, format=4, quality=1, mip_filter=1, input_format=2),
+    dict(w=16, h=16, format=1, quality=1, mip_filter=2, input_format=1, gamma=(1.0, 1.0), kaiser=(2.0, 6.0, 0.75)),
+    dict(w=17, h=9, format=4, quality=1, mip_filter=2, alpha_mode=1, wrap=1, header=False),
+    dict(w=3, h=5, format=1, quality=1),
+    dict(w=20, h=12, format=7, quality=1, mip_filter=0, normal_map=1, normalize_mips=0),
+    dict(w=16, h=16, format=11, quality=1),
+]
+
+
+def dds_input(i, case):
+    """Seeded input of DDS case i: BGRA8 levels (source mipmaps included) or interleaved float RGBA."""
+    w, h = case["w"], case["h"]
+    levels = pyoracle.level_sizes(w, h)[:case.get("nsrc_levels", 1)]
+    fmt = case.get("input_format", 0)
+    parts = []
+    for j, (lw, lh) in enumerate(levels):
+        rng = np.random.default_rng(9000 + 10 * i + j)
+        img = synth.colour_texture(lw, lh, 900 + 10 * i + j, scale=0.2,
+                                   alpha=rng.integers(0, 256, (lh, lw)).astype(np.uint8))
+        if fmt == 0:
+            parts.append(img.reshape(-1))
+        else:
+            rgba = img[..., [2, 1, 0, 3]].astype(np.float32) / 255.0 + rng.normal(0, 0.01, (lh, lw, 4)).astype(np.float32)
+            rgba = np.clip(rgba, 0, 1).astype(np.float32)
+            parts.append((rgba.astype(np.float16) if fmt == 1 else rgba).reshape(-1).view(np.uint8))
+    return np.concatenate(parts)
 
 
 if __name__ == "__main__":
