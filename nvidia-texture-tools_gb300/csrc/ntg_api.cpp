@@ -96,11 +96,20 @@ struct AxisTable {
     float *d_w = nullptr;
     int *d_left = nullptr;
     std::vector<int> left;
+    bool half = false;  // exact 2:1 with every output on the same taps (left[i] = left0 + 2i, equal rows)
+    int left0 = 0;
+};
+
+// Launch shape of the 2:1 mip kernel (output rows per warp strip, threads per CTA).
+struct MipTuning {
+    int strip = 32;
+    int threads = 128;
+    long long tail_texels = 4096;  // a chain's remaining levels go to one tail CTA from a source this small
 };
 
 // Device copy of one 256-entry table set for an (in, out, gamma) transform combination.
 struct XformTables {
-    float *d_in = nullptr;       // input transform of 8-bit values
+    float *d_in = nullptr;       // input transform of 8-bit RGB values [256], then v / 255 for alpha [256]
     float *d_comp = nullptr;     // output(input(v/255)) for the BC1 level-0 path
     uint8_t *d_comp8 = nullptr;  // quantised composition (RGB) + alpha quantiser, 512 bytes
     float *d_steps = nullptr;    // sRGB quantiser steps
@@ -119,6 +128,9 @@ struct ntg_context {
     size_t ws_bytes = 0;
     EncJob *d_jobs = nullptr;   // job list of chain encodes
     int d_jobs_cap = 0;
+    MipJob *d_mipjobs = nullptr;  // job lists of chain mip launches
+    int d_mipjobs_cap = 0;
+    MipTuning tune;
     bool profile = false;       // record phase events in chain calls
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
@@ -129,6 +141,7 @@ struct ntg_context {
         for (void *p : owned) cudaFree(p);
         if (ws) cudaFree(ws);
         if (d_jobs) cudaFree(d_jobs);
+        if (d_mipjobs) cudaFree(d_mipjobs);
     }
 
     int alloc(void **p, size_t bytes) {
@@ -159,6 +172,12 @@ struct ntg_context {
         std::vector<float> w((size_t)t.ws * dst);
         t.left.resize(dst);
         build_polyphase(filter, width, p0, p1, src, dst, w.data(), t.left.data());
+        t.left0 = t.left[0];
+        t.half = src == 2 * dst;
+        for (int i = 1; i < dst && t.half; i++) {
+            t.half = t.left[i] == t.left0 + 2 * i &&
+                     std::memcmp(&w[(size_t)i * t.ws], &w[0], (size_t)t.ws * sizeof(float)) == 0;
+        }
         if (alloc((void **)&t.d_w, w.size() * sizeof(float)) != NTG_OK) return nullptr;
         if (alloc((void **)&t.d_left, t.left.size() * sizeof(int)) != NTG_OK) return nullptr;
         if (cudaMemcpy(t.d_w, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
@@ -172,9 +191,10 @@ struct ntg_context {
         auto it = xforms.find(key);
         if (it != xforms.end()) return &it->second;
         XformTables t;
-        float lin[256], comp[256], steps[256];
+        float lin[512], comp[256], steps[256];  // lin: input transform of RGB, then v / 255 for alpha
         uint8_t comp8[512];
         build_input_lut(in_x, gamma, tables, lin);
+        for (int v = 0; v < 256; v++) lin[256 + v] = (float)v / 255.0f;
         build_composed_lut(in_x, out_x, gamma, tables, comp);
         build_composed_lut8(in_x, out_x, gamma, tables, comp8);
         build_srgb_steps(steps);
@@ -252,44 +272,184 @@ ChainPlan plan_chain(int w, int h, const ntg_chain_options &o, bool keep_level0_
     return P;
 }
 
+struct MipKey {
+    int kernel, ws, weighted, u8;
+    bool operator<(const MipKey &o) const {
+        return std::tie(kernel, ws, weighted, u8) < std::tie(o.kernel, o.ws, o.weighted, o.u8);
+    }
+};
+
+// The mip job of one buildNextMipmap step from `src` (planar FP32; null = the BGRA8 input through
+// the input table `lut`) of size S into `dst` of size D, and the kernel variant that runs it:
+// the box path, the 2:1 kernel when both axes halve with uniform taps, else the general kernel.
+int plan_step(ntg_context *ctx, const ntg_chain_options &o, float width, const float p[2], bool fast_box,
+              const float *src, const uint32_t *bgra, const float *lut, Level S, Level D, float *dst, uint32_t *q,
+              const float *steps, MipJob &J, MipKey &key) {
+    std::memset(&J, 0, sizeof J);
+    J.src = src; J.bgra8 = src ? nullptr : bgra; J.lut = lut;
+    J.W = S.w; J.H = S.h; J.w = D.w; J.h = D.h;
+    J.wrap = o.wrap; J.dst = dst; J.q_out = q; J.xform = o.out_xform; J.steps = steps;
+    if (fast_box) {
+        if (!src) return fail(NTG_ERROR_INVALID_INPUT, "box downsample needs an FP32 source level");
+        key = {MIP_FAST_BOX, 0, 0, 0};
+        return NTG_OK;
+    }
+    const AxisTable *ax = ctx->axis(o.filter, width, p[0], p[1], S.w, D.w);
+    const AxisTable *ay = ctx->axis(o.filter, width, p[0], p[1], S.h, D.h);
+    if (!ax || !ay) return fail(NTG_ERROR_CUDA, "polyphase table upload failed");
+    J.wsx = ax->ws; J.wsy = ay->ws; J.kx = ax->d_w; J.ky = ay->d_w; J.lx = ax->d_left; J.ly = ay->d_left;
+    const int weighted = o.weighted != 0, u8 = src == nullptr;
+    if (ax->half && ay->half && ax->ws == ay->ws && poly2x_supported(ax->ws)) {
+        J.cx = ax->left0; J.cy = ay->left0;
+        J.tiles_x = (D.w + 31) / 32;
+        J.strip = ctx->tune.strip;
+        key = {MIP_POLY2X, ax->ws, weighted, u8};
+        return NTG_OK;
+    }
+    if (ax->ws > poly_max_window() || ay->ws > poly_max_window())
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "polyphase windows wider than 32 taps are not supported");
+    J.tiles_x = (D.w + poly_tile_w() - 1) / poly_tile_w();
+    J.rx_max = max_window(*ax, poly_tile_w());
+    J.ry_max = max_window(*ay, poly_tile_h());
+    key = {MIP_POLY, 0, weighted, u8};
+    return NTG_OK;
+}
+
+long long mip_units(const MipKey &k, const MipJob &J) {
+    if (k.kernel == MIP_FAST_BOX) return (long long)J.w * J.h;
+    if (k.kernel == MIP_POLY2X) return (long long)J.tiles_x * ((J.h + J.strip - 1) / J.strip);
+    return (long long)J.tiles_x * ((J.h + poly_tile_h() - 1) / poly_tile_h());
+}
+
+// Groups the jobs of one chain depth by kernel variant into launches; appends the jobs to `all`.
+void group_launches(const std::vector<std::pair<MipKey, MipJob>> &items, const MipTuning &tune, std::vector<MipJob> &all,
+                    std::vector<MipLaunch> &out) {
+    std::map<MipKey, std::vector<MipJob>> groups;
+    for (const auto &it : items) groups[it.first].push_back(it.second);
+    for (auto &g : groups) {
+        MipLaunch m;
+        std::memset(&m, 0, sizeof m);
+        m.kernel = g.first.kernel; m.ws = g.first.ws; m.weighted = g.first.weighted; m.u8 = g.first.u8;
+        m.first_job = (int)all.size();
+        m.njobs = (int)g.second.size();
+        m.threads = tune.threads;
+        if (m.kernel == MIP_POLY2X) {
+            // a warp sweeps its strip serially: shorten the strips until the launch has enough warps
+            const long long target = 152LL * 16;
+            int strip = tune.strip;
+            for (;;) {
+                long long n = 0;
+                for (const MipJob &J : g.second) n += (long long)J.tiles_x * ((J.h + strip - 1) / strip);
+                if (strip <= 2 || n >= target) break;
+                strip /= 2;
+            }
+            for (MipJob &J : g.second) J.strip = strip;
+        }
+        long long units = 0;
+        int rx = 0, ry = 0;
+        for (MipJob J : g.second) {
+            J.first_unit = units;
+            units += mip_units(g.first, J);
+            rx = std::max(rx, J.rx_max);
+            ry = std::max(ry, J.ry_max);
+            all.push_back(J);
+        }
+        m.units = units;
+        m.smem = m.kernel == MIP_POLY ? poly_smem_bytes(rx, ry) : m.kernel == MIP_POLY2X ? poly2x_smem_bytes(m.ws, m.threads) : 0;
+        out.push_back(m);
+    }
+}
+
+// First destination level of a chain that its tail launch computes (lv.size() = no tail).
+size_t tail_start(const ChainPlan &P, const MipTuning &tune) {
+    const long long limit = std::min<long long>(tune.tail_texels, tail_max_texels());
+    for (size_t l = 1; l < P.lv.size(); l++)
+        if ((long long)P.lv[l - 1].w * P.lv[l - 1].h <= limit) return P.lv.size() - l >= 2 ? l : P.lv.size();
+    return P.lv.size();
+}
+
+// Mip job of destination level l of a chain.
+int chain_step(ntg_context *ctx, const ChainPlan &P, size_t l, const uint32_t *d_bgra, const ntg_chain_options &o,
+               const XformTables *xt, uint8_t *ws, MipJob &J, MipKey &key) {
+    const float *src = P.f_off[l - 1] != NONE ? (const float *)(ws + P.f_off[l - 1]) : nullptr;
+    uint32_t *q = P.q_off[l] != NONE ? (uint32_t *)(ws + P.q_off[l]) : nullptr;
+    return plan_step(ctx, o, P.width, P.p, P.fast_box, src, d_bgra, xt->d_in, P.lv[l - 1], P.lv[l],
+                     (float *)(ws + P.f_off[l]), q, xt->d_steps, J, key);
+}
+
+// Appends the tail jobs of a chain (levels from..end) to `all` as tail chain number `chain`.
+int chain_tail(ntg_context *ctx, const ChainPlan &P, size_t from, const uint32_t *d_bgra, const ntg_chain_options &o,
+               const XformTables *xt, uint8_t *ws, long long chain, std::vector<MipJob> &all) {
+    const size_t first = all.size();
+    for (size_t l = from; l < P.lv.size(); l++) {
+        MipJob J;
+        MipKey key;
+        NTG_TRY(chain_step(ctx, P, l, d_bgra, o, xt, ws, J, key));
+        J.first_unit = chain;
+        all.push_back(J);
+    }
+    all[first].tiles_x = (int)(P.lv.size() - from);
+    return NTG_OK;
+}
+
+// The mip steps of one chain: one stage (list of launches) per destination level, then one tail
+// launch for the small levels.
+int chain_stages(ntg_context *ctx, const ChainPlan &P, const uint32_t *d_bgra, const ntg_chain_options &o,
+                 const XformTables *xt, uint8_t *ws, std::vector<MipJob> &all,
+                 std::vector<std::vector<MipLaunch>> &stages) {
+    const size_t tail = tail_start(P, ctx->tune);
+    for (size_t l = 1; l < tail; l++) {
+        std::vector<std::pair<MipKey, MipJob>> items(1);
+        NTG_TRY(chain_step(ctx, P, l, d_bgra, o, xt, ws, items[0].second, items[0].first));
+        stages.emplace_back();
+        group_launches(items, ctx->tune, all, stages.back());
+    }
+    if (tail < P.lv.size()) {
+        MipLaunch m;
+        std::memset(&m, 0, sizeof m);
+        m.kernel = MIP_TAIL;
+        m.weighted = o.weighted != 0;
+        m.first_job = (int)all.size();
+        NTG_TRY(chain_tail(ctx, P, tail, d_bgra, o, xt, ws, 0, all));
+        m.njobs = (int)all.size() - m.first_job;
+        m.units = 1;
+        stages.push_back({m});
+    }
+    return NTG_OK;
+}
+
+int upload_mip_jobs(ntg_context *ctx, const std::vector<MipJob> &jobs, cudaStream_t s) {
+    if (jobs.empty()) return NTG_OK;
+    if ((int)jobs.size() > ctx->d_mipjobs_cap) {
+        if (ctx->d_mipjobs) NTG_CUDA(cudaFreeAsync(ctx->d_mipjobs, s));
+        ctx->d_mipjobs = nullptr;
+        const int cap = std::max<int>((int)jobs.size(), 64);
+        NTG_CUDA(cudaMallocAsync((void **)&ctx->d_mipjobs, cap * sizeof(MipJob), s));
+        ctx->d_mipjobs_cap = cap;
+    }
+    NTG_CUDA(cudaMemcpyAsync(ctx->d_mipjobs, jobs.data(), jobs.size() * sizeof(MipJob), cudaMemcpyHostToDevice, s));
+    return NTG_OK;
+}
+
+int run_stages(const std::vector<std::vector<MipLaunch>> &stages, const MipJob *d_jobs, cudaStream_t s) {
+    for (const auto &stage : stages)
+        for (const MipLaunch &m : stage) NTG_TRY(launched(launch_mip(m, d_jobs, s), "mip filter"));
+    return NTG_OK;
+}
+
 // Builds the levels of a chain into the workspace. Level 0 comes straight from the BGRA8 input:
 // the fast box path materialises it as FP32, the polyphase path reads the bytes through the input
 // transform table.
 int build_levels(ntg_context *ctx, const ChainPlan &P, const uint32_t *d_bgra, const ntg_chain_options &o,
                  const XformTables *xt, uint8_t *ws, cudaStream_t s) {
-    const int L = (int)P.lv.size();
     if (P.f_off[0] != NONE) {
         NTG_TRY(launched(launch_set_image(d_bgra, (size_t)P.lv[0].w * P.lv[0].h, xt->d_in, (float *)(ws + P.f_off[0]), s), "set image"));
     }
-    for (int l = 1; l < L; l++) {
-        const Level &S = P.lv[l - 1], &D = P.lv[l];
-        float *dst = (float *)(ws + P.f_off[l]);
-        uint32_t *q = P.q_off[l] != NONE ? (uint32_t *)(ws + P.q_off[l]) : nullptr;
-        if (P.fast_box) {
-            NTG_TRY(launched(launch_fast_down((const float *)(ws + P.f_off[l - 1]), S.w, S.h, dst, q, o.out_xform, xt->d_steps, s), "box downsample"));
-            continue;
-        }
-        const AxisTable *ax = ctx->axis(o.filter, P.width, P.p[0], P.p[1], S.w, D.w);
-        const AxisTable *ay = ctx->axis(o.filter, P.width, P.p[0], P.p[1], S.h, D.h);
-        if (!ax || !ay) return fail(NTG_ERROR_CUDA, "polyphase table upload failed");
-        PolyArgs a;
-        a.src = P.f_off[l - 1] != NONE ? (const float *)(ws + P.f_off[l - 1]) : nullptr;
-        a.bgra8 = a.src ? nullptr : d_bgra;
-        a.lut = xt->d_in;
-        a.W = S.w; a.H = S.h; a.w = D.w; a.h = D.h;
-        a.wsx = ax->ws; a.wsy = ay->ws;
-        a.kx = ax->d_w; a.ky = ay->d_w; a.lx = ax->d_left; a.ly = ay->d_left;
-        a.wrap = o.wrap;
-        a.dst = dst;
-        a.q_out = q;
-        a.xform = o.out_xform;
-        a.steps = xt->d_steps;
-        a.weighted = o.weighted != 0;
-        a.rx_max = max_window(*ax, poly_tile_w());
-        a.ry_max = max_window(*ay, poly_tile_h());
-        NTG_TRY(launched(launch_poly(a, s), "polyphase filter (windows wider than 32 taps are not supported)"));
-    }
-    return NTG_OK;
+    std::vector<MipJob> all;
+    std::vector<std::vector<MipLaunch>> stages;
+    NTG_TRY(chain_stages(ctx, P, d_bgra, o, xt, ws, all, stages));
+    NTG_TRY(upload_mip_jobs(ctx, all, s));
+    return run_stages(stages, ctx->d_mipjobs, s);
 }
 
 int upload_jobs(ntg_context *ctx, const std::vector<EncJob> &jobs, cudaStream_t s) {
@@ -432,19 +592,15 @@ int ntg_mip_level(ntg_context *ctx, const float *d_src, int w, int h, float *d_d
     float fw, p[2];
     filter_defaults(o, fw, p);
     const int dw = std::max(1, w / 2), dh = std::max(1, h / 2);
-    if (uses_fast_box(o, fw) && !weighted)
-        return launched(launch_fast_down(d_src, w, h, d_dst, nullptr, 0, nullptr, S(stream)), "box downsample");
-    const AxisTable *ax = ctx->axis(filter, fw, p[0], p[1], w, dw);
-    const AxisTable *ay = ctx->axis(filter, fw, p[0], p[1], h, dh);
-    if (!ax || !ay) return fail(NTG_ERROR_CUDA, "polyphase table upload failed");
-    PolyArgs a;
-    std::memset(&a, 0, sizeof a);
-    a.src = d_src; a.W = w; a.H = h; a.w = dw; a.h = dh;
-    a.wsx = ax->ws; a.wsy = ay->ws; a.kx = ax->d_w; a.ky = ay->d_w; a.lx = ax->d_left; a.ly = ay->d_left;
-    a.wrap = wrap; a.dst = d_dst; a.weighted = weighted != 0;
-    a.rx_max = max_window(*ax, poly_tile_w());
-    a.ry_max = max_window(*ay, poly_tile_h());
-    return launched(launch_poly(a, S(stream)), "polyphase filter (windows wider than 32 taps are not supported)");
+    std::vector<std::pair<MipKey, MipJob>> items(1);
+    NTG_TRY(plan_step(ctx, o, fw, p, uses_fast_box(o, fw) && !weighted, d_src, nullptr, nullptr, Level{w, h},
+                      Level{dw, dh}, d_dst, nullptr, nullptr, items[0].second, items[0].first));
+    std::vector<MipJob> all;
+    std::vector<std::vector<MipLaunch>> stages(1);
+    group_launches(items, ctx->tune, all, stages[0]);
+    cudaStream_t s = S(stream);
+    NTG_TRY(upload_mip_jobs(ctx, all, s));
+    return run_stages(stages, ctx->d_mipjobs, s);
 }
 
 int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,

@@ -45,30 +45,53 @@ int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, 
 int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s);
 int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s);
 
-struct PolyArgs {
-    const float *src;
-    const uint32_t *bgra8;
-    const float *lut;
-    int W, H, w, h, wsx, wsy;
-    const float *kx, *ky;
-    const int *lx, *ly;
-    int wrap;
-    float *dst;
-    uint32_t *q_out;
-    int xform;
-    const float *steps;
-    bool weighted;
-    int rx_max, ry_max;  // largest source window of any output tile (host-computed)
+// One buildNextMipmap step (source level -> destination level) of one texture. A mip launch walks a
+// list of these: its units (destination texels, tiles or strips, depending on the kernel) are
+// numbered across the jobs (`first_unit`), so one launch covers the same step of many textures.
+struct MipJob {
+    const float *src;        // planar FP32 source level, or null to read bgra8 through lut
+    const uint32_t *bgra8;   // BGRA8 source words (level 0 read straight from the input)
+    const float *lut;        // 256-entry input transform for bgra8 RGB
+    int W, H, w, h;          // source and destination sizes
+    int wsx, wsy;            // polyphase windows
+    const float *kx, *ky;    // weights: w x wsx and h x wsy (the 2:1 kernel reads row 0 only)
+    const int *lx, *ly;      // window offsets of every output column / row (general kernel)
+    int cx, cy;              // 2:1 kernel: window offset of output column / row 0
+    int wrap;                // 0 clamp, 1 repeat, 2 mirror
+    float *dst;              // planar FP32 destination level
+    uint32_t *q_out;         // optional quantised BGRA8 destination (for the BC3/BC5 encoders)
+    int xform;               // output transform folded into the quantiser (0 none, 1 gamma 2.2, 2 sRGB)
+    const float *steps;      // sRGB quantiser steps (xform 2)
+    int tiles_x;             // units along x (tail launches: levels in the chain, on its first job)
+    int strip;               // 2:1 kernel: output rows per unit
+    int rx_max, ry_max;      // general kernel: widest source window of a tile (host side, for shared memory)
+    long long first_unit;    // running unit count of the launch (tail launches: the chain's index)
+};
+
+enum MipKernel { MIP_FAST_BOX = 0, MIP_POLY = 1, MIP_POLY2X = 2, MIP_TAIL = 3 };
+
+// One launch over jobs [first_job, first_job + njobs) of a device job array.
+struct MipLaunch {
+    int kernel;              // MipKernel
+    int ws;                  // 2:1 kernel: window size (3, 5 or 13)
+    int weighted, u8;        // template switches: alpha-weighted taps, BGRA8 source
+    int first_job, njobs;
+    long long units;
+    size_t smem;             // dynamic shared memory
+    int threads;             // 2:1 kernel: threads per CTA (one strip per warp)
 };
 
 int launch_set_image(const uint32_t *bgra, size_t n, const float *lut, float *out, cudaStream_t s);
 int launch_quantize(const float *rgba, size_t n, int xform, const float *steps, uint32_t *out, cudaStream_t s);
 int launch_transform(float *rgba, size_t n, int kind, float p, cudaStream_t s);
-int launch_fast_down(const float *src, int W, int H, float *dst, uint32_t *q_out, int xform, const float *steps,
-                     cudaStream_t s);
-int launch_poly(const PolyArgs &a, cudaStream_t s);
+int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s);
+bool poly2x_supported(int ws);
+size_t poly_smem_bytes(int rx_max, int ry_max);
+size_t poly2x_smem_bytes(int ws, int threads);
 int poly_tile_w();
 int poly_tile_h();
+int poly_max_window();
+int tail_max_texels();  // largest source level a tail launch starts from
 
 int launch_decode(int format, const uint8_t *blocks, int w, int h, float *rgba, cudaStream_t s);
 int launch_rms(const float *ref, const float *dec, int w, int h, int alpha_mode, double *sums, cudaStream_t s);

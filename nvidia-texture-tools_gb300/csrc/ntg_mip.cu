@@ -71,18 +71,44 @@ __global__ void k_quantize_level(const float *__restrict__ rgba, size_t n, Quant
 }
 
 // ---------------------------------------------------------------------------------------------
+// Job lists. Every mip kernel takes an array of MipJob (one level step of one texture) and a
+// running unit count per job, so one launch covers a level of any number of textures; a unit is a
+// destination texel (box), a PTW x PTH tile (general polyphase) or a 32-column x `strip`-row
+// strip (2:1 polyphase). A unit finds its job by binary search over `first_unit`.
+__device__ __forceinline__ int find_mip_job(const MipJob *__restrict__ jobs, int njobs, long long u) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].first_unit <= u) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The sRGB quantiser steps are one table for every job (they depend on no option); a CTA copies
+// it into shared memory once, so the 8-step search of each quantised channel stays on chip.
+__device__ __forceinline__ void load_steps(const MipJob *__restrict__ jobs, float *s_steps) {
+    const float *steps = jobs[0].steps;
+    if (steps)
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) s_steps[i] = __ldg(steps + i);
+}
+
+// ---------------------------------------------------------------------------------------------
 // FloatImage::fastDownSample (src/nvimage/FloatImage.cpp:559-737): 2x2 box for even sizes,
 // pair average for 1-D images and the three-tap polyphase box for odd sizes. One thread per
-// destination texel and channel.
-__global__ void k_fast_down(const float *__restrict__ src0, int W, int H, float *__restrict__ dst0,
-                            uint32_t *__restrict__ q_out, Quant q) {
+// destination texel, all four channels.
+__global__ void k_fast_down(const MipJob *__restrict__ jobs, int njobs, long long units) {
     __shared__ float s_steps[256];
-    if (q_out && q.xform == 2)
-        for (int i = threadIdx.x; i < 256; i += blockDim.x) s_steps[i] = q.steps[i];
+    load_steps(jobs, s_steps);
     __syncthreads();
-    const unsigned w = W / 2 > 1 ? (unsigned)W / 2 : 1u, h = H / 2 > 1 ? (unsigned)H / 2 : 1u;
-    const size_t sn = (size_t)W * H, dn = (size_t)w * h;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < dn; t += (size_t)gridDim.x * blockDim.x) {
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < units;
+         u += (long long)gridDim.x * blockDim.x) {
+        const MipJob &L = jobs[find_mip_job(jobs, njobs, u)];
+        const int W = L.W, H = L.H;
+        const float *src0 = L.src;
+        const unsigned w = W / 2 > 1 ? (unsigned)W / 2 : 1u, h = H / 2 > 1 ? (unsigned)H / 2 : 1u;
+        const size_t sn = (size_t)W * H, dn = (size_t)w * h;
+        const size_t t = (size_t)(u - L.first_unit);
         const unsigned x = (unsigned)(t % w), y = (unsigned)(t / w);
         float v[4];
 #pragma unroll
@@ -132,34 +158,18 @@ __global__ void k_fast_down(const float *__restrict__ src0, int W, int H, float 
                 f = acc * scale;
             }
             v[c] = f;
-            dst0[c * dn + t] = f;
+            L.dst[c * dn + t] = f;
         }
-        if (q_out) q_out[t] = quantize_bgra(v[0], v[1], v[2], v[3], q.xform, s_steps);
+        if (L.q_out) L.q_out[t] = quantize_bgra(v[0], v[1], v[2], v[3], L.xform, s_steps);
     }
 }
 
 // ---------------------------------------------------------------------------------------------
-// Fused separable polyphase resize: FloatImage::resize 2D (src/nvimage/FloatImage.cpp:761-808)
-// = applyKernelX over every source row into a (w' x H) plane, then applyKernelY
-// (:1115-1176). A CTA owns a TW x TH output tile: it stages the (wrapped) source window of the
-// tile in shared memory, runs the X taps for the rows the tile's Y taps touch, then the Y taps.
-// The optional weighted mode applies the alpha-weighted kernels (:1212-1281) to RGB.
-struct PolyLevel {
-    const float *src;        // planar FP32 source level (null when reading bgra8 + lut)
-    const uint32_t *bgra8;   // BGRA8 source words (level 0 read straight from the input)
-    const float *lut;        // 256-entry input transform for bgra8 RGB
-    int W, H, w, h;
-    int wsx, wsy;            // window sizes
-    const float *kx;         // w * wsx weights
-    const float *ky;         // h * wsy weights
-    const int *lx;           // w left offsets
-    const int *ly;           // h left offsets
-    int wrap;                // 0 clamp, 1 repeat, 2 mirror (src/nvimage/FloatImage.h:298-317)
-    float *dst;              // planar FP32 destination level
-    uint32_t *q_out;         // optional quantised BGRA8 destination
-    Quant q;
-};
-
+// Separable polyphase resize: FloatImage::resize 2D (src/nvimage/FloatImage.cpp:761-808) =
+// applyKernelX over every source row into a (w' x H) plane, then applyKernelY (:1115-1176). Wrap
+// modes follow FloatImage::index (src/nvimage/FloatImage.h:298-317). The weighted variants apply the
+// alpha-weighted kernels (:1212-1281) to RGB. Channel arithmetic is the reference's, lane by lane:
+// each sum starts at 0 and adds k * v in tap order, so levels are bit-identical.
 __device__ __forceinline__ int wrap_index(int x, int w, int wm) {
     if (wm == 0) return x < 0 ? 0 : (x > w - 1 ? w - 1 : x);
     if (wm == 1) return x >= 0 ? x % w : (x + 1) % w + w - 1;
@@ -169,123 +179,409 @@ __device__ __forceinline__ int wrap_index(int x, int w, int wm) {
     return x;
 }
 
-constexpr int PTW = 32;    // output tile width (one warp lane per output column)
-constexpr int PTH = 16;    // output tile height
-constexpr int PMAXW = 32;  // widest window handled by the fused kernel
+template <bool SRC_U8>
+__device__ __forceinline__ float4 load_texel(const MipJob &L, size_t s, size_t sn) {
+    if (SRC_U8) {
+        const uint32_t p = __ldg(L.bgra8 + s);
+        return make_float4(__ldg(L.lut + ((p >> 16) & 255)), __ldg(L.lut + ((p >> 8) & 255)), __ldg(L.lut + (p & 255)),
+                           (float)(p >> 24) / 255.0f);
+    }
+    return make_float4(__ldg(L.src + s), __ldg(L.src + sn + s), __ldg(L.src + 2 * sn + s), __ldg(L.src + 3 * sn + s));
+}
+
+// One tap: sum += k * v for every channel (the weighted form weighs RGB by k * (alpha + 1/256)).
+template <bool WEIGHTED>
+__device__ __forceinline__ void tap(float4 &sum, float &norm, float k, const float4 v) {
+    if (WEIGHTED) {
+        const float wgt = k * (v.w + (1.0f / 256.0f));
+        norm += wgt;
+        sum.x += wgt * v.x; sum.y += wgt * v.y; sum.z += wgt * v.z;
+        sum.w += k * v.w;
+    } else {
+        sum.x += k * v.x; sum.y += k * v.y; sum.z += k * v.z; sum.w += k * v.w;
+    }
+}
+
+template <bool WEIGHTED>
+__device__ __forceinline__ float4 finish(float4 sum, float norm) {
+    if (WEIGHTED) { sum.x = sum.x / norm; sum.y = sum.y / norm; sum.z = sum.z / norm; }
+    return sum;
+}
+
+__device__ __forceinline__ void store_texel(const MipJob &L, size_t o, size_t dn, float4 v, const float *s_steps) {
+    L.dst[o] = v.x;
+    L.dst[dn + o] = v.y;
+    L.dst[2 * dn + o] = v.z;
+    L.dst[3 * dn + o] = v.w;
+    if (L.q_out) L.q_out[o] = quantize_bgra(v.x, v.y, v.z, v.w, L.xform, s_steps);
+}
+
+constexpr int PTW = 32;    // general kernel: output tile width (one warp lane per output column)
+constexpr int PTH = 16;    // general kernel: output tile height
+constexpr int PMAXW = 32;  // widest window handled
 constexpr int PTHREADS = 256;
 constexpr int PWARPS = PTHREADS / 32;
 
-// One CTA per PTW x PTH output tile, all four channels at once (RGBA as float4 in shared memory):
-//  1. wrap maps for the tile's source rows and columns (FloatImage::index, one wrap per row/column),
-//  2. the wrapped source window staged once as float4 (from planar FP32 or BGRA8 + input table),
-//  3. X taps for every window row into a (rows x PTW) float4 plane,
-//  4. Y taps, written as four planes and, optionally, the quantised BGRA8 word.
-// Channel arithmetic is the reference's, lane by lane: sum starts at 0 and adds k * v in tap order.
+// General kernel, any scale and window (odd sizes, 1-wide axes). One CTA per PTW x PTH output
+// tile: wrap maps for the tile's source rows and columns, the wrapped source window staged once as
+// float4, X taps for every window row into a (rows x PTW) plane, then the Y taps.
 template <bool WEIGHTED, bool SRC_U8>
-__global__ void __launch_bounds__(PTHREADS) k_poly(PolyLevel L) {
+__global__ void __launch_bounds__(PTHREADS) k_poly(const MipJob *__restrict__ jobs, int njobs) {
     extern __shared__ float4 sm4[];
-    const int ox0 = blockIdx.x * PTW, oy0 = blockIdx.y * PTH;
+    __shared__ float s_kx[PTW * PMAXW], s_ky[PTH * PMAXW], s_steps[256];
+    __shared__ int s_lx[PTW], s_ly[PTH];
+    load_steps(jobs, s_steps);
+    const MipJob &L = jobs[find_mip_job(jobs, njobs, blockIdx.x)];
+    const int lu = (int)(blockIdx.x - L.first_unit);
+    const int ox0 = (lu % L.tiles_x) * PTW, oy0 = (lu / L.tiles_x) * PTH;
     const int tw = min(PTW, L.w - ox0), th = min(PTH, L.h - oy0);
-    const int xlo = L.lx[ox0], xhi = L.lx[ox0 + tw - 1] + L.wsx - 1;
-    const int ylo = L.ly[oy0], yhi = L.ly[oy0 + th - 1] + L.wsy - 1;
+    const int wsx = L.wsx, wsy = L.wsy;
+    const int xlo = L.lx[ox0], xhi = L.lx[ox0 + tw - 1] + wsx - 1;
+    const int ylo = L.ly[oy0], yhi = L.ly[oy0 + th - 1] + wsy - 1;
     const int rx = xhi - xlo + 1, ry = yhi - ylo + 1;
     float4 *s_in = sm4;                 // ry * rx
     float4 *s_tmp = s_in + ry * rx;     // ry * PTW
     int *s_col = reinterpret_cast<int *>(s_tmp + ry * PTW);  // rx
     int *s_row = s_col + rx;                                  // ry
-    __shared__ float s_kx[PTW * PMAXW], s_ky[PTH * PMAXW], s_steps[256], s_lut[256];
-    __shared__ int s_lx[PTW], s_ly[PTH];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < tw * L.wsx; i += PTHREADS) s_kx[i] = L.kx[(size_t)ox0 * L.wsx + i];
-    for (int i = tid; i < th * L.wsy; i += PTHREADS) s_ky[i] = L.ky[(size_t)oy0 * L.wsy + i];
+    for (int i = tid; i < tw * wsx; i += PTHREADS) s_kx[i] = L.kx[(size_t)ox0 * wsx + i];
+    for (int i = tid; i < th * wsy; i += PTHREADS) s_ky[i] = L.ky[(size_t)oy0 * wsy + i];
     if (tid < tw) s_lx[tid] = L.lx[ox0 + tid] - xlo;
     if (tid < th) s_ly[tid] = L.ly[oy0 + tid] - ylo;
     for (int i = tid; i < rx; i += PTHREADS) s_col[i] = wrap_index(xlo + i, L.W, L.wrap);
     for (int i = tid; i < ry; i += PTHREADS) s_row[i] = wrap_index(ylo + i, L.H, L.wrap);
-    if (L.q_out && L.q.xform == 2) for (int i = tid; i < 256; i += PTHREADS) s_steps[i] = L.q.steps[i];
-    if (SRC_U8) for (int i = tid; i < 256; i += PTHREADS) s_lut[i] = L.lut[i];
     __syncthreads();
 
     const size_t sn = (size_t)L.W * L.H;
     for (int r = warp; r < ry; r += PWARPS) {
         const size_t rowoff = (size_t)s_row[r] * L.W;
-        float4 *dst = s_in + r * rx;
-        for (int x = lane; x < rx; x += 32) {
-            const size_t s = rowoff + s_col[x];
-            float4 v;
-            if (SRC_U8) {
-                const uint32_t p = L.bgra8[s];
-                v = make_float4(s_lut[(p >> 16) & 255], s_lut[(p >> 8) & 255], s_lut[p & 255], (float)(p >> 24) / 255.0f);
-            } else {
-                v = make_float4(L.src[s], L.src[sn + s], L.src[2 * sn + s], L.src[3 * sn + s]);
-            }
-            dst[x] = v;
-        }
+        for (int x = lane; x < rx; x += 32) s_in[r * rx + x] = load_texel<SRC_U8>(L, rowoff + s_col[x], sn);
     }
     __syncthreads();
 
-    // X taps: one lane per output column, warps over the window rows
-    if (lane < tw) {
-        const float *k = s_kx + lane * L.wsx;
+    if (lane < tw) {  // X taps: one lane per output column, warps over the window rows
+        const float *k = s_kx + lane * wsx;
         const int off = s_lx[lane];
         for (int r = warp; r < ry; r += PWARPS) {
             const float4 *row = s_in + r * rx + off;
             float4 sum = make_float4(0, 0, 0, 0);
-            if (WEIGHTED) {
-                float norm = 0;
-                for (int j = 0; j < L.wsx; j++) {
-                    const float4 v = row[j];
-                    const float kj = k[j];
-                    const float wgt = kj * (v.w + (1.0f / 256.0f));
-                    norm += wgt;
-                    sum.x += wgt * v.x; sum.y += wgt * v.y; sum.z += wgt * v.z;
-                    sum.w += kj * v.w;
-                }
-                sum.x = sum.x / norm; sum.y = sum.y / norm; sum.z = sum.z / norm;
-            } else {
-                for (int j = 0; j < L.wsx; j++) {
-                    const float4 v = row[j];
-                    const float kj = k[j];
-                    sum.x += kj * v.x; sum.y += kj * v.y; sum.z += kj * v.z; sum.w += kj * v.w;
-                }
-            }
-            s_tmp[r * PTW + lane] = sum;
+            float norm = 0;
+            for (int j = 0; j < wsx; j++) tap<WEIGHTED>(sum, norm, k[j], row[j]);
+            s_tmp[r * PTW + lane] = finish<WEIGHTED>(sum, norm);
         }
     }
     __syncthreads();
 
-    // Y taps: one lane per output column, warps over the output rows
-    if (lane < tw) {
+    if (lane < tw) {  // Y taps: one lane per output column, warps over the output rows
         const size_t dn = (size_t)L.w * L.h;
         for (int y = warp; y < th; y += PWARPS) {
-            const float *k = s_ky + y * L.wsy;
+            const float *k = s_ky + y * wsy;
             const float4 *col = s_tmp + s_ly[y] * PTW + lane;
             float4 sum = make_float4(0, 0, 0, 0);
-            if (WEIGHTED) {
-                float norm = 0;
-                for (int j = 0; j < L.wsy; j++) {
-                    const float4 v = col[j * PTW];
-                    const float kj = k[j];
-                    const float wgt = kj * (v.w + (1.0f / 256.0f));
-                    norm += wgt;
-                    sum.x += wgt * v.x; sum.y += wgt * v.y; sum.z += wgt * v.z;
-                    sum.w += kj * v.w;
-                }
-                sum.x = sum.x / norm; sum.y = sum.y / norm; sum.z = sum.z / norm;
-            } else {
-                for (int j = 0; j < L.wsy; j++) {
-                    const float4 v = col[j * PTW];
-                    const float kj = k[j];
-                    sum.x += kj * v.x; sum.y += kj * v.y; sum.z += kj * v.z; sum.w += kj * v.w;
+            float norm = 0;
+            for (int j = 0; j < wsy; j++) tap<WEIGHTED>(sum, norm, k[j], col[j * PTW]);
+            store_texel(L, (size_t)(oy0 + y) * L.w + ox0 + lane, dn, finish<WEIGHTED>(sum, norm), s_steps);
+        }
+    }
+}
+
+// Exact 2:1 kernel (both axes halve and every output has the same taps: power-of-two chains).
+// One warp per strip of 32 output columns x `strip` output rows sweeps the source rows top to
+// bottom, two rows per step. Each source row is staged once in shared memory (wrapped, even and
+// odd columns in separate halves so the stride-2 tap reads are conflict-free), its X taps are
+// computed per lane, and the result goes into the running Y sums of the outputs whose window
+// contains the row. Output t's window starts at row 2t, so at step p the NS open sums belong to
+// outputs p, p-1, ..., p-NS+1: row 2p gives sum d its tap 2d and row 2p+1 its tap 2d+1, the
+// oldest sum is then complete and written, and the window slides by one output. Every sum starts
+// at 0 and receives its taps in order, exactly like applyKernelY's loop.
+template <int WS>
+struct Poly2x {
+    static_assert(WS % 2 == 1, "odd windows");
+    static constexpr int NS = (WS + 1) / 2;        // open output sums
+    static constexpr int SPAN = 62 + WS;           // source columns of 32 output columns
+    static constexpr int HALF = ((SPAN + 1) / 2 + 3) / 8 * 8 + 4;  // >= SPAN/2, = 4 mod 8: conflict-free stores
+    static constexpr int ROW = 2 * HALF;           // float4 per staged row
+    static constexpr int WARP_F4 = 2 * ROW + 8 + 128;          // per-warp shared memory in float4
+};
+
+// A source texel as loaded (BGRA8 word or four FP32 planes), converted to float4 when staged.
+template <bool SRC_U8> struct RawTexel;
+template <> struct RawTexel<true> { uint32_t v; };
+template <> struct RawTexel<false> { float4 v; };
+
+template <bool SRC_U8>
+__device__ __forceinline__ void fetch_raw(const MipJob &L, size_t s, size_t sn, RawTexel<SRC_U8> &r) {
+    if constexpr (SRC_U8) r.v = __ldg(L.bgra8 + s);
+    else r.v = make_float4(__ldg(L.src + s), __ldg(L.src + sn + s), __ldg(L.src + 2 * sn + s), __ldg(L.src + 3 * sn + s));
+}
+
+template <bool SRC_U8>
+__device__ __forceinline__ float4 convert_raw(const float *lut, const RawTexel<SRC_U8> &r) {
+    if constexpr (SRC_U8) {
+        const uint32_t p = r.v;
+        return make_float4(__ldg(lut + ((p >> 16) & 255)), __ldg(lut + ((p >> 8) & 255)), __ldg(lut + (p & 255)),
+                           (float)(p >> 24) / 255.0f);
+    } else {
+        return r.v;
+    }
+}
+
+// Loads two source rows of a strip (wrapped) into registers.
+struct RowFetch {
+    int r0, S, H, W, wrap, c0, span;
+    bool interior;
+    int lane;
+    size_t sn;
+    template <bool SRC_U8, int CPL>
+    __device__ __forceinline__ void pair(const MipJob &L, RawTexel<SRC_U8> (&pre)[2][CPL], int sa) const {
+#pragma unroll
+        for (int rr = 0; rr < 2; rr++) {
+            if (sa + rr < S) {
+                const int gy = r0 + sa + rr;
+                const size_t rowoff = (size_t)(gy >= 0 && gy < H ? gy : wrap_index(gy, H, wrap)) * W;
+#pragma unroll
+                for (int k = 0; k < CPL; k++) {
+                    const int c = lane + 32 * k;
+                    if (c < span) fetch_raw<SRC_U8>(L, rowoff + (interior ? c0 + c : wrap_index(c0 + c, W, wrap)), sn, pre[rr][k]);
                 }
             }
-            const size_t o = (size_t)(oy0 + y) * L.w + ox0 + lane;
-            L.dst[o] = sum.x;
-            L.dst[dn + o] = sum.y;
-            L.dst[2 * dn + o] = sum.z;
-            L.dst[3 * dn + o] = sum.w;
-            if (L.q_out) L.q_out[o] = quantize_bgra(sum.x, sum.y, sum.z, sum.w, L.q.xform, s_steps);
         }
+    }
+};
+
+template <int WS, bool WEIGHTED, bool SRC_U8>
+__global__ void __launch_bounds__(256, 2) k_poly2x(const MipJob *__restrict__ jobs, int njobs, long long units) {
+    using P = Poly2x<WS>;
+    constexpr int NS = P::NS, HALF = P::HALF, ROW = P::ROW;
+    constexpr int CPL = (P::SPAN + 31) / 32;  // staged columns per lane
+    extern __shared__ float4 sm4[];
+    __shared__ float s_steps[256];
+    load_steps(jobs, s_steps);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long u = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    if (u >= units) return;
+    const MipJob &L = jobs[find_mip_job(jobs, njobs, u)];
+    const long long lu = u - L.first_unit;
+    const int x0 = (int)(lu % L.tiles_x) * 32, y0 = (int)(lu / L.tiles_x) * L.strip;
+    const int W = L.W, H = L.H, w = L.w, wrap = L.wrap;
+    const int tv = min(L.strip, L.h - y0);
+    const int x = x0 + lane;
+    const bool xv = x < w;
+    // per-warp shared memory: two staged rows, the X and Y weights, then (8-bit source) the input
+    // table of RGB and alpha
+    float4 *buf = sm4 + warp * P::WARP_F4;
+    float *s_k = reinterpret_cast<float *>(buf + 2 * ROW);     // kx [16], ky [16]
+    float *s_lut = s_k + 32;
+    if (lane < WS) {
+        s_k[lane] = __ldg(L.kx + lane);
+        s_k[16 + lane] = __ldg(L.ky + lane);
+    }
+    if constexpr (SRC_U8)
+        for (int i = lane; i < 512; i += 32) s_lut[i] = __ldg(L.lut + i);
+    const int c0 = 2 * x0 + L.cx, r0 = 2 * y0 + L.cy;
+    const int span = 2 * (min(32, w - x0) - 1) + WS;
+    const bool interior = c0 >= 0 && c0 + span <= W;
+    const size_t sn = (size_t)W * H, dn = (size_t)w * L.h;
+    const int S = 2 * tv + WS - 2;   // source rows of the strip
+    const int steps = tv + NS - 1;   // row pairs
+
+    // source rows go through registers one pair ahead of the taps
+    RawTexel<SRC_U8> pre[2][CPL];
+    const RowFetch F{r0, S, H, W, wrap, c0, span, interior, lane, sn};
+
+    // open Y sums (norm: the alpha-weighted kernels' running weight)
+    float4 acc[NS];
+    float nrm[NS];
+#pragma unroll
+    for (int d = 0; d < NS; d++) { acc[d] = make_float4(0, 0, 0, 0); nrm[d] = 0; }
+
+    F.pair<SRC_U8, CPL>(L, pre, 0);
+#pragma unroll 1
+    for (int p = 0; p < steps; p++) {
+        const int sa = 2 * p;
+        __syncwarp();
+#pragma unroll
+        for (int rr = 0; rr < 2; rr++) {
+            if (sa + rr < S) {
+#pragma unroll
+                for (int k = 0; k < CPL; k++) {
+                    const int c = lane + 32 * k;
+                    if (c < span) {
+                        float4 v;
+                        if constexpr (SRC_U8) {
+                            const uint32_t q = pre[rr][k].v;
+                            v = make_float4(s_lut[(q >> 16) & 255], s_lut[(q >> 8) & 255], s_lut[q & 255], s_lut[256 + (q >> 24)]);
+                        } else {
+                            v = pre[rr][k].v;
+                        }
+                        buf[rr * ROW + (c & 1) * HALF + (c >> 1)] = v;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (sa + 2 < S) F.pair<SRC_U8, CPL>(L, pre, sa + 2);
+
+        const int t = p - (NS - 1);  // the oldest sum completes with row 2p
+        const bool emit = t >= 0 && t < tv && xv;
+        const size_t o = (size_t)(y0 + t) * w + x;
+        float4 h[2];
+#pragma unroll
+        for (int rr = 0; rr < 2; rr++) {
+            const float4 *row = buf + rr * ROW + lane;
+            float4 sum = make_float4(0, 0, 0, 0);
+            float norm = 0;
+#pragma unroll
+            for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, s_k[j], row[(j & 1) * HALF + (j >> 1)]);
+            h[rr] = finish<WEIGHTED>(sum, norm);
+        }
+        // row 2p: tap 2d of output p - d (the newest sum starts here)
+        acc[0] = make_float4(0, 0, 0, 0);
+        nrm[0] = 0;
+#pragma unroll
+        for (int d = 0; d < NS; d++) tap<WEIGHTED>(acc[d], nrm[d], s_k[16 + 2 * d], h[0]);
+        if (emit) store_texel(L, o, dn, finish<WEIGHTED>(acc[NS - 1], nrm[NS - 1]), s_steps);
+        // row 2p + 1: tap 2d + 1, then slide the window by one output
+#pragma unroll
+        for (int d = NS - 2; d >= 0; d--) {
+            tap<WEIGHTED>(acc[d], nrm[d], s_k[16 + 2 * d + 1], h[1]);
+            acc[d + 1] = acc[d];
+            nrm[d + 1] = nrm[d];
+        }
+    }
+}
+
+// Chain tails: once a texture's level is small (at most TAIL_MAX texels), one CTA finishes every
+// remaining level in shared memory, one level after the other, instead of one latency-bound
+// launch per tiny level. Levels are planar FP32 in shared memory; each polyphase step runs the
+// X pass over every source row into a plane, then the Y pass (applyKernelX / applyKernelY order),
+// box steps use the fastDownSample formulas; every level is also written out. The jobs of a tail
+// are consecutive in the list: the first carries the number of levels in tiles_x, and all carry
+// the chain's index in first_unit.
+constexpr int TAIL_MAX = 4096;
+
+__device__ __forceinline__ float fast_box_texel(const float *src, int W, int H, unsigned w, unsigned h, unsigned t) {
+    const unsigned x = t % w, y = t / w;
+    if (W == 1 || H == 1) {
+        const unsigned n = w * h, i = t;
+        const float *s = src + 2 * (size_t)i;
+        if (((unsigned)W * (unsigned)H) & 1) {
+            const float scale = 1.0f / (2 * n + 1);
+            const float w0 = (float)(n - i), w1 = (float)(n - 0), w2 = (float)(1 + i);
+            return scale * (w0 * s[0] + w1 * s[1] + w2 * s[2]);
+        }
+        return 0.5f * (s[0] + s[1]);
+    }
+    const float *s = src + (size_t)(2 * y) * W + 2 * x;
+    if ((W & 1) == 0 && (H & 1) == 0) return 0.25f * (s[0] + s[1] + s[W] + s[W + 1]);
+    if ((W & 1) && (H & 1)) {
+        const float scale = 1.0f / (float)((unsigned)W * (unsigned)H);
+        const float v0 = (float)(h - y), v1 = (float)(h - 0), v2 = (float)(1 + y);
+        const float w0 = (float)(w - x), w1 = (float)(w - 0), w2 = (float)(1 + x);
+        float acc = 0.0f;
+        acc += v0 * (w0 * s[0] + w1 * s[1] + w2 * s[2]);
+        acc += v1 * (w0 * s[W] + w1 * s[W + 1] + w2 * s[W + 2]);
+        acc += v2 * (w0 * s[2 * W] + w1 * s[2 * W + 1] + w2 * s[2 * W + 2]);
+        return acc * scale;
+    }
+    if (W & 1) {
+        const float scale = 1.0f / (float)(2 * (unsigned)W);
+        const float w0 = (float)(w - x), w1 = (float)(w - 0), w2 = (float)(1 + x);
+        float acc = 0.0f;
+        acc += w0 * (s[0] + s[W]);
+        acc += w1 * (s[1] + s[W + 1]);
+        acc += w2 * (s[2] + s[W + 2]);
+        return acc * scale;
+    }
+    const float scale = 1.0f / (float)(2 * (unsigned)H);
+    const float v0 = (float)(h - y), v1 = (float)(h - 0), v2 = (float)(1 + y);
+    float acc = 0.0f;
+    acc += v0 * (s[0] + s[1]);
+    acc += v1 * (s[W] + s[W + 1]);
+    acc += v2 * (s[2 * W] + s[2 * W + 1]);
+    return acc * scale;
+}
+
+size_t tail_smem_bytes() { return (size_t)4 * (TAIL_MAX + TAIL_MAX / 2 + TAIL_MAX / 2) * sizeof(float); }
+
+template <bool WEIGHTED>
+__global__ void __launch_bounds__(256) k_mip_tail(const MipJob *__restrict__ jobs, int njobs) {
+    extern __shared__ float4 sm4[];
+    __shared__ float s_steps[256];
+    float *s_a = reinterpret_cast<float *>(sm4);  // source level, 4 planes of up to TAIL_MAX
+    float *s_t = s_a + 4 * TAIL_MAX;              // X pass, 4 planes of up to TAIL_MAX / 2
+    float *s_b = s_t + 2 * TAIL_MAX;              // destination level, 4 planes of up to TAIL_MAX / 2
+    load_steps(jobs, s_steps);
+    int j0 = 0, hi = njobs - 1;  // first job of chain blockIdx.x
+    while (j0 < hi) {
+        const int mid = (j0 + hi) >> 1;
+        if (jobs[mid].first_unit < (long long)blockIdx.x) j0 = mid + 1;
+        else hi = mid;
+    }
+    const int count = jobs[j0].tiles_x;
+    {  // stage the chain's source level
+        const MipJob &L = jobs[j0];
+        const int n = L.W * L.H;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            if (L.src) {
+#pragma unroll
+                for (int c = 0; c < 4; c++) s_a[c * n + i] = L.src[(size_t)c * n + i];
+            } else {
+                const uint32_t q = L.bgra8[i];
+                s_a[i] = __ldg(L.lut + ((q >> 16) & 255));
+                s_a[n + i] = __ldg(L.lut + ((q >> 8) & 255));
+                s_a[2 * n + i] = __ldg(L.lut + (q & 255));
+                s_a[3 * n + i] = __ldg(L.lut + 256 + (q >> 24));
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < count; k++) {
+        const MipJob &L = jobs[j0 + k];
+        const int W = L.W, H = L.H, w = L.w, h = L.h;
+        const int sn = W * H, tn = H * w, dn = w * h;
+        if (L.kx == nullptr) {
+            for (int o = threadIdx.x; o < dn; o += blockDim.x)
+#pragma unroll
+                for (int c = 0; c < 4; c++) s_b[c * dn + o] = fast_box_texel(s_a + c * sn, W, H, w, h, o);
+        } else {
+            for (int i = threadIdx.x; i < tn; i += blockDim.x) {  // X taps of every source row
+                const int x = i % w, y = i / w;
+                const float *kx = L.kx + (size_t)x * L.wsx;
+                const int lx = L.lx[x];
+                float4 sum = make_float4(0, 0, 0, 0);
+                float norm = 0;
+                for (int j = 0; j < L.wsx; j++) {
+                    const int s = y * W + wrap_index(lx + j, W, L.wrap);
+                    tap<WEIGHTED>(sum, norm, kx[j], make_float4(s_a[s], s_a[sn + s], s_a[2 * sn + s], s_a[3 * sn + s]));
+                }
+                sum = finish<WEIGHTED>(sum, norm);
+                s_t[i] = sum.x; s_t[tn + i] = sum.y; s_t[2 * tn + i] = sum.z; s_t[3 * tn + i] = sum.w;
+            }
+            __syncthreads();
+            for (int o = threadIdx.x; o < dn; o += blockDim.x) {  // Y taps
+                const int x = o % w, y = o / w;
+                const float *ky = L.ky + (size_t)y * L.wsy;
+                const int ly = L.ly[y];
+                float4 sum = make_float4(0, 0, 0, 0);
+                float norm = 0;
+                for (int j = 0; j < L.wsy; j++) {
+                    const int s = wrap_index(ly + j, H, L.wrap) * w + x;
+                    tap<WEIGHTED>(sum, norm, ky[j], make_float4(s_t[s], s_t[tn + s], s_t[2 * tn + s], s_t[3 * tn + s]));
+                }
+                sum = finish<WEIGHTED>(sum, norm);
+                s_b[o] = sum.x; s_b[dn + o] = sum.y; s_b[2 * dn + o] = sum.z; s_b[3 * dn + o] = sum.w;
+            }
+        }
+        __syncthreads();
+        for (int o = threadIdx.x; o < dn; o += blockDim.x)
+            store_texel(L, (size_t)o, (size_t)dn, make_float4(s_b[o], s_b[dn + o], s_b[2 * dn + o], s_b[3 * dn + o]), s_steps);
+        // the destination becomes the next source (s_b is at most TAIL_MAX / 2 per plane)
+        for (int i = threadIdx.x; i < dn; i += blockDim.x)
+#pragma unroll
+            for (int c = 0; c < 4; c++) s_a[c * dn + i] = s_b[c * dn + i];
+        __syncthreads();
     }
 }
 
@@ -349,43 +645,79 @@ int launch_quantize(const float *rgba, size_t n, int xform, const float *steps, 
     return launch_status();
 }
 
-int launch_fast_down(const float *src, int W, int H, float *dst, uint32_t *q_out, int xform, const float *steps,
-                     cudaStream_t s) {
-    const size_t dn = (size_t)(W / 2 > 1 ? W / 2 : 1) * (H / 2 > 1 ? H / 2 : 1);
-    k_fast_down<<<grid_for(dn, 256), 256, 0, s>>>(src, W, H, dst, q_out, Quant{xform, steps});
+template <bool W, bool U8>
+static int launch_poly_t(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
+    static std::atomic<unsigned long long> configured{0};
+    if (first_use_on_device(configured))
+        cudaFuncSetAttribute(k_poly<W, U8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    k_poly<W, U8><<<(unsigned)m.units, PTHREADS, m.smem, s>>>(jobs, m.njobs);
     return launch_status();
 }
 
-size_t poly_smem_bytes(int rx_max, int ry_max, bool) {
+template <int WS, bool W, bool U8>
+static int launch_poly2x_t(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
+    const int warps = m.threads / 32;
+    const long long grid = (m.units + warps - 1) / warps;
+    k_poly2x<WS, W, U8><<<(unsigned)grid, m.threads, m.smem, s>>>(jobs, m.njobs, m.units);
+    return launch_status();
+}
+
+template <int WS>
+static int launch_poly2x_ws(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
+    if (m.weighted) return m.u8 ? launch_poly2x_t<WS, true, true>(m, jobs, s) : launch_poly2x_t<WS, true, false>(m, jobs, s);
+    return m.u8 ? launch_poly2x_t<WS, false, true>(m, jobs, s) : launch_poly2x_t<WS, false, false>(m, jobs, s);
+}
+
+bool poly2x_supported(int ws) { return ws == 3 || ws == 5 || ws == 13; }
+
+size_t poly_smem_bytes(int rx_max, int ry_max) {
     return (size_t)ry_max * rx_max * sizeof(float4) + (size_t)ry_max * PTW * sizeof(float4) +
            (size_t)(rx_max + ry_max) * sizeof(int);
 }
 
-template <bool W, bool U8>
-static int launch_poly_t(const PolyLevel &L, size_t sm, cudaStream_t s) {
-    static std::atomic<unsigned long long> configured{0};
-    if (first_use_on_device(configured))
-        cudaFuncSetAttribute(k_poly<W, U8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    dim3 grid((L.w + PTW - 1) / PTW, (L.h + PTH - 1) / PTH);
-    k_poly<W, U8><<<grid, PTHREADS, sm, s>>>(L);
-    return launch_status();
+size_t poly2x_smem_bytes(int ws, int threads) {
+    const int per_warp = ws == 3 ? Poly2x<3>::WARP_F4 : ws == 5 ? Poly2x<5>::WARP_F4 : Poly2x<13>::WARP_F4;
+    return (size_t)(threads / 32) * per_warp * sizeof(float4);
 }
 
-int launch_poly(const PolyArgs &a, cudaStream_t s) {
-    PolyLevel L;
-    L.src = a.src; L.bgra8 = a.bgra8; L.lut = a.lut;
-    L.W = a.W; L.H = a.H; L.w = a.w; L.h = a.h;
-    L.wsx = a.wsx; L.wsy = a.wsy; L.kx = a.kx; L.ky = a.ky; L.lx = a.lx; L.ly = a.ly;
-    L.wrap = a.wrap; L.dst = a.dst; L.q_out = a.q_out; L.q = Quant{a.xform, a.steps};
-    const size_t sm = poly_smem_bytes(a.rx_max, a.ry_max, a.weighted);
-    if (a.wsx > PMAXW || a.wsy > PMAXW || sm > 200 * 1024) return 2;  // Error_UnsupportedFeature
-    const bool u8 = a.src == nullptr;
-    if (a.weighted) return u8 ? launch_poly_t<true, true>(L, sm, s) : launch_poly_t<true, false>(L, sm, s);
-    return u8 ? launch_poly_t<false, true>(L, sm, s) : launch_poly_t<false, false>(L, sm, s);
+int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s) {
+    if (m.units <= 0 || m.njobs <= 0) return 0;
+    const MipJob *jobs = d_jobs + m.first_job;
+    switch (m.kernel) {
+        case MIP_FAST_BOX: {
+            const long long cap = 152LL * 64, g = (m.units + 255) / 256;
+            k_fast_down<<<(unsigned)(g < cap ? g : cap), 256, 0, s>>>(jobs, m.njobs, m.units);
+            return launch_status();
+        }
+        case MIP_POLY:
+            if (m.smem > 200 * 1024) return 2;  // Error_UnsupportedFeature
+            if (m.weighted) return m.u8 ? launch_poly_t<true, true>(m, jobs, s) : launch_poly_t<true, false>(m, jobs, s);
+            return m.u8 ? launch_poly_t<false, true>(m, jobs, s) : launch_poly_t<false, false>(m, jobs, s);
+        case MIP_TAIL: {
+            static std::atomic<unsigned long long> configured{0};
+            if (first_use_on_device(configured)) {
+                cudaFuncSetAttribute(k_mip_tail<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem_bytes());
+                cudaFuncSetAttribute(k_mip_tail<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem_bytes());
+            }
+            if (m.weighted) k_mip_tail<true><<<(unsigned)m.units, 256, tail_smem_bytes(), s>>>(jobs, m.njobs);
+            else k_mip_tail<false><<<(unsigned)m.units, 256, tail_smem_bytes(), s>>>(jobs, m.njobs);
+            return launch_status();
+        }
+        case MIP_POLY2X:
+            if (m.threads < 32 || m.threads > 256 || m.threads % 32) return 1;
+            if (m.ws == 3) return launch_poly2x_ws<3>(m, jobs, s);
+            if (m.ws == 5) return launch_poly2x_ws<5>(m, jobs, s);
+            if (m.ws == 13) return launch_poly2x_ws<13>(m, jobs, s);
+            return 2;
+        default:
+            return 1;
+    }
 }
 
 int poly_tile_w() { return PTW; }
 int poly_tile_h() { return PTH; }
+int poly_max_window() { return PMAXW; }
+int tail_max_texels() { return TAIL_MAX; }
 
 NTG_DEFINE_TABLE_UPLOAD(upload_tables_mip)
 
