@@ -152,6 +152,40 @@ int ntg_compress_chain_host(ntg_context *ctx, const void *h_bgra, int w, int h, 
 int ntg_mip_chain(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
                   float *d_levels, void *stream);
 
+/* ---- batches: many textures of uneven sizes, whole chains, one CUDA graph ----
+ * No counterpart in the reference, which compresses one image per Compressor::process call
+ * (src/nvtt/Context.cpp:217-346); a batch runs that loop for every texture at once. Each
+ * texture's chain gives the same blocks as ntg_compress_chain with the same options. The plan
+ * groups the level steps of all textures by depth (one mip launch per depth and kernel variant;
+ * the small last levels of all textures in one tail launch), encodes every level of every texture
+ * with one launch per (format, quality), and captures the sequence in a CUDA graph. The device
+ * pointers are baked into the graph: to compress new images, write them into the same input
+ * buffers and launch again. A batch uses its context's tables and must be destroyed first. */
+typedef struct ntg_batch ntg_batch;
+typedef struct ntg_batch_texture {
+    const void *d_bgra;        /* device BGRA8 level 0, w * h words */
+    int w, h;
+    ntg_chain_options opt;
+    void *d_blocks;            /* device output, ntg_chain_bytes(w, h, &opt) bytes */
+} ntg_batch_texture;
+
+/* Plans the batch, allocates its level workspace (FP32 + BGRA8 levels of every texture), runs the
+ * sequence once (this computes the outputs) and captures it. Launch shapes come from the tuning
+ * cache when it holds an entry for this device and batch (file: $NTG_TUNE_CACHE, else
+ * $HOME/.cache/ntg_tune.json), else defaults. */
+int ntg_batch_build(ntg_context *ctx, const ntg_batch_texture *textures, int count, ntg_batch **out);
+/* Replays the graph on `stream` (enqueue only). */
+int ntg_batch_launch(ntg_batch *batch, void *stream);
+/* Times candidate launch shapes on this batch (rows per strip and threads per CTA of the 2:1 mip
+ * kernel, the tail threshold, blocks per CTA of each encoder), keeps the fastest, recaptures the
+ * graph and stores the choice in the tuning cache. Synchronises `stream`. */
+int ntg_batch_autotune(ntg_batch *batch, void *stream);
+/* Texels of all levels, 4x4 blocks, kernel launches per replay, and the launch shapes in use:
+ * shape[] = {strip, threads, tail texels, bc1 blocks/CTA, bc3 blocks/CTA, bc5 blocks/CTA}.
+ * Any pointer may be NULL. */
+int ntg_batch_info(const ntg_batch *batch, long long *texels, long long *blocks, int *launches, int shape[6]);
+int ntg_batch_destroy(ntg_batch *batch);
+
 /* Phase timing of chain calls: when enabled, ntg_compress_chain records CUDA events on its stream
  * around the mip phase and the encode phase; ntg_profile_read waits for the last call's events and
  * returns the two durations in milliseconds. */

@@ -4,10 +4,14 @@
 
 #include <cuda_runtime.h>
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -464,10 +468,11 @@ int upload_jobs(ntg_context *ctx, const std::vector<EncJob> &jobs, cudaStream_t 
     return NTG_OK;
 }
 
-int launch_encode(int format, const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s) {
-    int r = format == NTG_FORMAT_BC1 ? launch_bc1(d_jobs, njobs, nblocks, quality, s)
-            : format == NTG_FORMAT_BC3 ? launch_bc3(d_jobs, njobs, nblocks, quality, s)
-                                       : launch_bc5(d_jobs, njobs, nblocks, quality, s);
+int launch_encode(int format, const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s,
+                  int threads = 0) {
+    int r = format == NTG_FORMAT_BC1 ? launch_bc1(d_jobs, njobs, nblocks, quality, threads, s)
+            : format == NTG_FORMAT_BC3 ? launch_bc3(d_jobs, njobs, nblocks, quality, threads, s)
+                                       : launch_bc5(d_jobs, njobs, nblocks, quality, threads, s);
     return launched(r, "encoder launch");
 }
 
@@ -800,6 +805,438 @@ int ntg_error_sums(ntg_context *ctx, const float *d_ref, const float *d_img, int
     if (!ctx || !d_ref || !d_img || !d_sums || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
     NTG_TRY(ensure_device(ctx));
     return launched(launch_rms(d_ref, d_img, w, h, alpha_mode, d_sums, S(stream)), "error sums");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Batches: every texture's chain planned together, launched as one CUDA graph.
+
+struct ntg_batch {
+    ntg_context *ctx = nullptr;
+    std::vector<ntg_batch_texture> tex;
+    std::vector<ntg_chain_options> opts;  // normalised
+    std::vector<ChainPlan> plans;
+    std::vector<const XformTables *> xts;
+    std::vector<size_t> base;             // workspace offset of each texture's levels
+    uint8_t *d_ws = nullptr;
+    MipJob *d_mip = nullptr;
+    EncJob *d_enc = nullptr;
+    std::vector<int> set_images;          // textures whose level 0 is materialised (box path)
+    std::vector<std::vector<MipLaunch>> stages;
+    struct Enc {
+        int format, quality, first, njobs;
+        long long nblocks;
+    };
+    std::vector<Enc> encodes;
+    MipTuning tune;
+    int enc_threads[3] = {64, 128, 128};  // blocks per CTA of the BC1, BC3, BC5 encoders
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long texels = 0, blocks = 0;
+    int launches = 0;
+    std::string key;                      // tuning-cache key (device | batch signature)
+
+    ~ntg_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (d_ws) cudaFree(d_ws);
+        if (d_mip) cudaFree(d_mip);
+        if (d_enc) cudaFree(d_enc);
+    }
+};
+
+namespace {
+
+int enc_slot(int format) { return format == NTG_FORMAT_BC1 ? 0 : format == NTG_FORMAT_BC3 ? 1 : 2; }
+
+// Plans the mip stages and encode launches of a batch for its current tuning and uploads the job
+// lists (the workspace layout does not depend on the tuning).
+int batch_plan(ntg_batch *b) {
+    ntg_context *ctx = b->ctx;
+    const size_t n = b->tex.size();
+    std::vector<MipJob> all;
+    b->stages.clear();
+    b->set_images.clear();
+    size_t max_levels = 0;
+    std::vector<size_t> tails(n);
+    for (size_t t = 0; t < n; t++) {
+        max_levels = std::max(max_levels, b->plans[t].lv.size());
+        tails[t] = tail_start(b->plans[t], b->tune);
+        if (b->plans[t].f_off[0] != NONE) b->set_images.push_back((int)t);
+    }
+    for (size_t l = 1; l < max_levels; l++) {
+        std::vector<std::pair<MipKey, MipJob>> items;
+        for (size_t t = 0; t < n; t++) {
+            const ChainPlan &P = b->plans[t];
+            if (l >= P.lv.size() || l >= tails[t]) continue;
+            items.emplace_back();
+            NTG_TRY(chain_step(ctx, P, l, (const uint32_t *)b->tex[t].d_bgra, b->opts[t], b->xts[t], b->d_ws + b->base[t],
+                               items.back().second, items.back().first));
+        }
+        std::vector<MipLaunch> stage;
+        if (!items.empty()) group_launches(items, b->tune, all, stage);
+        for (int weighted = 0; weighted < 2; weighted++) {  // tails starting at this level
+            MipLaunch m;
+            std::memset(&m, 0, sizeof m);
+            m.kernel = MIP_TAIL;
+            m.weighted = weighted;
+            m.first_job = (int)all.size();
+            long long chains = 0;
+            for (size_t t = 0; t < n; t++) {
+                if (tails[t] != l || (b->opts[t].weighted != 0) != (weighted != 0)) continue;
+                NTG_TRY(chain_tail(ctx, b->plans[t], l, (const uint32_t *)b->tex[t].d_bgra, b->opts[t], b->xts[t],
+                                   b->d_ws + b->base[t], chains++, all));
+            }
+            if (chains) {
+                m.njobs = (int)all.size() - m.first_job;
+                m.units = chains;
+                stage.push_back(m);
+            }
+        }
+        if (!stage.empty()) b->stages.push_back(stage);
+    }
+    std::map<std::pair<int, int>, std::vector<size_t>> groups;
+    for (size_t t = 0; t < n; t++) groups[{b->opts[t].format, b->opts[t].quality}].push_back(t);
+    std::vector<EncJob> ejobs;
+    b->encodes.clear();
+    for (auto &g : groups) {
+        ntg_batch::Enc e{g.first.first, g.first.second, (int)ejobs.size(), 0, 0};
+        long long nb = 0;
+        for (size_t t : g.second)
+            chain_jobs(b->plans[t], (const uint32_t *)b->tex[t].d_bgra, b->opts[t], b->xts[t], b->d_ws + b->base[t],
+                       (uint8_t *)b->tex[t].d_blocks, ejobs, nb);
+        e.njobs = (int)ejobs.size() - e.first;
+        e.nblocks = nb;
+        b->encodes.push_back(e);
+    }
+    if (b->d_mip) cudaFree(b->d_mip);
+    if (b->d_enc) cudaFree(b->d_enc);
+    b->d_mip = nullptr;
+    b->d_enc = nullptr;
+    if (!all.empty()) {
+        NTG_CUDA(cudaMalloc((void **)&b->d_mip, all.size() * sizeof(MipJob)));
+        NTG_CUDA(cudaMemcpy(b->d_mip, all.data(), all.size() * sizeof(MipJob), cudaMemcpyHostToDevice));
+    }
+    NTG_CUDA(cudaMalloc((void **)&b->d_enc, ejobs.size() * sizeof(EncJob)));
+    NTG_CUDA(cudaMemcpy(b->d_enc, ejobs.data(), ejobs.size() * sizeof(EncJob), cudaMemcpyHostToDevice));
+    b->launches = (int)b->set_images.size() + (int)b->encodes.size();
+    for (const auto &st : b->stages) b->launches += (int)st.size();
+    return NTG_OK;
+}
+
+int batch_mips(ntg_batch *b, cudaStream_t s) {
+    for (int t : b->set_images) {
+        const ChainPlan &P = b->plans[t];
+        NTG_TRY(launched(launch_set_image((const uint32_t *)b->tex[t].d_bgra, (size_t)P.lv[0].w * P.lv[0].h, b->xts[t]->d_in,
+                                          (float *)(b->d_ws + b->base[t] + P.f_off[0]), s), "set image"));
+    }
+    return run_stages(b->stages, b->d_mip, s);
+}
+
+int batch_encodes(ntg_batch *b, cudaStream_t s, int only_format = -1) {
+    for (const auto &e : b->encodes) {
+        if (only_format >= 0 && e.format != only_format) continue;
+        NTG_TRY(launch_encode(e.format, b->d_enc + e.first, e.njobs, e.nblocks, e.quality, s, b->enc_threads[enc_slot(e.format)]));
+    }
+    return NTG_OK;
+}
+
+// Runs the sequence once on a private stream (first-use attributes, and the outputs), then
+// captures it into a graph.
+int batch_capture(ntg_batch *b) {
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    cudaStream_t cs;
+    NTG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    int r = batch_mips(b, cs);
+    if (r == NTG_OK) r = batch_encodes(b, cs);
+    cudaError_t e = cudaStreamSynchronize(cs);
+    if (r == NTG_OK && e != cudaSuccess) r = cuda_fail(e, "batch run");
+    if (r == NTG_OK) {
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) r = cuda_fail(e, "begin capture");
+        else {
+            r = batch_mips(b, cs);
+            if (r == NTG_OK) r = batch_encodes(b, cs);
+            e = cudaStreamEndCapture(cs, &b->graph);
+            if (r == NTG_OK && e != cudaSuccess) r = cuda_fail(e, "end capture");
+        }
+    }
+    if (r == NTG_OK) {
+        e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        if (e != cudaSuccess) r = cuda_fail(e, "graph instantiate");
+    }
+    cudaStreamDestroy(cs);
+    return r;
+}
+
+// ---- tuning cache: a small JSON file of {"key", launch shape, timings} entries
+
+struct TuneEntry {
+    std::string key;
+    int strip = 32, threads = 128, tail = 4096, bc1 = 64, bc3 = 128, bc5 = 128;
+    double mip_ms = 0, encode_ms = 0;
+};
+
+std::string tune_cache_path() {
+    const char *p = std::getenv("NTG_TUNE_CACHE");
+    if (p && *p) return p;
+    const char *home = std::getenv("HOME");
+    return std::string(home && *home ? home : ".") + "/.cache/ntg_tune.json";
+}
+
+// Value after "field": in one flat JSON object (numbers, or a string without escapes).
+size_t json_value(const std::string &obj, const char *field) {
+    const std::string pat = std::string("\"") + field + "\"";
+    size_t i = obj.find(pat);
+    if (i == std::string::npos) return std::string::npos;
+    i += pat.size();
+    while (i < obj.size() && (obj[i] == ' ' || obj[i] == ':')) i++;
+    return i;
+}
+
+double json_number(const std::string &obj, const char *field, double def) {
+    const size_t i = json_value(obj, field);
+    return i == std::string::npos ? def : std::atof(obj.c_str() + i);
+}
+
+std::vector<TuneEntry> tune_cache_read() {
+    std::vector<TuneEntry> v;
+    FILE *f = std::fopen(tune_cache_path().c_str(), "rb");
+    if (!f) return v;
+    std::string text;
+    char buf[4096];
+    size_t k;
+    while ((k = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, k);
+    std::fclose(f);
+    size_t pos = 0;
+    while ((pos = text.find('{', pos + 1)) != std::string::npos) {
+        const size_t end = text.find('}', pos);
+        if (end == std::string::npos) break;
+        const std::string obj = text.substr(pos, end - pos);
+        const size_t k0 = json_value(obj, "key");
+        if (k0 == std::string::npos || obj[k0] != '"') continue;
+        const size_t k1 = obj.find('"', k0 + 1);
+        if (k1 == std::string::npos) continue;
+        TuneEntry e;
+        e.key = obj.substr(k0 + 1, k1 - k0 - 1);
+        e.strip = (int)json_number(obj, "strip", 32);
+        e.threads = (int)json_number(obj, "threads", 128);
+        e.tail = (int)json_number(obj, "tail", 4096);
+        e.bc1 = (int)json_number(obj, "bc1", 64);
+        e.bc3 = (int)json_number(obj, "bc3", 128);
+        e.bc5 = (int)json_number(obj, "bc5", 128);
+        e.mip_ms = json_number(obj, "mip_ms", 0);
+        e.encode_ms = json_number(obj, "encode_ms", 0);
+        v.push_back(e);
+    }
+    return v;
+}
+
+void tune_cache_write(const std::vector<TuneEntry> &v) {
+    const std::string path = tune_cache_path();
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {  // create the parent directory if it is missing (one level)
+        const std::string dir = path.substr(0, slash);
+        if (!dir.empty()) mkdir(dir.c_str(), 0755);
+    }
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) return;
+    std::fprintf(f, "{\"version\": 1, \"entries\": [\n");
+    for (size_t i = 0; i < v.size(); i++) {
+        const TuneEntry &e = v[i];
+        std::fprintf(f,
+                     "  {\"key\": \"%s\", \"strip\": %d, \"threads\": %d, \"tail\": %d, \"bc1\": %d, \"bc3\": %d, \"bc5\": %d, "
+                     "\"mip_ms\": %.4f, \"encode_ms\": %.4f}%s\n",
+                     e.key.c_str(), e.strip, e.threads, e.tail, e.bc1, e.bc3, e.bc5, e.mip_ms, e.encode_ms,
+                     i + 1 < v.size() ? "," : "");
+    }
+    std::fprintf(f, "]}\n");
+    std::fclose(f);
+}
+
+void apply_entry(ntg_batch *b, const TuneEntry &e) {
+    b->tune.strip = e.strip;
+    b->tune.threads = e.threads;
+    b->tune.tail_texels = e.tail;
+    b->enc_threads[0] = e.bc1;
+    b->enc_threads[1] = e.bc3;
+    b->enc_threads[2] = e.bc5;
+}
+
+// Device name and a hash of every texture's size and options.
+std::string batch_key(const ntg_batch *b) {
+    cudaDeviceProp prop;
+    std::string dev = cudaGetDeviceProperties(&prop, b->ctx->device) == cudaSuccess ? prop.name : "device";
+    for (char &c : dev)
+        if (c == '"' || c == '\\') c = '_';
+    unsigned long long h = 1469598103934665603ull;
+    auto mix = [&](long long v) {
+        for (int i = 0; i < 8; i++) { h ^= (unsigned long long)((v >> (8 * i)) & 255); h *= 1099511628211ull; }
+    };
+    for (size_t t = 0; t < b->tex.size(); t++) {
+        const ntg_chain_options &o = b->opts[t];
+        mix(b->tex[t].w); mix(b->tex[t].h); mix(o.format); mix(o.quality); mix(o.filter); mix(o.alpha_mode);
+        mix(o.in_xform); mix(o.out_xform); mix(o.weighted); mix(o.max_levels);
+    }
+    char buf[32];
+    std::snprintf(buf, sizeof buf, "%016llx", h);
+    return dev + "|" + buf;
+}
+
+float time_ms(cudaStream_t s, const std::function<int()> &fn, int reps, int *status) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int r = 0; r < reps && *status == NTG_OK; r++) {
+        cudaEventRecord(e0, s);
+        *status = fn();
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess) *status = cuda_fail(cudaGetLastError(), "tuning run");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return best;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ntg_batch_build(ntg_context *ctx, const ntg_batch_texture *textures, int count, ntg_batch **out) {
+    g_error.clear();
+    if (!ctx || !textures || count <= 0 || !out) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    std::unique_ptr<ntg_batch> b(new ntg_batch);
+    b->ctx = ctx;
+    b->tex.assign(textures, textures + count);
+    size_t off = 0;
+    for (int t = 0; t < count; t++) {
+        const ntg_batch_texture &T = textures[t];
+        if (!T.d_bgra || !T.d_blocks || T.w <= 0 || T.h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad texture");
+        NTG_TRY(check_opts(&T.opt));
+        const ntg_chain_options o = normalized(T.opt);
+        if ((o.in_xform == NTG_XFORM_GAMMA || o.out_xform == NTG_XFORM_GAMMA) && o.gamma != 2.2f)
+            return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "power-law gamma other than 2.2 is not supported on the GPU");
+        b->opts.push_back(o);
+        b->plans.push_back(plan_chain(T.w, T.h, o, false));
+        const XformTables *xt = ctx->xform(o.in_xform, o.out_xform, o.gamma);
+        if (!xt) return fail(NTG_ERROR_CUDA, "table upload failed");
+        b->xts.push_back(xt);
+        b->base.push_back(off);
+        off = align256(off + b->plans.back().bytes);
+        for (const Level &L : b->plans.back().lv) {
+            b->texels += (long long)L.w * L.h;
+            b->blocks += blocks_of(L.w, L.h);
+        }
+    }
+    NTG_CUDA(cudaMalloc((void **)&b->d_ws, std::max<size_t>(off, 256)));
+    b->key = batch_key(b.get());
+    for (const TuneEntry &e : tune_cache_read())
+        if (e.key == b->key) apply_entry(b.get(), e);
+    NTG_TRY(batch_plan(b.get()));
+    NTG_TRY(batch_capture(b.get()));
+    *out = b.release();
+    return NTG_OK;
+}
+
+int ntg_batch_launch(ntg_batch *b, void *stream) {
+    g_error.clear();
+    if (!b || !b->exec) return fail(NTG_ERROR_INVALID_INPUT, "batch not built");
+    NTG_TRY(ensure_device(b->ctx));
+    NTG_CUDA(cudaGraphLaunch(b->exec, S(stream)));
+    return NTG_OK;
+}
+
+int ntg_batch_autotune(ntg_batch *b, void *stream) {
+    g_error.clear();
+    if (!b) return fail(NTG_ERROR_INVALID_INPUT, "null batch");
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    NTG_TRY(ensure_device(b->ctx));
+    cudaStream_t s = S(stream);
+    int status = NTG_OK;
+    // mip launch shapes: rows per strip x threads per CTA x tail threshold
+    const MipTuning keep = b->tune;
+    MipTuning best = keep;
+    float best_ms = 1e30f;
+    for (int tail : {1024, 4096})
+        for (int threads : {64, 128, 256})
+            for (int strip : {8, 16, 32, 64}) {
+                b->tune.strip = strip;
+                b->tune.threads = threads;
+                b->tune.tail_texels = tail;
+                NTG_TRY(batch_plan(b));
+                const float ms = time_ms(s, [&] { return batch_mips(b, s); }, 3, &status);
+                NTG_TRY(status);
+                if (ms < best_ms) { best_ms = ms; best = b->tune; }
+            }
+    b->tune = best;
+    NTG_TRY(batch_plan(b));
+    // encoder blocks per CTA, per format present
+    float enc_total = 0;
+    for (int format : {NTG_FORMAT_BC1, NTG_FORMAT_BC3, NTG_FORMAT_BC5}) {
+        bool present = false;
+        for (const auto &e : b->encodes) present = present || e.format == format;
+        if (!present) continue;
+        const int slot = enc_slot(format);
+        int best_t = b->enc_threads[slot];
+        float best_e = 1e30f;
+        for (int threads : {32, 64, 128}) {
+            if (format == NTG_FORMAT_BC1 && threads > 64) continue;
+            b->enc_threads[slot] = threads;
+            const float ms = time_ms(s, [&] { return batch_encodes(b, s, format); }, 3, &status);
+            NTG_TRY(status);
+            if (ms < best_e) { best_e = ms; best_t = threads; }
+        }
+        b->enc_threads[slot] = best_t;
+        enc_total += best_e;
+    }
+    NTG_TRY(batch_capture(b));
+    std::vector<TuneEntry> cache = tune_cache_read();
+    TuneEntry e;
+    e.key = b->key;
+    e.strip = b->tune.strip;
+    e.threads = b->tune.threads;
+    e.tail = (int)b->tune.tail_texels;
+    e.bc1 = b->enc_threads[0];
+    e.bc3 = b->enc_threads[1];
+    e.bc5 = b->enc_threads[2];
+    e.mip_ms = best_ms;
+    e.encode_ms = enc_total;
+    cache.erase(std::remove_if(cache.begin(), cache.end(), [&](const TuneEntry &x) { return x.key == e.key; }), cache.end());
+    cache.push_back(e);
+    tune_cache_write(cache);
+    return NTG_OK;
+}
+
+int ntg_batch_info(const ntg_batch *b, long long *texels, long long *blocks, int *launches, int shape[6]) {
+    if (!b) return fail(NTG_ERROR_INVALID_INPUT, "null batch");
+    if (texels) *texels = b->texels;
+    if (blocks) *blocks = b->blocks;
+    if (launches) *launches = b->launches;
+    if (shape) {
+        shape[0] = b->tune.strip;
+        shape[1] = b->tune.threads;
+        shape[2] = (int)b->tune.tail_texels;
+        shape[3] = b->enc_threads[0];
+        shape[4] = b->enc_threads[1];
+        shape[5] = b->enc_threads[2];
+    }
+    return NTG_OK;
+}
+
+int ntg_batch_destroy(ntg_batch *b) {
+    if (!b) return NTG_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaDeviceSynchronize();
+    delete b;
+    return NTG_OK;
 }
 
 }  // extern "C"

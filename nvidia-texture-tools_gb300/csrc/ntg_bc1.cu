@@ -527,9 +527,9 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     store_block(out, o);
 }
 
-int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t stream) {
+int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
-    const int T = 64;
+    const int T = threads == 32 ? 32 : 64;  // blocks per CTA (one thread per 4x4 block)
     const size_t sm = (size_t)T * (48 * sizeof(float4) + 16 * sizeof(float));
     const unsigned grid = (unsigned)((nblocks + T - 1) / T);
     static std::atomic<unsigned long long> configured{0};

@@ -541,9 +541,9 @@ __global__ void __launch_bounds__(128) k_bc5(const EncJob *__restrict__ jobs, in
     pack_alpha(QUALITY >= 2 ? dxt5a_optimal(ch) : dxt5a_quick(ch), dst + 8);
 }
 
-int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t stream) {
+int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
-    const int T = 128;
+    const int T = threads == 32 || threads == 64 ? threads : 128;  // blocks per CTA
     const size_t sm = (size_t)T * 17 * sizeof(float4);
     const unsigned grid = (unsigned)((nblocks + T - 1) / T);
     switch (quality) {
@@ -554,9 +554,9 @@ int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, 
     return launch_status();
 }
 
-int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t stream) {
+int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
-    const int T = 128;
+    const int T = threads == 32 || threads == 64 ? threads : 128;  // blocks per CTA
     const unsigned grid = (unsigned)((nblocks + T - 1) / T);
     if (quality >= 2) k_bc5<2><<<grid, T, 0, stream>>>(d_jobs, njobs, nblocks);
     else k_bc5<1><<<grid, T, 0, stream>>>(d_jobs, njobs, nblocks);

@@ -41,9 +41,10 @@ struct EncJob {
     long long first_block;    // index of this job's first block in the launch
 };
 
-int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s);
-int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s);
-int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s);
+// threads = blocks per CTA (one thread per 4x4 block); 0 = the default shape.
+int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
+int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
+int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 
 // One buildNextMipmap step (source level -> destination level) of one texture. A mip launch walks a
 // list of these: its units (destination texels, tiles or strips, depending on the kernel) are

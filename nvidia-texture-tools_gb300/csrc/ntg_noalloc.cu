@@ -134,8 +134,8 @@ extern "C" int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_r
     if (cudaMemcpyAsync(d_job, &j, sizeof j, cudaMemcpyHostToDevice, s) != cudaSuccess)
         return report_status(ntg::launch_status(), "copy of the job record");
     const long long nblocks = (long long)((w + 3) / 4) * ((h + 3) / 4);
-    st = format == NTG_FORMAT_BC1 ? ntg::launch_bc1(d_job, 1, nblocks, quality, s)
-         : format == NTG_FORMAT_BC3 ? ntg::launch_bc3(d_job, 1, nblocks, quality, s)
-                                    : ntg::launch_bc5(d_job, 1, nblocks, quality, s);
+    st = format == NTG_FORMAT_BC1 ? ntg::launch_bc1(d_job, 1, nblocks, quality, 0, s)
+         : format == NTG_FORMAT_BC3 ? ntg::launch_bc3(d_job, 1, nblocks, quality, 0, s)
+                                    : ntg::launch_bc5(d_job, 1, nblocks, quality, 0, s);
     return report_status(st, "encoder launch");
 }

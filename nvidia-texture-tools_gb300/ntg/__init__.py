@@ -53,6 +53,11 @@ class ChainOptions(ctypes.Structure):
 _lib = None
 
 
+class BatchTexture(ctypes.Structure):
+    """Mirror of ntg_batch_texture."""
+    _fields_ = [("d_bgra", _vp), ("w", _i), ("h", _i), ("opt", ChainOptions), ("d_blocks", _vp)]
+
+
 def build(force: bool = False) -> str:
     import importlib.util
     spec = importlib.util.spec_from_file_location("ntg_build", os.path.join(PKG, "build.py"))
@@ -90,6 +95,12 @@ def lib():
         "ntg_error_sums": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp]),
         "ntg_host_polyphase": (_i, [_i, _f, _vp, _i, _i, _vp, _vp, _i]),
         "ntg_host_transform_tables": (_i, [_i, _i, _f, _vp, _vp, _vp, _vp]),
+        "ntg_batch_build": (_i, [_vp, ctypes.POINTER(BatchTexture), _i, ctypes.POINTER(_vp)]),
+        "ntg_batch_launch": (_i, [_vp, _vp]),
+        "ntg_batch_autotune": (_i, [_vp, _vp]),
+        "ntg_batch_info": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                                ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+        "ntg_batch_destroy": (_i, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -249,3 +260,41 @@ def host_transform_tables(in_xform, out_xform, gamma=2.2):
     lib().ntg_host_transform_tables(in_xform, out_xform, gamma, lut_in.ctypes.data, comp.ctypes.data, lut8.ctypes.data,
                                     steps.ctypes.data)
     return lut_in, comp, lut8, steps
+
+
+class Batch:
+    """Many textures' chains as one CUDA graph (ntg_batch). `textures` is a list of
+    (bgra device tensor, w, h, ChainOptions, output device tensor); the tensors must outlive the batch."""
+
+    def __init__(self, ctx: "Context", textures):
+        self.ctx = ctx
+        self._keep = [(t[0], t[4]) for t in textures]
+        arr = (BatchTexture * len(textures))()
+        for i, (bgra, w, h, opt, out) in enumerate(textures):
+            arr[i].d_bgra, arr[i].w, arr[i].h, arr[i].opt, arr[i].d_blocks = bgra.data_ptr(), w, h, opt, out.data_ptr()
+        self.h = ctypes.c_void_p()
+        _check(lib().ntg_batch_build(ctx.h, arr, len(textures), ctypes.byref(self.h)))
+
+    def launch(self, stream=None):
+        _check(lib().ntg_batch_launch(self.h, _stream_ptr(stream)))
+
+    def autotune(self, stream=None):
+        _check(lib().ntg_batch_autotune(self.h, _stream_ptr(stream)))
+
+    def info(self):
+        tex, blk, n = ctypes.c_longlong(), ctypes.c_longlong(), _i()
+        shape = (_i * 6)()
+        _check(lib().ntg_batch_info(self.h, ctypes.byref(tex), ctypes.byref(blk), ctypes.byref(n), shape))
+        keys = ("strip", "threads", "tail_texels", "bc1_blocks_per_cta", "bc3_blocks_per_cta", "bc5_blocks_per_cta")
+        return {"texels": tex.value, "blocks": blk.value, "launches": n.value, "shape": dict(zip(keys, list(shape)))}
+
+    def close(self):
+        if self.h:
+            lib().ntg_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

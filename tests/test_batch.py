@@ -1,0 +1,165 @@
+"""Batches (ntg_batch_*): many textures' chains in one CUDA graph. Every texture's blocks must equal
+what the single-chain path (ntg_compress_chain, itself pinned to the oracle) gives with the same
+options, and a few are checked against the oracle directly; graph replays, new inputs written into
+the same buffers, and the autotuner's launch shapes must not change a byte."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import ntg
+import ntg.synth as synth
+from test_gpu_parity import oracle_chain
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+# (w, h, format, quality, filter, alpha_mode, in_xform, out_xform, wrap, weighted)
+MIXED = [
+    (256, 256, 4, 1, 2, 1, 2, 2, 2, 0),   # the Kaiser / sRGB / BC3 / transparency chain
+    (128, 128, 1, 1, 0, 0, 0, 0, 2, 0),   # box / BC1 / linear (fast box path, level 0 materialised)
+    (64, 32, 7, 1, 1, 0, 0, 0, 1, 0),     # BC5 normal map, triangle, repeat
+    (96, 40, 4, 1, 1, 1, 1, 1, 0, 0),     # gamma 2.2, triangle, clamp
+    (37, 19, 1, 1, 2, 0, 1, 1, 2, 0),     # odd sizes, Kaiser, BC1 + gamma
+    (1, 64, 4, 1, 0, 1, 0, 0, 2, 0),      # 1-D, polyphase box (transparency)
+    (64, 1, 1, 0, 0, 0, 0, 0, 2, 0),      # 1-D fast box, range fit
+    (31, 31, 4, 3, 2, 0, 2, 2, 1, 0),     # odd, Highest quality alpha
+    (16, 16, 1, 2, 2, 0, 2, 2, 2, 0),     # smaller than the tail threshold from level 0, Production
+    (512, 64, 4, 0, 1, 1, 2, 2, 2, 0),    # non-square, Fastest BC3
+    (8, 8, 7, 2, 1, 0, 0, 0, 2, 0),       # tiny BC5 Production
+    (64, 64, 4, 1, 2, 1, 0, 0, 2, 1),     # alpha-weighted Kaiser taps
+    (128, 32, 1, 1, 1, 1, 2, 2, 2, 1),    # alpha-weighted triangle, BC1 + sRGB
+    (256, 128, 1, 1, 2, 0, 2, 2, 0, 0),   # Kaiser clamp, BC1 + sRGB
+]
+
+
+def options(c):
+    w, h, fmt, q, filt, am, ix, ox, wrap, weighted = c
+    return ntg.ChainOptions.make(format=fmt, quality=q, filter=filt, wrap=wrap, alpha_mode=am, in_xform=ix,
+                                 out_xform=ox, gamma=2.2, weighted=weighted)
+
+
+def image(c, seed):
+    w, h, fmt = c[0], c[1], c[2]
+    if fmt == 7:
+        return synth.normal_map(w, h, seed)
+    rng = np.random.default_rng(seed)
+    return synth.colour_texture(w, h, seed, scale=0.25, alpha=rng.integers(0, 256, (h, w)).astype(np.uint8))
+
+
+def make_batch(ctx, cases, seed0):
+    imgs, textures, refs = [], [], []
+    for i, c in enumerate(cases):
+        img = image(c, seed0 + i)
+        d_in = dev(img.reshape(-1).view(np.uint32))
+        opt = options(c)
+        out = dev(np.zeros(ntg.chain_bytes(c[0], c[1], opt), np.uint8))
+        imgs.append(img)
+        textures.append((d_in, c[0], c[1], opt, out))
+        refs.append(host(ctx.compress_chain(d_in, c[0], c[1], opt)))
+    return imgs, textures, refs
+
+
+def test_batch_matches_single_chains(ctx, tmp_path, monkeypatch):
+    monkeypatch.setenv("NTG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    _, textures, refs = make_batch(ctx, MIXED, 100)
+    b = ntg.Batch(ctx, textures)
+    try:
+        for t, r in zip(textures, refs):  # build() ran the sequence once
+            assert np.array_equal(host(t[4]), r)
+        for t in textures:
+            t[4].zero_()
+        b.launch()
+        b.launch()  # replays are idempotent
+        for t, r in zip(textures, refs):
+            assert np.array_equal(host(t[4]), r)
+        info = b.info()
+        assert info["texels"] == sum(sum(lw * lh for lw, lh in ntg.chain_levels(c[0], c[1])) for c in MIXED)
+        assert info["launches"] < 4 * 10 + 8  # grouped by depth, not one launch per texture level
+    finally:
+        b.close()
+
+
+def test_batch_new_inputs_in_same_buffers(ctx, tmp_path, monkeypatch):
+    monkeypatch.setenv("NTG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    cases = MIXED[:6]
+    _, textures, _ = make_batch(ctx, cases, 200)
+    b = ntg.Batch(ctx, textures)
+    try:
+        refs = []
+        for i, (c, t) in enumerate(zip(cases, textures)):
+            img = image(c, 900 + i)
+            t[0].copy_(dev(img.reshape(-1).view(np.uint32)))
+            refs.append(host(ctx.compress_chain(t[0], c[0], c[1], t[3])))
+        b.launch()
+        for t, r in zip(textures, refs):
+            assert np.array_equal(host(t[4]), r)
+    finally:
+        b.close()
+
+
+def test_autotune_keeps_results_and_caches_shape(ctx, tmp_path, monkeypatch):
+    cache = tmp_path / "tune.json"
+    monkeypatch.setenv("NTG_TUNE_CACHE", str(cache))
+    _, textures, refs = make_batch(ctx, MIXED, 300)
+    b = ntg.Batch(ctx, textures)
+    try:
+        b.autotune()
+        shape = b.info()["shape"]
+        for t in textures:
+            t[4].zero_()
+        b.launch()
+        for t, r in zip(textures, refs):
+            assert np.array_equal(host(t[4]), r)
+    finally:
+        b.close()
+    entries = json.loads(cache.read_text())["entries"]
+    assert len(entries) == 1 and entries[0]["strip"] == shape["strip"] and entries[0]["bc3"] == shape["bc3_blocks_per_cta"]
+    b2 = ntg.Batch(ctx, textures)  # same device and textures: the cached shape is used
+    try:
+        assert b2.info()["shape"] == shape
+    finally:
+        b2.close()
+
+
+def test_batch_c2_mix_matches_oracle(ctx, oracle, tmp_path, monkeypatch):
+    """The batched workload's mix (BC1/BC3/BC5, triangle mips, fBm normal maps) at small sizes,
+    checked against the oracle itself."""
+    monkeypatch.setenv("NTG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    specs = synth.batch_specs(12, 77, 3, 7)
+    textures = []
+    for (w, h, fmt, seed) in specs:
+        img = synth.batch_texture(w, h, fmt, seed)
+        opt = ntg.ChainOptions.make(format=fmt, quality=1, filter=ntg.FILTER_TRIANGLE, wrap=ntg.WRAP_MIRROR,
+                                    alpha_mode=ntg.ALPHA_TRANSPARENCY if fmt == 4 else ntg.ALPHA_NONE,
+                                    in_xform=ntg.XFORM_SRGB if fmt != 7 else ntg.XFORM_NONE,
+                                    out_xform=ntg.XFORM_SRGB if fmt != 7 else ntg.XFORM_NONE)
+        out = dev(np.zeros(ntg.chain_bytes(w, h, opt), np.uint8))
+        textures.append((dev(img.reshape(-1).view(np.uint32)), w, h, opt, out, img))
+    b = ntg.Batch(ctx, [t[:5] for t in textures])
+    try:
+        b.launch()
+        for (d_in, w, h, opt, out, img) in textures:
+            if opt.format == 1:
+                continue  # BC1 levels after a float sRGB transform use the device powf (checked elsewhere)
+            _, ref = oracle_chain(oracle, img, w, h, opt.format, 1, 1, opt.alpha_mode, opt.in_xform, opt.out_xform, 2)
+            assert np.array_equal(host(out), ref), (w, h, opt.format)
+    finally:
+        b.close()
+
+
+def test_batch_rejects_bad_input(ctx):
+    with pytest.raises(ntg.NtgError):
+        ntg.Batch(ctx, [])
