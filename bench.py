@@ -45,6 +45,14 @@ WORKLOADS = {
     "c1_2k": (2048, 2048, 4, 1, 2, 1, 2, 2,
               "2048x2048 RGBA8 sRGB, Kaiser(w3,a4,s1) mips, transparency, BC3 Normal, 12 levels"),
 }
+# Batched workloads: (count, seed, kmin, kmax, filter, description). Sizes 2^k per axis with k in
+# [kmin, kmax], 80% square; formats 50% BC1 / 30% BC3 (transparency) / 20% BC5 fBm normal maps;
+# linear colour; Normal quality; whole chains; one graph per step (ntg_batch).
+BATCHES = {
+    "c2": (256, 0xC2, 6, 11, 1, "256 textures 64..2048 px (80% square), 50/30/20 BC1/BC3/BC5, Triangle mips, "
+                                "one CUDA graph (ntg_batch), autotuned launch shapes"),
+    "c2_small": (64, 0xC2, 6, 9, 1, "64 textures 64..512 px, 50/30/20 BC1/BC3/BC5, Triangle mips, one CUDA graph"),
+}
 
 # FP32 operations of one cluster-split evaluation of squish's WeightedClusterFit::Compress4
 # (src/nvtt/squish/weightedclusterfit.cpp:505-545), each multiply/add/min/max/floor/divide counted
@@ -397,21 +405,210 @@ def run_gpu(args):
     return 0
 
 
+# ---------------------------------------------------------------------------------------------
+# Batched workloads
+
+def batch_textures(name):
+    """(w, h, format, options tuple, image) per texture. One seeded image per distinct (size, format):
+    textures that share both share the image."""
+    import ntg.synth as synth
+    count, seed, kmin, kmax, filt, _ = BATCHES[name]
+    cache, out = {}, []
+    for (w, h, fmt, _s) in synth.batch_specs(count, seed, kmin, kmax):
+        key = (w, h, fmt)
+        if key not in cache:
+            cache[key] = synth.batch_texture(w, h, fmt, seed ^ (w * 131 + h * 7 + fmt))
+        am = 1 if fmt == 4 else 0
+        out.append((w, h, fmt, (fmt, 1, filt, am, 0, 0), cache[key]))
+    return out
+
+
+def batch_options(o):
+    import ntg
+    fmt, quality, filt, am, ix, ox = o
+    return ntg.ChainOptions.make(format=fmt, quality=quality, filter=filt, wrap=ntg.WRAP_MIRROR, alpha_mode=am,
+                                 in_xform=ix, out_xform=ox)
+
+
+def run_gpu_batch(args):
+    import torch
+    import ntg
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    name = args.workload
+    desc = BATCHES[name][5]
+    ctx = ntg.Context(local)
+    specs = batch_textures(name)
+    textures, host_in = [], []
+    for (w, h, fmt, o, img) in specs:
+        opt = batch_options(o)
+        d_in = torch.from_numpy(img.reshape(-1).view(np.uint32)).cuda()
+        d_out = torch.empty(ntg.chain_bytes(w, h, opt), dtype=torch.uint8, device="cuda")
+        textures.append((d_in, w, h, opt, d_out))
+        host_in.append(img)
+    t0 = time.perf_counter()
+    batch = ntg.Batch(ctx, textures)
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    batch.autotune()
+    tune_s = time.perf_counter() - t0
+    info = batch.info()
+    texels = info["texels"]
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        batch.launch()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t_wall = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            batch.launch()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        wall = time.perf_counter() - t_wall
+    dev_ms = max_over_ranks(world, sum(s.elapsed_time(e) for s, e in zip(starts, ends)), torch.device("cuda"))
+    value = world * texels * args.steps / (dev_ms / 1000.0) / 1e6
+    ref_out = [t[4].cpu().numpy() for t in textures]
+
+    # end to end: pinned host inputs copied in, the graph, every texture's blocks copied out
+    h_in = [torch.from_numpy(img.reshape(-1).view(np.uint32)).pin_memory() for img in host_in]
+    h_out = [torch.empty(t[4].numel(), dtype=torch.uint8).pin_memory() for t in textures]
+    bi = sum(int(x.numel()) * 4 for x in h_in)
+    bo = sum(int(x.numel()) for x in h_out)
+
+    def e2e_step():
+        for t, x in zip(textures, h_in):
+            t[0].copy_(x, non_blocking=True)
+        batch.launch()
+        for t, y in zip(textures, h_out):
+            y.copy_(t[4], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    e2e_step()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = max_over_ranks(world, time.perf_counter() - t0, torch.device("cuda"))
+    e2e_value = world * texels * args.steps / e2e_s / 1e6
+    same = all(np.array_equal(y.numpy(), r) for y, r in zip(h_out, ref_out))
+
+    if rank == 0:
+        phases, blocks = batch.time_phases()
+        clocks = clk.summary()
+        peaks, peak_src = measured_peaks()
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        # mip phase against HBM: read level l-1 (BGRA8 for level 0, else FP32 planar), write level l
+        # (FP32 planar, plus the BGRA8 copy the BC3/BC5 encoders read)
+        mip_bytes = 0
+        for (w, h, fmt, o, img) in specs:
+            lv = ntg.chain_levels(w, h)
+            for i in range(1, len(lv)):
+                mip_bytes += lv[i - 1][0] * lv[i - 1][1] * (4 if i == 1 else 16)
+                mip_bytes += lv[i][0] * lv[i][1] * (16 + (4 if fmt != 1 else 0))
+        mip_gbs = mip_bytes / (phases["mips"] / 1000.0) / 1e9
+        dominant = max(("bc1", "bc3", "bc5", "mips"), key=lambda k: phases[k])
+        roof_mips = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
+                     "traffic": None, "kernel": "mip launches of the batch (k_poly2x, k_poly, k_mip_tail, k_fast_down)",
+                     "algorithmic_bytes": mip_bytes, "ms": phases["mips"], "peak_source": peak_src}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": desc, "textures": len(specs), "texels_per_step": texels,
+                           "blocks_per_step": info["blocks"], "l2": "flushed (256 MiB write) between steps",
+                           "method": "plain (non-learned) cluster fit", "replicas": world,
+                           "launch_shape": info["shape"], "build_s": build_s, "autotune_s": tune_s,
+                           "images": "one seeded image per distinct (size, format)"},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
+                        "matches_device_path": same},
+                "gpu_launches": info["launches"] * args.steps,
+                "clocks": clocks, "roofline": None, "roofline_mips": roof_mips,
+                "phase_ms": phases, "phase_blocks": blocks, "dominant_phase": dominant,
+                "wall_s_timed": wall, "cpu_baseline": None}
+        if not args.no_cpu and world == 1:
+            try:
+                line["cpu_baseline"] = cpu_batch_sample(name, specs, os.cpu_count() or 1, 20.0)
+            except Exception as e:  # reported, not fatal
+                line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                        "sample": f"failed: {e}"}
+        print(json.dumps(line), flush=True)
+    batch.close()
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def cpu_batch_sample(name, specs, threads, budget_s):
+    """The oracle port on the host cores over the batch's textures in order until about `budget_s`
+    seconds of work: whole chains, mips on one thread, encode on `threads`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build_oracle()
+    oracle = pyoracle.Oracle()
+    done, texels, total = 0, 0, 0.0
+    for (w, h, fmt, o, img) in specs:
+        spec = (w, h, fmt, o[1], o[2], o[3], o[4], o[5])
+        total += cpu_chain(oracle, img, spec, threads)[0]
+        texels += chain_texels(w, h)
+        done += 1
+        if total >= budget_s:
+            break
+    return {"value": texels / total / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"the first {done} of {len(specs)} textures of {name} with their whole chains "
+                      f"({texels} texels, {total:.1f} s)"}
+
+
+def run_reference_batch(args):
+    """The reference arm on a batch: the oracle port over a bounded sample of its textures per step."""
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return 0
+    name = args.workload
+    specs = batch_textures(name)
+    threads = os.cpu_count() or 1
+    sample = cpu_batch_sample(name, specs, threads, 5.0)
+    for _ in range(args.warmup - 1):
+        cpu_batch_sample(name, specs, threads, 5.0)
+    vals = [cpu_batch_sample(name, specs, threads, 5.0) for _ in range(args.steps)]
+    value = statistics.mean(v["value"] for v in vals)
+    why = ("the reference library itself cannot be built on this host (its source tree is absent), so its C "
+           "restatement in oracle/ runs: mips on one thread as the reference filters, encode on every core")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": BATCHES[name][5], "sample": sample["sample"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample["sample"] + "; " + why},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ntg", choices=["ntg", "reference"])
-    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS) + sorted(BATCHES))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3
     if args.impl == "reference":
-        return run_reference(args)
-    return run_gpu(args)
+        return run_reference_batch(args) if args.workload in BATCHES else run_reference(args)
+    return run_gpu_batch(args) if args.workload in BATCHES else run_gpu(args)
 
 
 if __name__ == "__main__":

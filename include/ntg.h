@@ -184,6 +184,10 @@ int ntg_batch_autotune(ntg_batch *batch, void *stream);
  * shape[] = {strip, threads, tail texels, bc1 blocks/CTA, bc3 blocks/CTA, bc5 blocks/CTA}.
  * Any pointer may be NULL. */
 int ntg_batch_info(const ntg_batch *batch, long long *texels, long long *blocks, int *launches, int shape[6]);
+/* Runs the batch's phases once each, outside the graph, timed with CUDA events on `stream`:
+ * ms[0] = every mip launch, ms[1..3] = the BC1, BC3, BC5 encoder launches (0 when absent), and
+ * blocks[0..2] = the 4x4 blocks of each format. Synchronises `stream`. */
+int ntg_batch_time_phases(ntg_batch *batch, void *stream, float ms[4], long long blocks[3]);
 int ntg_batch_destroy(ntg_batch *batch);
 
 /* Phase timing of chain calls: when enabled, ntg_compress_chain records CUDA events on its stream

@@ -1231,6 +1231,27 @@ int ntg_batch_info(const ntg_batch *b, long long *texels, long long *blocks, int
     return NTG_OK;
 }
 
+int ntg_batch_time_phases(ntg_batch *b, void *stream, float ms[4], long long blocks[3]) {
+    g_error.clear();
+    if (!b || !ms) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    NTG_TRY(ensure_device(b->ctx));
+    cudaStream_t s = S(stream);
+    int status = NTG_OK;
+    ms[0] = time_ms(s, [&] { return batch_mips(b, s); }, 1, &status);
+    NTG_TRY(status);
+    const int formats[3] = {NTG_FORMAT_BC1, NTG_FORMAT_BC3, NTG_FORMAT_BC5};
+    for (int i = 0; i < 3; i++) {
+        long long nb = 0;
+        for (const auto &e : b->encodes)
+            if (e.format == formats[i]) nb += e.nblocks;
+        if (blocks) blocks[i] = nb;
+        ms[1 + i] = nb ? time_ms(s, [&] { return batch_encodes(b, s, formats[i]); }, 1, &status) : 0.0f;
+        NTG_TRY(status);
+    }
+    return NTG_OK;
+}
+
 int ntg_batch_destroy(ntg_batch *b) {
     if (!b) return NTG_OK;
     cudaSetDevice(b->ctx->device);

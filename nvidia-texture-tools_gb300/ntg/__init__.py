@@ -101,6 +101,7 @@ def lib():
         "ntg_batch_info": (_i, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
                                 ctypes.POINTER(_i), ctypes.POINTER(_i)]),
         "ntg_batch_destroy": (_i, [_vp]),
+        "ntg_batch_time_phases": (_i, [_vp, _vp, ctypes.POINTER(_f), ctypes.POINTER(ctypes.c_longlong)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -287,6 +288,14 @@ class Batch:
         _check(lib().ntg_batch_info(self.h, ctypes.byref(tex), ctypes.byref(blk), ctypes.byref(n), shape))
         keys = ("strip", "threads", "tail_texels", "bc1_blocks_per_cta", "bc3_blocks_per_cta", "bc5_blocks_per_cta")
         return {"texels": tex.value, "blocks": blk.value, "launches": n.value, "shape": dict(zip(keys, list(shape)))}
+
+    def time_phases(self, stream=None):
+        """{mips, bc1, bc3, bc5} ms of one run of each phase outside the graph, and blocks per format."""
+        ms = (_f * 4)()
+        blocks = (ctypes.c_longlong * 3)()
+        _check(lib().ntg_batch_time_phases(self.h, _stream_ptr(stream), ms, blocks))
+        return ({"mips": ms[0], "bc1": ms[1], "bc3": ms[2], "bc5": ms[3]},
+                {"bc1": blocks[0], "bc3": blocks[1], "bc5": blocks[2]})
 
     def close(self):
         if self.h:
