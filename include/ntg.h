@@ -190,6 +190,36 @@ int ntg_batch_info(const ntg_batch *batch, long long *texels, long long *blocks,
 int ntg_batch_time_phases(ntg_batch *batch, void *stream, float ms[4], long long blocks[3]);
 int ntg_batch_destroy(ntg_batch *batch);
 
+/* ---- the learned endpoint proposal's network ----
+ * No counterpart in the reference. An MLP 48 -> 256 -> 256 -> 8 (GELU; BF16 weights and
+ * activations, FP32 accumulation) on the tcgen05 tensor cores: inputs are a 4x4 block's texels as
+ * 16 x RGB in [0, 1]; outputs 0-5 are the two endpoints (RGB, RGB) of the block's cluster fit,
+ * output 6 the fit's error as log(1 + SSE) (SSE in 8-bit units, colour-weighted), output 7 unused.
+ * Parameters are one flat FP32 vector: W1 [256 x 48], b1 [256], W2 [256 x 256], b2 [256],
+ * W3 [8 x 256], b3 [8] (weights row-major, out x in). Training is Adam (beta 0.9 / 0.999, eps 1e-8)
+ * on the weighted mean squared error of the outputs (weights 1 for the endpoints, 0.25 for the
+ * error, 0 for output 7). Device buffers: x [batch x 48], targets [batch x 8], y [batch x 16]
+ * (columns 8-15 zero), all FP32 row-major; batch a multiple of 8. */
+typedef struct ntg_mlp ntg_mlp;
+int ntg_mlp_create(int device, unsigned long long seed, ntg_mlp **out);
+int ntg_mlp_destroy(ntg_mlp *mlp);
+int ntg_mlp_param_count(void);
+int ntg_mlp_get_params(ntg_mlp *mlp, float *h_params);
+int ntg_mlp_set_params(ntg_mlp *mlp, const float *h_params);
+int ntg_mlp_infer(ntg_mlp *mlp, const float *d_x, int batch, float *d_y, void *stream);
+/* One forward + backward pass: the flat gradient (parameter layout) into d_grads (may be NULL) and
+ * the loss into *h_loss (may be NULL); synchronises `stream`. */
+int ntg_mlp_gradients(ntg_mlp *mlp, const float *d_x, const float *d_t, int batch, float *d_grads, float *h_loss,
+                      void *stream);
+/* One Adam step (enqueue only); the batch's loss into *d_loss (device, may be NULL). */
+int ntg_mlp_train_step(ntg_mlp *mlp, const float *d_x, const float *d_t, int batch, float lr, float *d_loss,
+                       void *stream);
+/* Non-zero when a tensor-core wait of an earlier call gave up (synchronises the device). */
+int ntg_mlp_status(ntg_mlp *mlp);
+/* The network's matrix product on its own: C[M x N] (FP32) = A[M x K] * B[N x K]^T, A and B BF16
+ * row-major, K a multiple of 8 (exposed for testing the tensor-core path). */
+int ntg_gemm_bf16(const void *d_a, const void *d_b, int M, int N, int K, float *d_c, void *stream);
+
 /* Phase timing of chain calls: when enabled, ntg_compress_chain records CUDA events on its stream
  * around the mip phase and the encode phase; ntg_profile_read waits for the last call's events and
  * returns the two durations in milliseconds. */

@@ -24,7 +24,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc") if os.path.exists(os.path.join(CUDA, "bin", "nvcc")) else "nvcc"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["ntg_bc1.cu", "ntg_bc3.cu", "ntg_mip.cu", "ntg_decode.cu", "ntg_noalloc.cu"]
+CU_SOURCES = ["ntg_bc1.cu", "ntg_bc3.cu", "ntg_mip.cu", "ntg_decode.cu", "ntg_noalloc.cu", "ntg_mlp.cu"]
 CPP_SOURCES = ["ntg_api.cpp", "ntg_host_tables.cpp", "nvtt_api.cpp"]
 HEADERS = ["ntg_device.cuh", "ntg_internal.h", "ntg_host_tables.h"]
 

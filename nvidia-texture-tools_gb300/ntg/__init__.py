@@ -102,6 +102,16 @@ def lib():
                                 ctypes.POINTER(_i), ctypes.POINTER(_i)]),
         "ntg_batch_destroy": (_i, [_vp]),
         "ntg_batch_time_phases": (_i, [_vp, _vp, ctypes.POINTER(_f), ctypes.POINTER(ctypes.c_longlong)]),
+        "ntg_mlp_create": (_i, [_i, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
+        "ntg_mlp_destroy": (_i, [_vp]),
+        "ntg_mlp_param_count": (_i, []),
+        "ntg_mlp_get_params": (_i, [_vp, _vp]),
+        "ntg_mlp_set_params": (_i, [_vp, _vp]),
+        "ntg_mlp_infer": (_i, [_vp, _vp, _i, _vp, _vp]),
+        "ntg_mlp_gradients": (_i, [_vp, _vp, _vp, _i, _vp, ctypes.POINTER(_f), _vp]),
+        "ntg_mlp_train_step": (_i, [_vp, _vp, _vp, _i, _f, _vp, _vp]),
+        "ntg_mlp_status": (_i, [_vp]),
+        "ntg_gemm_bf16": (_i, [_vp, _vp, _i, _i, _i, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -307,3 +317,69 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class MLP:
+    """The learned endpoint proposal's network (ntg_mlp): 48 -> 256 -> 256 -> 8 on the tensor cores."""
+    IN, OUT, OUTP = 48, 8, 16
+
+    def __init__(self, device: int = 0, seed: int = 0x4E4554):
+        self.h = ctypes.c_void_p()
+        _check(lib().ntg_mlp_create(device, seed, ctypes.byref(self.h)))
+
+    @staticmethod
+    def param_count() -> int:
+        return int(lib().ntg_mlp_param_count())
+
+    def get_params(self) -> np.ndarray:
+        p = np.empty(self.param_count(), np.float32)
+        _check(lib().ntg_mlp_get_params(self.h, p.ctypes.data))
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.param_count()
+        _check(lib().ntg_mlp_set_params(self.h, p.ctypes.data))
+
+    def infer(self, x, out=None, stream=None):
+        import torch
+        b = x.shape[0]
+        out = out if out is not None else torch.empty((b, self.OUTP), dtype=torch.float32, device=x.device)
+        _check(lib().ntg_mlp_infer(self.h, x.data_ptr(), b, out.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def gradients(self, x, t, stream=None):
+        import torch
+        g = torch.empty(self.param_count(), dtype=torch.float32, device=x.device)
+        loss = _f()
+        _check(lib().ntg_mlp_gradients(self.h, x.data_ptr(), t.data_ptr(), x.shape[0], g.data_ptr(), ctypes.byref(loss),
+                                       _stream_ptr(stream)))
+        return g, loss.value
+
+    def train_step(self, x, t, lr=1e-3, loss_out=None, stream=None):
+        _check(lib().ntg_mlp_train_step(self.h, x.data_ptr(), t.data_ptr(), x.shape[0], lr,
+                                        loss_out.data_ptr() if loss_out is not None else None, _stream_ptr(stream)))
+
+    def status(self):
+        _check(lib().ntg_mlp_status(self.h))
+
+    def close(self):
+        if self.h:
+            lib().ntg_mlp_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def gemm_bf16(a, b, stream=None):
+    """C = A @ B^T with A [M x K], B [N x K] torch bf16 CUDA tensors, through the tensor-core kernel."""
+    import torch
+    m, k = a.shape
+    n = b.shape[0]
+    c = torch.empty((m, n), dtype=torch.float32, device=a.device)
+    _check(lib().ntg_gemm_bf16(a.data_ptr(), b.data_ptr(), m, n, k, c.data_ptr(), _stream_ptr(stream)))
+    return c

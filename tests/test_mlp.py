@@ -1,0 +1,91 @@
+"""The learned proposal's network on the tensor cores (tcgen05): the matrix-product kernel against a
+torch FP32 product of the same BF16 operands, the forward pass and the gradients against the FP64
+oracle (oracle/mlp_oracle.py), and Adam training reducing the loss."""
+import numpy as np
+import pytest
+
+import ntg
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 256, 48), (200, 16, 256), (256, 48, 1024), (1000, 256, 256), (64, 64, 16)])
+def test_gemm_matches_torch(m, n, k):
+    torch = _torch()
+    g = torch.Generator(device="cpu").manual_seed(m * 7 + n + k)
+    a = torch.randn(m, k, generator=g).to(torch.bfloat16).cuda()
+    b = torch.randn(n, k, generator=g).to(torch.bfloat16).cuda()
+    c = ntg.gemm_bf16(a, b)
+    ref = a.float() @ b.float().T
+    torch.cuda.synchronize()
+    err = (c - ref).abs().max().item()
+    assert err <= 1e-3 * max(1.0, ref.abs().max().item()), err
+
+
+def _data(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.random((n, 48), dtype=np.float32)
+    t = np.concatenate([rng.random((n, 6)), rng.random((n, 1)) * 4, np.zeros((n, 1))], axis=1).astype(np.float32)
+    return x, t
+
+
+def test_forward_matches_oracle():
+    torch = _torch()
+    import mlp_oracle
+    net = ntg.MLP(seed=11)
+    try:
+        x, _ = _data(512, 1)
+        y = net.infer(torch.from_numpy(x).cuda()).cpu().numpy()
+        ref, _ = mlp_oracle.forward(net.get_params(), x)
+        assert np.all(y[:, 8:] == 0)
+        assert np.max(np.abs(y[:, :8] - ref)) < 2e-3 * max(1.0, np.abs(ref).max())
+    finally:
+        net.close()
+
+
+@pytest.mark.parametrize("batch", [256, 1024])
+def test_gradients_match_oracle(batch):
+    torch = _torch()
+    import mlp_oracle
+    net = ntg.MLP(seed=5 + batch)
+    try:
+        x, t = _data(batch, batch)
+        g, loss = net.gradients(torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda())
+        g = g.cpu().numpy().astype(np.float64)
+        ref, ref_loss = mlp_oracle.gradients(net.get_params(), x, t)
+        assert abs(loss - ref_loss) <= 1e-3 * ref_loss
+        # per parameter block: relative L2 error of the gradient
+        offs = np.cumsum([0, 256 * 48, 256, 256 * 256, 256, 8 * 256, 8])
+        for a, b in zip(offs[:-1], offs[1:]):
+            num = np.linalg.norm(g[a:b] - ref[a:b])
+            den = max(np.linalg.norm(ref[a:b]), 1e-12)
+            assert num / den < 2e-2, (a, b, num / den)
+    finally:
+        net.close()
+
+
+def test_training_reduces_loss():
+    torch = _torch()
+    net = ntg.MLP(seed=3)
+    try:
+        x, t = _data(8192, 77)
+        # a learnable target: endpoints = per-block min / max of the first texel's channels
+        xt = x.reshape(-1, 16, 3)
+        t[:, 0:3] = xt.min(axis=1)
+        t[:, 3:6] = xt.max(axis=1)
+        t[:, 6] = np.log1p(((xt - xt.mean(axis=1, keepdims=True)) ** 2).sum(axis=(1, 2)) * 255.0)
+        dx, dt = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+        _, loss0 = net.gradients(dx, dt)
+        lossbuf = torch.zeros(1, dtype=torch.float32, device="cuda")
+        for _ in range(300):
+            net.train_step(dx, dt, lr=1e-3, loss_out=lossbuf)
+        net.status()
+        _, loss1 = net.gradients(dx, dt)
+        assert loss1 < 0.2 * loss0, (loss0, loss1)
+    finally:
+        net.close()
