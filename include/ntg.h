@@ -192,9 +192,12 @@ int ntg_batch_destroy(ntg_batch *batch);
 
 /* ---- the learned endpoint proposal's network ----
  * No counterpart in the reference. An MLP 48 -> 256 -> 256 -> 8 (GELU; BF16 weights and
- * activations, FP32 accumulation) on the tcgen05 tensor cores: inputs are a 4x4 block's texels as
- * 16 x RGB in [0, 1]; outputs 0-5 are the two endpoints (RGB, RGB) of the block's cluster fit,
- * output 6 the fit's error as log(1 + SSE) (SSE in 8-bit units, colour-weighted), output 7 unused.
+ * activations, FP32 accumulation) on the tcgen05 tensor cores: inputs are a 4x4 block's 16 texels
+ * in the block's principal frame (centred on its weighted mean colour, divided by its RMS deviation
+ * + 1/255, rotated onto the principal axis of its colours and two axes orthogonal to it, sorted
+ * along the axis); outputs 0-5 are the two endpoints of the block's cluster fit in that frame,
+ * output 6 the fit's error as log((SSE + 1) / (V + 1)) with V the block's weighted variance (both
+ * in 8-bit, colour-weighted units), output 7 unused.
  * Parameters are one flat FP32 vector: W1 [256 x 48], b1 [256], W2 [256 x 256], b2 [256],
  * W3 [8 x 256], b3 [8] (weights row-major, out x in). Training is Adam (beta 0.9 / 0.999, eps 1e-8)
  * on the weighted mean squared error of the outputs (weights 1 for the endpoints, 0.25 for the
@@ -206,7 +209,11 @@ int ntg_mlp_destroy(ntg_mlp *mlp);
 int ntg_mlp_param_count(void);
 int ntg_mlp_get_params(ntg_mlp *mlp, float *h_params);
 int ntg_mlp_set_params(ntg_mlp *mlp, const float *h_params);
+/* Inference: one persistent kernel per call, the weights resident in shared memory and the three
+ * layers chained through TMEM; any batch size. */
 int ntg_mlp_infer(ntg_mlp *mlp, const float *d_x, int batch, float *d_y, void *stream);
+/* The same forward pass as three separate tensor-core products (the training path). */
+int ntg_mlp_infer_unfused(ntg_mlp *mlp, const float *d_x, int batch, float *d_y, void *stream);
 /* One forward + backward pass: the flat gradient (parameter layout) into d_grads (may be NULL) and
  * the loss into *h_loss (may be NULL); synchronises `stream`. */
 int ntg_mlp_gradients(ntg_mlp *mlp, const float *d_x, const float *d_t, int batch, float *d_grads, float *h_loss,
@@ -216,6 +223,29 @@ int ntg_mlp_train_step(ntg_mlp *mlp, const float *d_x, const float *d_t, int bat
                        void *stream);
 /* Non-zero when a tensor-core wait of an earlier call gave up (synchronises the device). */
 int ntg_mlp_status(ntg_mlp *mlp);
+/* Learned BC1 encode of a chain (BC1 Normal quality; same options and output layout as
+ * ntg_compress_chain). Each block's texels go through the network; the proposal's palette seeds the
+ * cluster fit's ordering search, which evaluates only the orderings within `radius` (in each
+ * cumulative cluster end) of the proposal's, with the full search's arithmetic and order; a block
+ * whose result's error exceeds (1 + margin) x the network's estimate of the full fit's error gets
+ * the full fit. stats (host, may be NULL; then nothing synchronises): {blocks kept from the pruned
+ * search, blocks given the full fit, orderings evaluated by the pruned search}. */
+int ntg_compress_chain_learned(ntg_context *ctx, ntg_mlp *mlp, const void *d_bgra, int w, int h,
+                               const ntg_chain_options *opt, int radius, float margin, void *d_blocks,
+                               unsigned long long *stats, void *stream);
+/* The same pruned search with the proposals supplied by the caller (d_proposals [blocks x 16], the
+ * network's output layout) instead of the network: seeds from other methods, for comparison. */
+int ntg_compress_chain_proposed(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
+                                const float *d_proposals, int radius, float margin, void *d_blocks, unsigned long long *stats,
+                                void *stream);
+/* Training data from a BC1 chain: the network's inputs for every block of every level
+ * (d_x [blocks x 48]), and targets (d_t [blocks x 8]) from that chain's encoded blocks d_blocks
+ * (e.g. ntg_compress_chain's output): endpoints brighter first and the error term, in the
+ * block's frame, then 0. */
+int ntg_chain_features(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt, float *d_x,
+                       void *stream);
+int ntg_chain_targets(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
+                      const void *d_blocks, float *d_t, void *stream);
 /* The network's matrix product on its own: C[M x N] (FP32) = A[M x K] * B[N x K]^T, A and B BF16
  * row-major, K a multiple of 8 (exposed for testing the tensor-core path). */
 int ntg_gemm_bf16(const void *d_a, const void *d_b, int M, int N, int K, float *d_c, void *stream);

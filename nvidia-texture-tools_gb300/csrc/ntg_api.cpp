@@ -693,6 +693,106 @@ static int chain_common(ntg_context *ctx, const void *d_bgra, int w, int h, cons
     return NTG_OK;
 }
 
+// The learned endpoint proposal over a chain (BC1): the network's inputs for every block of every
+// level, training targets from the plain fit's blocks, or the learned encode (inputs -> network ->
+// pruned fit -> full fit for the listed blocks), all on one stream without host round trips.
+enum { LEARN_FEATURES = 0, LEARN_TARGETS = 1, LEARN_ENCODE = 2 };
+
+static int chain_learned(ntg_context *ctx, ntg_mlp *mlp, const void *d_bgra, int w, int h, const ntg_chain_options *opt_in,
+                         int mode, void *d_blocks, float *d_aux, int radius, float margin, unsigned long long *h_stats,
+                         void *stream, const float *d_proposals = nullptr) {
+    NTG_TRY(check_opts(opt_in));
+    if (!ctx || !d_bgra || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    if (opt_in->format != NTG_FORMAT_BC1) return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "the learned proposal is for BC1");
+    if (mode == LEARN_ENCODE && ((!mlp && !d_proposals) || opt_in->quality != NTG_QUALITY_NORMAL || radius < 0))
+        return fail(NTG_ERROR_INVALID_INPUT, "learned encode needs a network, Quality_Normal and radius >= 0");
+    const ntg_chain_options norm = normalized(*opt_in);
+    const ntg_chain_options *opt = &norm;
+    if ((opt->in_xform == NTG_XFORM_GAMMA || opt->out_xform == NTG_XFORM_GAMMA) && opt->gamma != 2.2f)
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "power-law gamma other than 2.2 is not supported on the GPU");
+    NTG_TRY(ensure_device(ctx));
+    cudaStream_t s = S(stream);
+    const ChainPlan P = plan_chain(w, h, *opt, false);
+    const XformTables *xt = ctx->xform(opt->in_xform, opt->out_xform, opt->gamma);
+    if (!xt) return fail(NTG_ERROR_CUDA, "table upload failed");
+    long long nb = 0;
+    for (const Level &L : P.lv) nb += blocks_of(L.w, L.h);
+    const size_t base = align256(std::max<size_t>(P.bytes, 256));
+    const size_t xoff = base, yoff = align256(xoff + (size_t)nb * 48 * 4), loff = align256(yoff + (size_t)nb * 16 * 4),
+                 soff = align256(loff + (size_t)nb * 8);
+    const size_t need = mode == LEARN_ENCODE ? soff + 256 : base;
+    uint8_t *ws = nullptr;
+    NTG_TRY(ctx->workspace(need, s, &ws));
+    NTG_TRY(build_levels(ctx, P, (const uint32_t *)d_bgra, *opt, xt, ws, s));
+    std::vector<EncJob> jobs;
+    long long nblocks = 0;
+    chain_jobs(P, (const uint32_t *)d_bgra, *opt, xt, ws, (uint8_t *)d_blocks, jobs, nblocks);
+    NTG_TRY(upload_jobs(ctx, jobs, s));
+    const int nj = (int)jobs.size();
+    if (mode == LEARN_FEATURES) return launched(launch_bc1_features(ctx->d_jobs, nj, nblocks, d_aux, s), "block features");
+    if (mode == LEARN_TARGETS) return launched(launch_bc1_targets(ctx->d_jobs, nj, nblocks, d_aux, s), "fit targets");
+    float *x = (float *)(ws + xoff), *y = (float *)(ws + yoff);
+    long long *list = (long long *)(ws + loff);
+    unsigned long long *stats = (unsigned long long *)(ws + soff);
+    if (d_proposals) {
+        y = const_cast<float *>(d_proposals);
+    } else {
+        NTG_TRY(launched(launch_bc1_features(ctx->d_jobs, nj, nblocks, x, s), "block features"));
+        int r = mlp_forward_device(mlp, x, nblocks, y, s);
+        if (r) return fail(r, std::string("proposal network: ") + ntg_last_error_string());
+    }
+    NTG_CUDA(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), s));
+    NTG_TRY(launched(launch_bc1_learned(ctx->d_jobs, nj, nblocks, y, radius, margin, list, stats, s), "pruned fit"));
+    NTG_TRY(launched(launch_bc1_list(ctx->d_jobs, nj, list, stats + 1, nblocks, s), "full fit of the listed blocks"));
+    if (h_stats) {
+        NTG_CUDA(cudaMemcpyAsync(h_stats, stats, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        NTG_CUDA(cudaStreamSynchronize(s));
+    }
+    return NTG_OK;
+}
+
+int ntg_compress_chain_proposed(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
+                                const float *d_proposals, int radius, float margin, void *d_blocks, unsigned long long *stats,
+                                void *stream) {
+    g_error.clear();
+    if (!ctx || !d_blocks || !d_proposals) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return chain_learned(ctx, nullptr, d_bgra, w, h, opt, LEARN_ENCODE, d_blocks, nullptr, radius, margin, stats, stream,
+                         d_proposals);
+}
+
+int ntg_chain_features(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt, float *d_x,
+                       void *stream) {
+    g_error.clear();
+    if (!ctx || !d_x) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return chain_learned(ctx, nullptr, d_bgra, w, h, opt, LEARN_FEATURES, nullptr, d_x, 0, 0, nullptr, stream);
+}
+
+int ntg_chain_targets(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
+                      const void *d_blocks, float *d_t, void *stream) {
+    g_error.clear();
+    if (!ctx || !d_blocks || !d_t) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return chain_learned(ctx, nullptr, d_bgra, w, h, opt, LEARN_TARGETS, const_cast<void *>(d_blocks), d_t, 0, 0, nullptr,
+                         stream);
+}
+
+int ntg_compress_chain_learned(ntg_context *ctx, ntg_mlp *mlp, const void *d_bgra, int w, int h,
+                               const ntg_chain_options *opt, int radius, float margin, void *d_blocks,
+                               unsigned long long *stats, void *stream) {
+    g_error.clear();
+    if (!ctx || !d_blocks) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->profile) NTG_CUDA(cudaEventRecord(ctx->ev[0], S(stream)));
+    int r = chain_learned(ctx, mlp, d_bgra, w, h, opt, LEARN_ENCODE, d_blocks, nullptr, radius, margin, stats, stream);
+    if (r == NTG_OK && ctx->profile) {
+        NTG_CUDA(cudaEventRecord(ctx->ev[1], S(stream)));
+        NTG_CUDA(cudaEventRecord(ctx->ev[2], S(stream)));
+    }
+    return r;
+}
+
 int ntg_compress_chain(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt, void *d_blocks,
                        void *stream) {
     g_error.clear();

@@ -162,8 +162,9 @@ __device__ __forceinline__ float mse_of(const Lane<float4> &in, const Lane<float
 }
 
 // compute_sat (src/nvtt/icbc.h:1812-1882) from n colours (xyz) and weights (w) in `col`.
-// Writes the prefix sums in principal-axis order to `sat`. Returns n.
-__device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &sat) {
+// Writes the prefix sums in principal-axis order to `sat` (and, when asked, the order itself as
+// 4-bit indices into `col`). Returns n.
+__device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &sat, uint64_t *order_out = nullptr) {
     // computeCentroid / computeCovariance (src/nvtt/icbc.h:1700-1741)
     f3 c = mk3(0, 0, 0);
     float total = 0.0f;
@@ -216,6 +217,7 @@ __device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &s
             }
         }
     }
+    if (order_out) *order_out = order;
     float4 acc = col[(int)(order & 15)];
     acc = make_float4(acc.x * acc.w, acc.y * acc.w, acc.z * acc.w, acc.w);
     sat[0] = acc;
@@ -281,6 +283,21 @@ __device__ void cluster_fit_four(const Lane<float4> &sat, int n, f3 metric, f3 &
     if (bi >= 0) four_eval(sat, c_tab.four[bi], sum, wsum, metric, start, end);
 }
 
+// The full search's best ordering code (0 when none), for training targets.
+__device__ uint32_t best_order_four(const Lane<float4> &sat, int n, f3 metric) {
+    const float4 s = sat[n - 1];
+    const f3 sum = xyz(s);
+    float best = FLT_MAX;
+    uint32_t bo = 0;
+    const int total = c_tab.four_total[n - 1];
+    for (int i = 0; i < total; i++) {
+        f3 a, b;
+        const float e = four_eval(sat, c_tab.four[i], sum, s.w, metric, a, b);
+        if (e < best) { best = e; bo = c_tab.four[i]; }
+    }
+    return bo;
+}
+
 // One ordering of cluster_fit_three (src/nvtt/icbc.h:2016-2247).
 __device__ __forceinline__ float three_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
                                             f3 &b) {
@@ -296,6 +313,20 @@ __device__ __forceinline__ float three_eval(const Lane<float4> &sat, uint32_t o,
     const float b2 = w2 + ab;
     const f3 ax = x0 + (x1 * 0.5f);
     return cf_eval(ax, sum, a2, b2, ab, metric, a, b);
+}
+
+__device__ uint32_t best_order_three(const Lane<float4> &sat, int n, f3 metric) {
+    const float4 s = sat[n - 1];
+    const f3 sum = xyz(s);
+    float best = FLT_MAX;
+    uint32_t bo = 0;
+    const int total = c_tab.three_total[n - 1];
+    for (int i = 0; i < total; i++) {
+        f3 a, b;
+        const float e = three_eval(sat, c_tab.three[i], sum, s.w, metric, a, b);
+        if (e < best) { best = e; bo = c_tab.three[i]; }
+    }
+    return bo;
 }
 
 __device__ void cluster_fit_three(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
@@ -358,23 +389,11 @@ __device__ __forceinline__ int find_job(const EncJob *jobs, int njobs, long long
     return lo;
 }
 
-template <int LEVEL>  // 0: icbc Level1, 7: Level8, 8: Level9
-__global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
-    extern __shared__ float4 smem[];
-    const int T = blockDim.x;
-    const int t = threadIdx.x;
-    const long long gblk = (long long)blockIdx.x * T + t;
-    if (gblk >= nblocks) return;
-    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
-    const int blk = (int)(gblk - J.first_block);
-    Lane<float4> in{smem + t, T};
-    Lane<float4> col{smem + 16 * T + t, T};
-    Lane<float4> sat{smem + 32 * T + t, T};
-    Lane<float> wi{reinterpret_cast<float *>(smem + 48 * T) + t, T};
-    const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
-    uint8_t *const out = J.out + 8 * (size_t)blk;
 
-    // FloatColorCompressorTask gather (src/nvtt/BlockCompressor.cpp:116-166)
+// FloatColorCompressorTask gather (src/nvtt/BlockCompressor.cpp:116-166): the block's 16 texels
+// after the output transform, weight saturate(alpha) under AlphaMode_Transparency, texels outside
+// the image at weight 0.
+__device__ __forceinline__ void gather_block(const EncJob &J, int blk, const Lane<float4> &in, const Lane<float> &wi) {
     const int bx = blk % J.bw, by = blk / J.bw;
     const size_t n = (size_t)J.w * J.h;
     const int vw = min(J.w - bx * 4, 4), vh = min(J.h - by * 4, 4);
@@ -403,6 +422,71 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
                 wi[k] = 0.0f;
             }
         }
+}
+
+// reduce_colors (src/nvtt/icbc.h:1638-1683), threshold 1/256: merges near-equal colours of
+// positive weight into `col` (weighted mean, summed weight). Returns the colour count.
+__device__ __forceinline__ int reduce_colors(const Lane<float4> &in, const Lane<float> &wi, const Lane<float4> &col,
+                                             bool &any_black) {
+    const float thr = 1.0f / 256;
+    int cnt = 0;
+    any_black = false;
+    for (int i = 0; i < 16; i++) {
+        float wt = wi[i];
+        if (wt > 0) {
+            f3 c = xyz(in[i]);
+            int j;
+            for (j = 0; j < cnt; j++) {
+                float4 q = col[j];
+                if (fabsf(q.x - c.x) < thr && fabsf(q.y - c.y) < thr && fabsf(q.z - c.z) < thr) {
+                    float den = q.w + wt;
+                    f3 s = (xyz(q) * q.w) + (c * wt);
+                    col[j] = make_float4(s.x / den, s.y / den, s.z / den, q.w + wt);
+                    break;
+                }
+            }
+            if (j == cnt) { col[cnt] = make_float4(c.x, c.y, c.z, wt); cnt++; }
+            if (is_black(c)) any_black = true;
+        }
+    }
+    return cnt;
+}
+
+// compress_dxt1_single_color_optimal (src/nvtt/icbc.h:3274-3289)
+__device__ __forceinline__ Block1 single_colour(float4 c) {
+    Block1 o;
+    int r = (int)(uint8_t)(ic_sat(c.x) * 255 + 0.5f);
+    int g = (int)(uint8_t)(ic_sat(c.y) * 255 + 0.5f);
+    int b = (int)(uint8_t)(ic_sat(c.z) * 255 + 0.5f);
+    o.c0 = ((unsigned)c_tab.icbc_match5[r][0] << 11) | ((unsigned)c_tab.icbc_match6[g][0] << 5) | c_tab.icbc_match5[b][0];
+    o.c1 = ((unsigned)c_tab.icbc_match5[r][1] << 11) | ((unsigned)c_tab.icbc_match6[g][1] << 5) | c_tab.icbc_match5[b][1];
+    o.idx = 0xaaaaaaaau;
+    if (o.c0 < o.c1) { unsigned tt = o.c0; o.c0 = o.c1; o.c1 = tt; o.idx ^= 0x55555555u; }
+    return o;
+}
+
+template <int LEVEL>  // 0: icbc Level1, 7: Level8, 8: Level9
+__global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
+                                            const long long *__restrict__ list, const unsigned long long *__restrict__ count) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x;
+    const int t = threadIdx.x;
+    long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    if (list) {  // a subset of the jobs' blocks (the learned path's fallbacks), *count long
+        if ((unsigned long long)gblk >= *count) return;
+        gblk = list[gblk];
+    }
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    Lane<float4> in{smem + t, T};
+    Lane<float4> col{smem + 16 * T + t, T};
+    Lane<float4> sat{smem + 32 * T + t, T};
+    Lane<float> wi{reinterpret_cast<float *>(smem + 48 * T) + t, T};
+    const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
+    uint8_t *const out = J.out + 8 * (size_t)blk;
+
+    gather_block(J, blk, in, wi);
 
     Block1 o{0, 0, 0};
     float err = FLT_MAX;
@@ -454,44 +538,15 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
         return;
     }
 
-    // reduce_colors (src/nvtt/icbc.h:1638-1683), threshold 1/256
-    const float thr = 1.0f / 256;
-    int cnt = 0;
     bool any_black = false;
-    for (int i = 0; i < 16; i++) {
-        float wt = wi[i];
-        if (wt > 0) {
-            f3 c = xyz(in[i]);
-            int j;
-            for (j = 0; j < cnt; j++) {
-                float4 q = col[j];
-                if (fabsf(q.x - c.x) < thr && fabsf(q.y - c.y) < thr && fabsf(q.z - c.z) < thr) {
-                    float den = q.w + wt;
-                    f3 s = (xyz(q) * q.w) + (c * wt);
-                    col[j] = make_float4(s.x / den, s.y / den, s.z / den, q.w + wt);
-                    break;
-                }
-            }
-            if (j == cnt) { col[cnt] = make_float4(c.x, c.y, c.z, wt); cnt++; }
-            if (is_black(c)) any_black = true;
-        }
-    }
+    const int cnt = reduce_colors(in, wi, col, any_black);
 
     if (cnt == 0) {
         store_block(out, Block1{0, 0, 0});
         return;
     }
     if (cnt == 1) {
-        // compress_dxt1_single_color_optimal (src/nvtt/icbc.h:3274-3289)
-        float4 c = col[0];
-        int r = (int)(uint8_t)(ic_sat(c.x) * 255 + 0.5f);
-        int g = (int)(uint8_t)(ic_sat(c.y) * 255 + 0.5f);
-        int b = (int)(uint8_t)(ic_sat(c.z) * 255 + 0.5f);
-        o.c0 = ((unsigned)c_tab.icbc_match5[r][0] << 11) | ((unsigned)c_tab.icbc_match6[g][0] << 5) | c_tab.icbc_match5[b][0];
-        o.c1 = ((unsigned)c_tab.icbc_match5[r][1] << 11) | ((unsigned)c_tab.icbc_match6[g][1] << 5) | c_tab.icbc_match5[b][1];
-        o.idx = 0xaaaaaaaau;
-        if (o.c0 < o.c1) { unsigned tt = o.c0; o.c0 = o.c1; o.c1 = tt; o.idx ^= 0x55555555u; }
-        store_block(out, o);
+        store_block(out, single_colour(col[0]));
         return;
     }
 
@@ -527,6 +582,336 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     store_block(out, o);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Learned endpoint proposal (no counterpart in the reference). The network reads a block's texels
+// and proposes its two endpoints and the error of the full cluster fit. The proposal's palette
+// assigns each of the block's reduced colours, in the cluster fit's principal-axis order, to a
+// cluster; the cumulative cluster ends give an ordering of cluster_fit_four (and of
+// cluster_fit_three), and only the orderings within `radius` of it in every cluster end are
+// evaluated - with the same arithmetic and in the same order as the full search, so a block whose
+// best ordering lies in that neighbourhood gets exactly the full fit's result. A block whose
+// pruned result's error exceeds (1 + margin) x the network's estimate of the full fit's error is
+// listed for the full fit.
+
+// The network works in each block's principal frame: texels centred on the block's weighted mean,
+// divided by its RMS deviation (plus 1/255), rotated onto the principal axis v of their weighted
+// covariance (power iteration as in the cluster fit; v points towards brighter colours) and two
+// axes orthogonal to it, and sorted along v (stable; texels of weight 0 sit at the mean). The
+// endpoints are expressed in the same frame, and the fit's error as a log ratio to the block's
+// total weighted variance V (evaluate_mse's units): err_estimate = (V + 1) exp(y6) - 1.
+struct Frame {
+    f3 mu, v, u1, u2;
+    float sigma, var;
+    __device__ f3 to(f3 c) const {
+        const f3 d = (c - mu) * (1.0f / sigma);
+        return mk3(dot(d, v), dot(d, u1), dot(d, u2));
+    }
+    __device__ f3 from(f3 q) const { return mu + ((v * q.x) + ((u1 * q.y) + (u2 * q.z))) * sigma; }
+};
+
+__device__ __forceinline__ Frame block_frame(const Lane<float4> &in, const Lane<float> &wi, f3 cw) {
+    Frame f;
+    float ws = 0.0f;
+    f3 m = mk3(0, 0, 0);
+    for (int i = 0; i < 16; i++) { const float w = wi[i]; ws += w; m = m + xyz(in[i]) * w; }
+    f.mu = ws > 0 ? m * (1.0f / ws) : mk3(0, 0, 0);
+    float ss = 0.0f, var = 0.0f, m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0;
+    for (int i = 0; i < 16; i++) {
+        const float w = wi[i];
+        const f3 d = xyz(in[i]) - f.mu;
+        const f3 dw = (d * cw) * 255.0f;
+        ss += w * dot(d, d);
+        var += w * dot(dw, dw);
+        m0 += w * d.x * d.x; m1 += w * d.x * d.y; m2 += w * d.x * d.z;
+        m3 += w * d.y * d.y; m4 += w * d.y * d.z; m5 += w * d.z * d.z;
+    }
+    f.sigma = (ws > 0 ? sqrtf(ss / (3.0f * ws)) : 0.0f) + 1.0f / 255.0f;
+    f.var = var;
+    f3 v = mk3(1, 1, 1);
+    if (!(m0 == 0 && m3 == 0 && m5 == 0)) {
+        const f3 r0 = mk3(m0, m1, m2), r1 = mk3(m1, m3, m4), r2 = mk3(m2, m4, m5);
+        const float l0 = dot(r0, r0), l1 = dot(r1, r1), l2 = dot(r2, r2);
+        v = (l0 > l1 && l0 > l2) ? r0 : (l1 > l2 ? r1 : r2);
+        for (int it = 0; it < 8; it++) {
+            const f3 q = mk3(v.x * m0 + v.y * m1 + v.z * m2, v.x * m1 + v.y * m3 + v.z * m4, v.x * m2 + v.y * m4 + v.z * m5);
+            const float nrm = sqrtf(dot(q, q));
+            if (!(nrm > 0)) break;
+            v = q * (1.0f / nrm);
+        }
+    }
+    float vn = sqrtf(dot(v, v));
+    v = vn > 0 ? v * (1.0f / vn) : mk3(0.57735027f, 0.57735027f, 0.57735027f);
+    if (v.x + v.y + v.z < 0) v = v * -1.0f;
+    // the coordinate axis least aligned with v, made orthogonal to it; then their cross product
+    const float ax = fabsf(v.x), ay = fabsf(v.y), az = fabsf(v.z);
+    f3 e = ax <= ay && ax <= az ? mk3(1, 0, 0) : (ay <= az ? mk3(0, 1, 0) : mk3(0, 0, 1));
+    f3 u1 = e - v * dot(e, v);
+    u1 = u1 * (1.0f / sqrtf(dot(u1, u1)));
+    f.v = v;
+    f.u1 = u1;
+    f.u2 = mk3(v.y * u1.z - v.z * u1.y, v.z * u1.x - v.x * u1.z, v.x * u1.y - v.y * u1.x);
+    return f;
+}
+
+// The network's input: the block's 16 texels as RGB in [0, 1] (as the encoder sees them), in
+// order of their projection on the block's principal axis v (stable; texels of weight 0 take the
+// block's mean colour).
+__global__ void __launch_bounds__(64) k_bc1_features(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
+                                                     float *__restrict__ x) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    Lane<float4> in{smem + t, T};
+    Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
+    gather_block(J, (int)(gblk - J.first_block), in, wi);
+    const Frame f = block_frame(in, wi, mk3(J.cw[0], J.cw[1], J.cw[2]));
+    for (int k = 0; k < 16; k++) {  // w = the projection, the sort key
+        const f3 c = wi[k] > 0 ? xyz(in[k]) : f.mu;
+        in[k] = make_float4(c.x, c.y, c.z, dot(c - f.mu, f.v));
+    }
+    for (int i = 1; i < 16; i++) {
+        const float4 key = in[i];
+        int j = i - 1;
+        while (j >= 0 && in[j].w > key.w) { in[j + 1] = in[j]; j--; }
+        in[j + 1] = key;
+    }
+    float *o = x + gblk * 48;
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+        const float4 v = in[k];
+        o[3 * k] = v.x; o[3 * k + 1] = v.y; o[3 * k + 2] = v.z;
+    }
+}
+
+// True when the cluster fit's axis order (ascending projection on its own, arbitrarily signed
+// principal vector) runs from brighter to darker along the block frame's axis v: the orderings are
+// then expressed mirrored, so that the network always sees them darker-first, like its inputs.
+__device__ __forceinline__ bool axis_reversed(const Lane<float4> &col, int n, uint64_t order, f3 v) {
+    const float first = dot(xyz(col[(int)(order & 15)]), v);
+    const float last = dot(xyz(col[(int)((order >> (4 * (n - 1))) & 15)]), v);
+    return first > last;
+}
+
+// Cumulative weight fraction of the sorted colours up to ordering end e (-1: none).
+__device__ __forceinline__ float cum_frac(const Lane<float4> &sat, int e, float wsum) {
+    return e < 0 ? 0.0f : sat[e].w / wsum;
+}
+
+// Training targets: the orderings the full searches choose for the block, as cumulative weight
+// fractions of its colours in principal-axis order - three ends of the four-cluster fit, two of
+// the three-cluster fit (over the non-black colours when the block has black ones; 0, 1 when it
+// has none to fit) - then log((SSE + 1) / (V + 1)) of the encoded block `J.out` against its
+// texels, and 0 twice.
+__global__ void __launch_bounds__(64) k_bc1_targets(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
+                                                    float *__restrict__ tg) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    Lane<float4> in{smem + t, T};
+    Lane<float4> col{smem + 16 * T + t, T};
+    Lane<float4> sat{smem + 32 * T + t, T};
+    Lane<float> wi{reinterpret_cast<float *>(smem + 48 * T) + t, T};
+    const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
+    gather_block(J, blk, in, wi);
+    const uint2 b = *reinterpret_cast<const uint2 *>(J.out + 8 * (size_t)blk);
+    Pal3 pal;
+    palette_f(b.x & 0xFFFF, b.x >> 16, pal);
+    const float sse = block_mse(in, wi, cw, pal, b.y);
+    const Frame f = block_frame(in, wi, cw);
+    float *o = tg + gblk * 8;
+    float w4[3] = {0, 0, 0}, w3[2] = {0, 1};
+    bool any_black = false;
+    const int cnt = reduce_colors(in, wi, col, any_black);
+    if (cnt >= 2) {
+        const f3 metric = cw * cw;
+        uint64_t order;
+        int sn = compute_sat(col, cnt, sat, &order);
+        float wsum = sat[sn - 1].w;
+        uint32_t bo = best_order_four(sat, sn, metric);
+        w4[0] = cum_frac(sat, (int)(bo & 255) - 1, wsum);
+        w4[1] = cum_frac(sat, (int)((bo >> 8) & 255) - 1, wsum);
+        w4[2] = cum_frac(sat, (int)((bo >> 16) & 255) - 1, wsum);
+        if (axis_reversed(col, sn, order, f.v)) { const float a = w4[0]; w4[0] = 1 - w4[2]; w4[1] = 1 - w4[1]; w4[2] = 1 - a; }
+        bool run3 = true;
+        if (any_black) {
+            int m = 0;
+            for (int i = 0; i < cnt; i++) {
+                float4 q = col[i];
+                if (is_black(xyz(q))) continue;
+                col[m++] = q;
+            }
+            if (m == 0) run3 = false;
+            else sn = compute_sat(col, m, sat, &order);
+        }
+        if (run3) {
+            wsum = sat[sn - 1].w;
+            bo = best_order_three(sat, sn, metric);
+            w3[0] = cum_frac(sat, (int)(bo & 255) - 1, wsum);
+            w3[1] = cum_frac(sat, (int)((bo >> 8) & 255) - 1, wsum);
+            if (axis_reversed(col, sn, order, f.v)) { const float a = w3[0]; w3[0] = 1 - w3[1]; w3[1] = 1 - a; }
+        }
+    }
+    o[0] = w4[0]; o[1] = w4[1]; o[2] = w4[2]; o[3] = w3[0]; o[4] = w3[1];
+    o[5] = logf((sse + 1.0f) / (f.var + 1.0f));
+    o[6] = 0.0f;
+    o[7] = 0.0f;
+}
+
+// Ordering end of a cumulative weight fraction: the last sorted colour whose cumulative weight is
+// within the fraction (-1 when none is).
+__device__ __forceinline__ int frac_end(const Lane<float4> &sat, int n, float frac) {
+    const float lim = frac * sat[n - 1].w * (1.0f + 1e-5f) + 1e-7f;
+    int e = -1;
+    for (int k = 0; k < n; k++)
+        if (sat[k].w <= lim) e = k;
+    return e;
+}
+
+__device__ __forceinline__ uint32_t pack_order(int e0, int e1, int e2) {
+    return (uint32_t)(e0 + 1) | ((uint32_t)(e1 + 1) << 8) | ((uint32_t)(e2 + 1) << 16);
+}
+
+// cluster_fit_four over the orderings whose cluster ends lie within r of (e0, e1, e2), in the full
+// search's order (last end, then first, then second); returns the number evaluated.
+__device__ int pruned_four(const Lane<float4> &sat, int n, f3 metric, int e0, int e1, int e2, int r, f3 &start, f3 &end) {
+    const float4 s = sat[n - 1];
+    const f3 sum = xyz(s);
+    const float wsum = s.w;
+    float best = FLT_MAX;
+    uint32_t bo = 0;
+    bool found = false;
+    int evaluated = 0;
+    for (int c = max(0, e2 - r); c <= min(n - 1, e2 + r); c++)
+        for (int a = max(-1, e0 - r); a <= min(c, e0 + r); a++)
+            for (int b = max(a, e1 - r); b <= min(c, e1 + r); b++) {
+                f3 pa, pb;
+                const uint32_t o = pack_order(a, b, c);
+                const float e = four_eval(sat, o, sum, wsum, metric, pa, pb);
+                evaluated++;
+                if (e < best) { best = e; bo = o; found = true; }
+            }
+    start = mk3(0, 0, 0);
+    end = mk3(0, 0, 0);
+    if (found) four_eval(sat, bo, sum, wsum, metric, start, end);
+    return evaluated;
+}
+
+__device__ int pruned_three(const Lane<float4> &sat, int n, f3 metric, int e0, int e1, int r, f3 &start, f3 &end) {
+    const float4 s = sat[n - 1];
+    const f3 sum = xyz(s);
+    const float wsum = s.w;
+    float best = FLT_MAX;
+    uint32_t bo = 0;
+    bool found = false;
+    int evaluated = 0;
+    for (int c = max(0, e1 - r); c <= min(n - 1, e1 + r); c++)
+        for (int a = max(-1, e0 - r); a <= min(c, e0 + r); a++) {
+            f3 pa, pb;
+            const uint32_t o = (uint32_t)(a + 1) | ((uint32_t)(c + 1) << 8);
+            const float e = three_eval(sat, o, sum, wsum, metric, pa, pb);
+            evaluated++;
+            if (e < best) { best = e; bo = o; found = true; }
+        }
+    start = mk3(0, 0, 0);
+    end = mk3(0, 0, 0);
+    if (found) three_eval(sat, bo, sum, wsum, metric, start, end);
+    return evaluated;
+}
+
+// Warp-aggregated append of this thread's block to `list` (count in *n) when `take`.
+__device__ __forceinline__ void append_block(bool take, long long gblk, long long *list, unsigned long long *n) {
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync(active, take);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(active) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(n, (unsigned long long)__popc(mask));
+    base = __shfl_sync(active, base, leader);
+    if (take) list[base + __popc(mask & ((1u << lane) - 1))] = gblk;
+}
+
+// stats[0] += blocks written here, stats[1] = fallback count (list length), stats[2] += orderings evaluated
+__global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
+                                                    const float *__restrict__ y, int radius, float margin,
+                                                    long long *__restrict__ fallback, unsigned long long *__restrict__ stats) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    Lane<float4> in{smem + t, T};
+    Lane<float4> col{smem + 16 * T + t, T};
+    Lane<float4> sat{smem + 32 * T + t, T};
+    Lane<float> wi{reinterpret_cast<float *>(smem + 48 * T) + t, T};
+    const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
+    uint8_t *const out = J.out + 8 * (size_t)blk;
+    gather_block(J, blk, in, wi);
+    bool any_black = false;
+    const int cnt = reduce_colors(in, wi, col, any_black);
+    bool take = false;
+    int evaluated = 0;
+    if (cnt <= 1) {
+        store_block(out, cnt == 0 ? Block1{0, 0, 0} : single_colour(col[0]));
+    } else {
+        const float *yp = y + gblk * 16;
+        const Frame f = block_frame(in, wi, cw);
+        const float full_pred = (f.var + 1.0f) * expf(yp[5]) - 1.0f;
+        const f3 metric = cw * cw;
+        uint64_t order;
+        int sn = compute_sat(col, cnt, sat, &order);
+        float q0 = yp[0], q1 = yp[1], q2 = yp[2];
+        if (axis_reversed(col, sn, order, f.v)) { const float a = q0; q0 = 1 - q2; q1 = 1 - q1; q2 = 1 - a; }
+        const int e0 = frac_end(sat, sn, q0), e1 = max(e0, frac_end(sat, sn, q1));
+        const int e2 = max(max(e1, 0), frac_end(sat, sn, q2));
+        f3 s0, s1;
+        evaluated += pruned_four(sat, sn, metric, e0, e1, e2, radius, s0, s1);
+        Block1 o{0, 0, 0}, cf;
+        float err = FLT_MAX;
+        float cerr = output_block4(in, wi, cw, s0, s1, cf);
+        bool run3 = true;
+        if (any_black) {
+            int m = 0;
+            for (int i = 0; i < cnt; i++) {
+                float4 q = col[i];
+                if (is_black(xyz(q))) continue;
+                col[m++] = q;
+            }
+            if (m == 0) run3 = false;
+            else sn = compute_sat(col, m, sat, &order);
+        }
+        if (run3) {
+            float r0 = yp[3], r1 = yp[4];
+            if (axis_reversed(col, sn, order, f.v)) { const float a = r0; r0 = 1 - r1; r1 = 1 - a; }
+            const int f0 = frac_end(sat, sn, r0), f1 = max(max(f0, 0), frac_end(sat, sn, r1));
+            evaluated += pruned_three(sat, sn, metric, f0, f1, radius, s0, s1);
+            Block1 b3;
+            float e3 = output_block3(in, wi, cw, true, s0, s1, b3);
+            if (e3 < cerr) { cerr = e3; cf = b3; }
+        }
+        if (cerr < err) { o = cf; err = cerr; }
+        take = !(err <= (1.0f + margin) * full_pred);  // NaN estimates fall back too
+        if (!take) store_block(out, o);
+    }
+    append_block(take, gblk, fallback, &stats[1]);
+    // warp-aggregated statistics
+    const unsigned active = __activemask();
+    unsigned long long written = take ? 0 : 1, ev = (unsigned long long)evaluated;
+    for (int off = 16; off > 0; off >>= 1) {
+        written += __shfl_down_sync(active, written, off);
+        ev += __shfl_down_sync(active, ev, off);
+    }
+    if ((threadIdx.x & 31) == __ffs(active) - 1) {
+        atomicAdd(&stats[0], written);
+        atomicAdd(&stats[2], ev);
+    }
+}
+
 int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
     const int T = threads == 32 ? 32 : 64;  // blocks per CTA (one thread per 4x4 block)
@@ -538,9 +923,56 @@ int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, 
         cudaFuncSetAttribute(k_bc1<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         cudaFuncSetAttribute(k_bc1<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     }
-    if (quality == 0) k_bc1<0><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks);
-    else if (quality == 2) k_bc1<8><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks);
-    else k_bc1<7><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks);
+    if (quality == 0) k_bc1<0><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks, nullptr, nullptr);
+    else if (quality == 2) k_bc1<8><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks, nullptr, nullptr);
+    else k_bc1<7><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks, nullptr, nullptr);
+    return launch_status();
+}
+
+static size_t bc1_smem(int T) { return (size_t)T * (48 * sizeof(float4) + 16 * sizeof(float)); }
+
+template <typename K>
+static void allow_smem(K kernel, size_t bytes, std::atomic<unsigned long long> &configured) {
+    if (first_use_on_device(configured)) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+int launch_bc1_features(const EncJob *d_jobs, int njobs, long long nblocks, float *x, cudaStream_t s) {
+    if (nblocks == 0) return 0;
+    const int T = 64;
+    k_bc1_features<<<(unsigned)((nblocks + T - 1) / T), T, (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float)), s>>>(
+        d_jobs, njobs, nblocks, x);
+    return launch_status();
+}
+
+int launch_bc1_targets(const EncJob *d_jobs, int njobs, long long nblocks, float *tg, cudaStream_t s) {
+    if (nblocks == 0) return 0;
+    const int T = 64;  // texels, colours, summed-area table and weights per thread, as k_bc1
+    static std::atomic<unsigned long long> configured{0};
+    allow_smem(k_bc1_targets, bc1_smem(T), configured);
+    k_bc1_targets<<<(unsigned)((nblocks + T - 1) / T), T, bc1_smem(T), s>>>(d_jobs, njobs, nblocks, tg);
+    return launch_status();
+}
+
+int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const float *y, int radius, float margin,
+                       long long *fallback, unsigned long long *stats, cudaStream_t s) {
+    if (nblocks == 0) return 0;
+    const int T = 64;
+    static std::atomic<unsigned long long> configured{0};
+    allow_smem(k_bc1_learned, bc1_smem(T), configured);
+    k_bc1_learned<<<(unsigned)((nblocks + T - 1) / T), T, bc1_smem(T), s>>>(d_jobs, njobs, nblocks, y, radius, margin,
+                                                                            fallback, stats);
+    return launch_status();
+}
+
+// The full Level8 fit over a list of blocks of the jobs (the learned path's fallbacks); the list's
+// length stays on the device, so the sequence needs no host round trip.
+int launch_bc1_list(const EncJob *d_jobs, int njobs, const long long *list, const unsigned long long *d_count,
+                    long long max_count, cudaStream_t s) {
+    if (max_count == 0) return 0;
+    const int T = 64;
+    static std::atomic<unsigned long long> configured{0};
+    allow_smem(k_bc1<7>, bc1_smem(T), configured);
+    k_bc1<7><<<(unsigned)((max_count + T - 1) / T), T, bc1_smem(T), s>>>(d_jobs, njobs, max_count, list, d_count);
     return launch_status();
 }
 

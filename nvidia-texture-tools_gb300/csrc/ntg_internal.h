@@ -46,6 +46,21 @@ int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, 
 int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 
+// Learned endpoint proposal, BC1 Normal quality: the network's inputs (x [nblocks x 48]), training
+// targets from encoded blocks (tg [nblocks x 8]), the pruned fit from the network's outputs
+// (y [nblocks x 16]) listing the blocks that need the full fit, and the full fit over such a list.
+int launch_bc1_features(const EncJob *d_jobs, int njobs, long long nblocks, float *x, cudaStream_t s);
+int launch_bc1_targets(const EncJob *d_jobs, int njobs, long long nblocks, float *tg, cudaStream_t s);
+int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const float *y, int radius, float margin,
+                       long long *fallback, unsigned long long *stats, cudaStream_t s);
+// The full fit over the first *d_count entries of `list` (at most max_count; no host round trip).
+int launch_bc1_list(const EncJob *d_jobs, int njobs, const long long *list, const unsigned long long *d_count,
+                    long long max_count, cudaStream_t s);
+}  // namespace ntg
+struct ntg_mlp;
+namespace ntg {
+int mlp_forward_device(ntg_mlp *m, const float *d_x, long long rows, float *d_y, cudaStream_t s);
+
 // One buildNextMipmap step (source level -> destination level) of one texture. A mip launch walks a
 // list of these: its units (destination texels, tiles or strips, depending on the kernel) are
 // numbered across the jobs (`first_unit`), so one launch covers the same step of many textures.

@@ -57,10 +57,10 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)_
 
 // Shared-memory matrix descriptor: start address, leading (K) and stride (row-group) byte offsets,
 // the fixed 0b001 field at bits 46-48, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo = SBO) {
     uint64_t d = (uint64_t)((addr & 0x3FFFF) >> 4);
     d |= (uint64_t)((LBO >> 4) & 0x3FFF) << 16;
-    d |= (uint64_t)((SBO >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
     d |= (uint64_t)1 << 46;
     return d;
 }
@@ -377,6 +377,140 @@ __global__ void k_refresh(const float *__restrict__ p, __nv_bfloat16 *__restrict
     }
 }
 
+// ---- fused inference: the whole network per 128-row tile, on one CTA per SM ----
+// The weights stay in shared memory for the kernel's lifetime (canonical layout, whole K per
+// operand: row group stride = K / 8 x 128 bytes); a tile's activations go X -> TMEM -> GELU -> the
+// same shared-memory operand buffer -> TMEM -> ... so nothing but x and y touches global memory.
+// TMEM: layer 1 in columns [0, 256), layer 2 in [256, 512), layer 3 in [0, 16).
+constexpr uint32_t SBO_IN = IN / 8 * 128, SBO_HID = HID / 8 * 128;
+constexpr size_t F_W1 = 0, F_W2 = F_W1 + (size_t)HID * IN * 2, F_W3 = F_W2 + (size_t)HID * HID * 2,
+                 F_ACT = F_W3 + (size_t)OUTP * HID * 2, F_BIAS = F_ACT + (size_t)BM * HID * 2,
+                 F_BYTES = F_BIAS + (size_t)(HID + HID + OUTP) * 4;
+
+// Writes 8 bf16 (16 bytes) at row r, K chunk kc of a canonical operand with row-group stride sbo.
+__device__ __forceinline__ void put8(uint8_t *base, uint32_t sbo, int r, int kc, uint4 v) {
+    *reinterpret_cast<uint4 *>(base + (r >> 3) * sbo + kc * LBO + (r & 7) * 16) = v;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// Copies a bf16 row-major [rows x K] matrix from global memory into the canonical layout.
+__device__ void load_operand(uint8_t *dst, const __nv_bfloat16 *src, int rows, int K) {
+    const int chunks = K / 8;
+    for (int p = threadIdx.x; p < rows * chunks; p += blockDim.x) {
+        const int r = p / chunks, kc = p % chunks;
+        put8(dst, (uint32_t)chunks * LBO, r, kc, *reinterpret_cast<const uint4 *>(src + (size_t)r * K + kc * 8));
+    }
+}
+
+// Bias + GELU of this thread's 256 accumulator columns into its row of the activation operand.
+__device__ __forceinline__ void hidden_epilogue(uint32_t lane_addr, const float *bias, uint8_t *act, int row) {
+#pragma unroll 1
+    for (int c0 = 0; c0 < HID; c0 += 16) {
+        float v[16];
+        tmem_ld16(lane_addr + c0, v);
+        uint32_t p[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) p[i] = pack_bf16(gelu(v[2 * i] + bias[c0 + 2 * i]), gelu(v[2 * i + 1] + bias[c0 + 2 * i + 1]));
+        put8(act, SBO_HID, row, c0 / 8, make_uint4(p[0], p[1], p[2], p[3]));
+        put8(act, SBO_HID, row, c0 / 8 + 1, make_uint4(p[4], p[5], p[6], p[7]));
+    }
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16 *__restrict__ w1, const __nv_bfloat16 *__restrict__ w2,
+                                                       const __nv_bfloat16 *__restrict__ w3, const float *__restrict__ b1,
+                                                       const float *__restrict__ b2, const float *__restrict__ b3,
+                                                       const float *__restrict__ x, long long rows, float *__restrict__ y,
+                                                       int *status) {
+    extern __shared__ __align__(16) uint8_t smem[];  // 226 KB of the 227 KB a CTA may have
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    uint8_t *sw1 = smem + F_W1, *sw2 = smem + F_W2, *sw3 = smem + F_W3, *act = smem + F_ACT;
+    float *sb = reinterpret_cast<float *>(smem + F_BIAS);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = threadIdx.x;
+    if (warp == 0) tmem_alloc(&tmem_base, 512);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    load_operand(sw1, w1, HID, IN);
+    load_operand(sw2, w2, HID, HID);
+    load_operand(sw3, w3, OUTP, HID);
+    for (int i = threadIdx.x; i < HID; i += blockDim.x) { sb[i] = b1[i]; sb[HID + i] = b2[i]; }
+    if (threadIdx.x < OUTP) sb[2 * HID + threadIdx.x] = b3[threadIdx.x];
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base, lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t a_act = smem_u32(act), a_w1 = smem_u32(sw1), a_w2 = smem_u32(sw2), a_w3 = smem_u32(sw3);
+    uint32_t phase = 0;
+    bool ok = true;
+    const long long tiles = (rows + BM - 1) / BM;
+    for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const long long r = tile * BM + row;
+        // X: this thread's row as bf16 (rows past the end are zero)
+#pragma unroll
+        for (int kc = 0; kc < IN / 8; kc++) {
+            float4 a = make_float4(0, 0, 0, 0), b = a;
+            if (r < rows) {
+                a = *reinterpret_cast<const float4 *>(x + r * IN + kc * 8);
+                b = *reinterpret_cast<const float4 *>(x + r * IN + kc * 8 + 4);
+            }
+            put8(act, SBO_IN, row, kc, make_uint4(pack_bf16(a.x, a.y), pack_bf16(a.z, a.w), pack_bf16(b.x, b.y), pack_bf16(b.z, b.w)));
+        }
+#pragma unroll 1
+        for (int layer = 0; layer < 3 && ok; layer++) {
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                tc_fence_after();
+                if (layer == 0) {
+#pragma unroll
+                    for (int j = 0; j < IN / 16; j++)
+                        mma_bf16(tmem, smem_desc(a_act + j * 2 * LBO, SBO_IN), smem_desc(a_w1 + j * 2 * LBO, SBO_IN),
+                                 idesc_bf16(BM, HID), j > 0);
+                } else if (layer == 1) {
+#pragma unroll 4
+                    for (int j = 0; j < HID / 16; j++)
+                        mma_bf16(tmem + HID, smem_desc(a_act + j * 2 * LBO, SBO_HID), smem_desc(a_w2 + j * 2 * LBO, SBO_HID),
+                                 idesc_bf16(BM, HID), j > 0);
+                } else {
+#pragma unroll 4
+                    for (int j = 0; j < HID / 16; j++)
+                        mma_bf16(tmem, smem_desc(a_act + j * 2 * LBO, SBO_HID), smem_desc(a_w3 + j * 2 * LBO, SBO_HID),
+                                 idesc_bf16(BM, OUTP), j > 0);
+                }
+                mma_commit(&bar);
+            }
+            ok = __syncthreads_and(mbar_wait(&bar, phase & 1)) != 0;
+            phase++;
+            tc_fence_after();
+            if (!ok) break;
+            if (layer < 2) {
+                hidden_epilogue(lane_addr + (layer == 0 ? 0u : (uint32_t)HID), sb + layer * HID, act, row);
+            } else {
+                float v[16];
+                tmem_ld16(lane_addr, v);
+                if (r < rows) {
+                    float4 *o = reinterpret_cast<float4 *>(y + r * OUTP);
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        o[q] = make_float4(v[4 * q] + sb[2 * HID + 4 * q], v[4 * q + 1] + sb[2 * HID + 4 * q + 1],
+                                           v[4 * q + 2] + sb[2 * HID + 4 * q + 2], v[4 * q + 3] + sb[2 * HID + 4 * q + 3]);
+                }
+            }
+        }
+    }
+    if (!ok && status) atomicExch(status, 1);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
 int grid_of(long long n) { return (int)std::min<long long>(152LL * 8, std::max<long long>(1, (n + 255) / 256)); }
 
 }  // namespace mlp
@@ -538,13 +672,18 @@ int check_status(ntg_mlp *m, cudaStream_t s) {
 namespace ntg {
 // Forward pass for callers inside the library (the learned encoder): x fp32 [batch x 48] ->
 // y fp32 [batch x 16].
-int mlp_forward_device(ntg_mlp *m, const float *d_x, int batch, float *d_y, cudaStream_t s) {
-    if (!m || !d_x || !d_y || batch <= 0) return NTG_ERROR_INVALID_INPUT;
-    int r = ensure_batch(m, batch);
-    if (!r) r = load_inputs(m, d_x, batch, s);
-    if (!r) r = forward(m, batch, false, s);
-    if (r) return r;
-    MLP_CUDA(cudaMemcpyAsync(d_y, m->y, sizeof(float) * batch * OUTP, cudaMemcpyDeviceToDevice, s));
+int mlp_forward_device(ntg_mlp *m, const float *d_x, long long rows, float *d_y, cudaStream_t s) {
+    if (!m || !d_x || !d_y || rows <= 0) return NTG_ERROR_INVALID_INPUT;
+    static std::atomic<unsigned long long> configured{0};
+    if (first_use_on_device(configured))
+        cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)F_BYTES);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
+    const long long tiles = (rows + BM - 1) / BM;
+    const int grid = (int)std::min<long long>(tiles, std::max(1, sms));
+    k_mlp_infer<<<grid, 128, F_BYTES, s>>>(m->w1, m->w2, m->w3, m->p + OFF_B1, m->p + OFF_B2, m->b3p, d_x, rows, d_y,
+                                           m->status);
+    MLP_LAUNCH(launch_status());
     return NTG_OK;
 }
 }  // namespace ntg
@@ -574,7 +713,7 @@ int ntg_mlp_create(int device, unsigned long long seed, ntg_mlp **out) {
     fill(OFF_W1, (size_t)HID * IN, IN); fill(OFF_B1, HID, IN);
     fill(OFF_W2, (size_t)HID * HID, HID); fill(OFF_B2, HID, HID);
     fill(OFF_W3, (size_t)OUT * HID, HID); fill(OFF_B3, OUT, HID);
-    const float wout[OUT] = {1, 1, 1, 1, 1, 1, 0.25f, 0};
+    const float wout[OUT] = {1, 1, 1, 1, 1, 0.25f, 0, 0};
     MLP_CUDA(cudaMemcpy(m->p, p.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice));
     MLP_CUDA(cudaMemset(m->m, 0, NPARAM * sizeof(float)));
     MLP_CUDA(cudaMemset(m->v, 0, NPARAM * sizeof(float)));
@@ -612,6 +751,13 @@ int ntg_mlp_set_params(ntg_mlp *m, const float *h_params) {
 }
 
 int ntg_mlp_infer(ntg_mlp *m, const float *d_x, int batch, float *d_y, void *stream) {
+    if (!m || !d_x || !d_y || batch <= 0) return mlp_fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    MLP_CUDA(cudaSetDevice(m->device));
+    return mlp_forward_device(m, d_x, batch, d_y, (cudaStream_t)stream);
+}
+
+// The unfused forward pass (three k_gemm launches), as training runs it; for testing.
+int ntg_mlp_infer_unfused(ntg_mlp *m, const float *d_x, int batch, float *d_y, void *stream) {
     if (!m || !d_x || !d_y || batch <= 0) return mlp_fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
     int r = ensure_batch(m, batch);

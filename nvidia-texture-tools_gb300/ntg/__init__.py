@@ -108,10 +108,17 @@ def lib():
         "ntg_mlp_get_params": (_i, [_vp, _vp]),
         "ntg_mlp_set_params": (_i, [_vp, _vp]),
         "ntg_mlp_infer": (_i, [_vp, _vp, _i, _vp, _vp]),
+        "ntg_mlp_infer_unfused": (_i, [_vp, _vp, _i, _vp, _vp]),
         "ntg_mlp_gradients": (_i, [_vp, _vp, _vp, _i, _vp, ctypes.POINTER(_f), _vp]),
         "ntg_mlp_train_step": (_i, [_vp, _vp, _vp, _i, _f, _vp, _vp]),
         "ntg_mlp_status": (_i, [_vp]),
         "ntg_gemm_bf16": (_i, [_vp, _vp, _i, _i, _i, _vp, _vp]),
+        "ntg_compress_chain_learned": (_i, [_vp, _vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _i, _f, _vp,
+                                            ctypes.POINTER(ctypes.c_ulonglong), _vp]),
+        "ntg_chain_features": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
+        "ntg_compress_chain_proposed": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _i, _f, _vp,
+                                             ctypes.POINTER(ctypes.c_ulonglong), _vp]),
+        "ntg_chain_targets": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp, _vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -212,6 +219,41 @@ class Context:
         out = out if out is not None else torch.empty(total, dtype=torch.float32, device=bgra.device)
         _check(lib().ntg_mip_chain(self.h, bgra.data_ptr(), w, h, ctypes.byref(opt), out.data_ptr(), _stream_ptr(stream)))
         return out
+
+    def compress_chain_learned(self, mlp, bgra, w, h, opt: ChainOptions, radius=2, margin=0.01, out=None, stats=True,
+                               stream=None):
+        """Learned BC1 chain encode; returns (blocks, {kept, full_fit, orderings}) (stats synchronise)."""
+        import torch
+        out = out if out is not None else torch.empty(chain_bytes(w, h, opt), dtype=torch.uint8, device=bgra.device)
+        st = (ctypes.c_ulonglong * 3)()
+        _check(lib().ntg_compress_chain_learned(self.h, mlp.h, bgra.data_ptr(), w, h, ctypes.byref(opt), radius, margin,
+                                                out.data_ptr(), st if stats else None, _stream_ptr(stream)))
+        return out, ({"kept": st[0], "full_fit": st[1], "orderings": st[2]} if stats else None)
+
+    def compress_chain_proposed(self, proposals, bgra, w, h, opt: ChainOptions, radius=2, margin=0.01, out=None,
+                                stream=None):
+        """The pruned search seeded by caller-supplied proposals ([blocks x 16] float32 device tensor)."""
+        import torch
+        out = out if out is not None else torch.empty(chain_bytes(w, h, opt), dtype=torch.uint8, device=bgra.device)
+        st = (ctypes.c_ulonglong * 3)()
+        _check(lib().ntg_compress_chain_proposed(self.h, bgra.data_ptr(), w, h, ctypes.byref(opt), proposals.data_ptr(),
+                                                 radius, margin, out.data_ptr(), st, _stream_ptr(stream)))
+        return out, {"kept": st[0], "full_fit": st[1], "orderings": st[2]}
+
+    def chain_features(self, bgra, w, h, opt: ChainOptions, stream=None):
+        import torch
+        n = sum(nblocks(lw, lh) for lw, lh in chain_levels(w, h, opt.max_levels))
+        x = torch.empty((n, 48), dtype=torch.float32, device=bgra.device)
+        _check(lib().ntg_chain_features(self.h, bgra.data_ptr(), w, h, ctypes.byref(opt), x.data_ptr(), _stream_ptr(stream)))
+        return x
+
+    def chain_targets(self, bgra, w, h, opt: ChainOptions, blocks, stream=None):
+        import torch
+        n = sum(nblocks(lw, lh) for lw, lh in chain_levels(w, h, opt.max_levels))
+        t = torch.empty((n, 8), dtype=torch.float32, device=bgra.device)
+        _check(lib().ntg_chain_targets(self.h, bgra.data_ptr(), w, h, ctypes.byref(opt), blocks.data_ptr(), t.data_ptr(),
+                                       _stream_ptr(stream)))
+        return t
 
     def profile(self, enable: bool = True):
         _check(lib().ntg_profile_enable(self.h, int(enable)))
@@ -346,6 +388,13 @@ class MLP:
         b = x.shape[0]
         out = out if out is not None else torch.empty((b, self.OUTP), dtype=torch.float32, device=x.device)
         _check(lib().ntg_mlp_infer(self.h, x.data_ptr(), b, out.data_ptr(), _stream_ptr(stream)))
+        return out
+
+    def infer_unfused(self, x, out=None, stream=None):
+        import torch
+        b = x.shape[0]
+        out = out if out is not None else torch.empty((b, self.OUTP), dtype=torch.float32, device=x.device)
+        _check(lib().ntg_mlp_infer_unfused(self.h, x.data_ptr(), b, out.data_ptr(), _stream_ptr(stream)))
         return out
 
     def gradients(self, x, t, stream=None):

@@ -13,7 +13,7 @@ import math
 import numpy as np
 
 IN, HID, OUT = 48, 256, 8
-LOSS_WEIGHTS = np.array([1, 1, 1, 1, 1, 1, 0.25, 0], np.float64)
+LOSS_WEIGHTS = np.array([1, 1, 1, 1, 1, 0.25, 0, 0], np.float64)
 
 
 def bf16(x):

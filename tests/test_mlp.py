@@ -30,7 +30,7 @@ def test_gemm_matches_torch(m, n, k):
 def _data(n, seed):
     rng = np.random.default_rng(seed)
     x = rng.random((n, 48), dtype=np.float32)
-    t = np.concatenate([rng.random((n, 6)), rng.random((n, 1)) * 4, np.zeros((n, 1))], axis=1).astype(np.float32)
+    t = np.concatenate([rng.random((n, 5)), rng.random((n, 1)) * 4, np.zeros((n, 2))], axis=1).astype(np.float32)
     return x, t
 
 
@@ -40,10 +40,26 @@ def test_forward_matches_oracle():
     net = ntg.MLP(seed=11)
     try:
         x, _ = _data(512, 1)
-        y = net.infer(torch.from_numpy(x).cuda()).cpu().numpy()
+        y = net.infer_unfused(torch.from_numpy(x).cuda()).cpu().numpy()
         ref, _ = mlp_oracle.forward(net.get_params(), x)
         assert np.all(y[:, 8:] == 0)
         assert np.max(np.abs(y[:, :8] - ref)) < 2e-3 * max(1.0, np.abs(ref).max())
+    finally:
+        net.close()
+
+
+@pytest.mark.parametrize("rows", [1, 127, 128, 5000, 40000])
+def test_fused_inference_matches_unfused(rows):
+    """The persistent fused kernel (weights in shared memory, layers chained through TMEM) against
+    the three-product path the training uses."""
+    torch = _torch()
+    net = ntg.MLP(seed=rows)
+    try:
+        x, _ = _data(rows, rows + 1)
+        dx = torch.from_numpy(x).cuda()
+        a = net.infer(dx).cpu().numpy()
+        b = net.infer_unfused(dx).cpu().numpy()
+        assert np.max(np.abs(a - b)) < 1e-3 * max(1.0, np.abs(b).max())
     finally:
         net.close()
 
@@ -74,11 +90,11 @@ def test_training_reduces_loss():
     net = ntg.MLP(seed=3)
     try:
         x, t = _data(8192, 77)
-        # a learnable target: endpoints = per-block min / max of the first texel's channels
+        # a learnable target: per-block channel minima and maxima, and a log spread
         xt = x.reshape(-1, 16, 3)
         t[:, 0:3] = xt.min(axis=1)
-        t[:, 3:6] = xt.max(axis=1)
-        t[:, 6] = np.log1p(((xt - xt.mean(axis=1, keepdims=True)) ** 2).sum(axis=(1, 2)) * 255.0)
+        t[:, 3:5] = xt.max(axis=1)[:, :2]
+        t[:, 5] = np.log1p(((xt - xt.mean(axis=1, keepdims=True)) ** 2).sum(axis=(1, 2)) * 255.0)
         dx, dt = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
         _, loss0 = net.gradients(dx, dt)
         lossbuf = torch.zeros(1, dtype=torch.float32, device="cuda")
