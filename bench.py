@@ -594,20 +594,137 @@ def run_reference_batch(args):
     return 0
 
 
+# ---------------------------------------------------------------------------------------------
+# The learned endpoint proposal (BC1): trained on seeded blocks of both generators, evaluated on a
+# separate-seed 2048x2048 texture against the plain GPU cluster fit.
+
+LEARNED = {"train_blocks": 1 << 24, "train_size": 2048, "batch": 8192, "lr": 1e-3, "eval_size": 2048,
+           "radius": 1, "margin": 0.25}
+
+
+def run_gpu_learned(args):
+    import torch
+    import ntg
+    from ntg import learned
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    ctx = ntg.Context(local)
+    cfg = LEARNED
+    t0 = time.perf_counter()
+    x, t = learned.training_set(ctx, cfg["train_blocks"], seed=0x5EED, size=cfg["train_size"])
+    data_s = time.perf_counter() - t0
+    net = ntg.MLP(seed=0x4E4554)
+    steps = cfg["train_blocks"] // cfg["batch"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = learned.train(net, x, t, steps=steps, batch=cfg["batch"], lr=cfg["lr"])
+    train_s = time.perf_counter() - t0
+    del x, t
+    size = cfg["eval_size"]
+    kind = 1  # the RGBA8 generator: sRGB colour, alpha field, Kaiser mips, transparency
+    img = learned.generator_texture(kind, size, 0xE7A1 + kind)
+    opt = learned.generator_options(kind)
+    d = torch.from_numpy(img).cuda()
+    texels = chain_texels(size, size)
+    plain = ctx.compress_chain(d, size, size, opt)
+    out, st = ctx.compress_chain_learned(net, d, size, size, opt, radius=cfg["radius"], margin=cfg["margin"])
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed_steps(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / args.steps
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        learned_ms = timed_steps(lambda: ctx.compress_chain_learned(net, d, size, size, opt, radius=cfg["radius"],
+                                                                    margin=cfg["margin"], out=out, stats=False))
+        plain_ms = timed_steps(lambda: ctx.compress_chain(d, size, size, opt, out=plain))
+    value = texels / (learned_ms / 1000.0) / 1e6
+    rmse_plain = learned.chain_rmse(ctx, d, size, size, opt, plain)
+    rmse_learned = learned.chain_rmse(ctx, d, size, size, opt, out)
+    same = float((out.view(-1, 8) == plain.view(-1, 8)).all(dim=1).float().mean().item())
+    nb = plain.numel() // 8
+    # the network's inference kernel against the tensor-core peak (one call over every block)
+    xf = ctx.chain_features(d, size, size, opt)
+    y = net.infer(xf)
+    infer_ms = learned.timed(lambda: net.infer(xf, out=y))
+    flop = nb * 2 * (48 * 256 + 256 * 256 + 256 * 16)
+    peaks, peak_src = measured_peaks()
+    tflops = flop / (infer_ms / 1000.0) / 1e12
+    peak = peaks.get("bf16_tflops", 1900.0)
+    # end to end: host image in, blocks out, through the same call
+    h_in = torch.from_numpy(img.reshape(-1)).pin_memory()
+    h_out = torch.empty(out.numel(), dtype=torch.uint8).pin_memory()
+
+    def e2e_step():
+        d.view(-1).copy_(h_in, non_blocking=True)
+        ctx.compress_chain_learned(net, d, size, size, opt, radius=cfg["radius"], margin=cfg["margin"], out=out,
+                                   stats=False)
+        h_out.copy_(out, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_value = texels * args.steps / (time.perf_counter() - t0) / 1e6
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": learned_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32",
+            "data": "synthetic",
+            "config": {"workload": f"learned endpoint proposal, BC1 Normal: {size}x{size} separate-seed RGBA8 texture "
+                                   "(sRGB, alpha field, Kaiser mips, transparency), whole chain",
+                       "texels_per_step": texels, "blocks_per_step": nb, "l2": "flushed (256 MiB write) between steps",
+                       "network": "MLP 48-256-256-8, GELU, BF16 weights/activations, FP32 accumulation (tcgen05)",
+                       "training": f"Adam lr {cfg['lr']}, batch {cfg['batch']}, {steps} steps on {cfg['train_blocks']} "
+                                   f"seeded blocks of both generators; data {data_s:.1f} s, training {train_s:.1f} s, "
+                                   f"loss {float(losses[0]):.4f} -> {float(losses[-64:].mean()):.4f}",
+                       "radius": cfg["radius"], "margin": cfg["margin"]},
+            "learned": {"chain_ms": learned_ms, "plain_chain_ms": plain_ms, "speedup_vs_plain": plain_ms / learned_ms,
+                        "rmse": rmse_learned, "plain_rmse": rmse_plain, "rmse_delta_pct": 100 * (rmse_learned / rmse_plain - 1),
+                        "blocks_equal_to_plain": same, "full_fit_fraction": st["full_fit"] / nb,
+                        "orderings_per_block": st["orderings"] / max(1, st["kept"] + st["full_fit"])},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(img.nbytes),
+                    "d2h_bytes_per_step": int(out.numel()), "matches_device_path": bool(torch.equal(h_out, out.cpu()))},
+            "gpu_launches": None, "clocks": clk.summary(),
+            "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                         "traffic": None, "kernel": "k_mlp_infer (fused 3-layer tcgen05 inference, one call over all blocks)",
+                         "flop_per_block": 2 * (48 * 256 + 256 * 256 + 256 * 16), "ms": infer_ms, "peak_source": peak_src},
+            "cpu_baseline": None}
+    print(json.dumps(line), flush=True)
+    net.close()
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ntg", choices=["ntg", "reference"])
-    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS) + sorted(BATCHES))
+    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS) + sorted(BATCHES) + ["c3"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3
     if args.impl == "reference":
+        if args.workload == "c3":
+            print(json.dumps({"impl": "reference", "unavailable": "the learned proposal has no counterpart in the "
+                              "reference; its plain cluster fit is the c1/c0 reference arm"}), flush=True)
+            return 0
         return run_reference_batch(args) if args.workload in BATCHES else run_reference(args)
+    if args.workload == "c3":
+        return run_gpu_learned(args)
     return run_gpu_batch(args) if args.workload in BATCHES else run_gpu(args)
 
 

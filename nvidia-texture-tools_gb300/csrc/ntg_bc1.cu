@@ -667,21 +667,23 @@ __global__ void __launch_bounds__(64) k_bc1_features(const EncJob *__restrict__ 
     Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
     gather_block(J, (int)(gblk - J.first_block), in, wi);
     const Frame f = block_frame(in, wi, mk3(J.cw[0], J.cw[1], J.cw[2]));
-    for (int k = 0; k < 16; k++) {  // w = the projection, the sort key
-        const f3 c = wi[k] > 0 ? xyz(in[k]) : f.mu;
-        in[k] = make_float4(c.x, c.y, c.z, dot(c - f.mu, f.v));
-    }
-    for (int i = 1; i < 16; i++) {
-        const float4 key = in[i];
-        int j = i - 1;
-        while (j >= 0 && in[j].w > key.w) { in[j + 1] = in[j]; j--; }
-        in[j + 1] = key;
-    }
-    float *o = x + gblk * 48;
+    float key[16];
 #pragma unroll
     for (int k = 0; k < 16; k++) {
-        const float4 v = in[k];
-        o[3 * k] = v.x; o[3 * k + 1] = v.y; o[3 * k + 2] = v.z;
+        const f3 c = wi[k] > 0 ? xyz(in[k]) : f.mu;
+        in[k] = make_float4(c.x, c.y, c.z, 0.0f);
+        const float p = dot(c - f.mu, f.v);
+        key[k] = p == p ? p : 0.0f;  // NaN texels rank as the mean, so the ranks stay a permutation
+    }
+    // stable ranks along the axis (ties keep the texel order), then each texel to its rank
+    float *o = x + gblk * 48;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        int rank = 0;
+#pragma unroll
+        for (int j = 0; j < 16; j++) rank += (key[j] < key[i]) | ((key[j] == key[i]) & (j < i));
+        const float4 v = in[i];
+        o[3 * rank] = v.x; o[3 * rank + 1] = v.y; o[3 * rank + 2] = v.z;
     }
 }
 

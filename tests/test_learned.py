@@ -1,0 +1,107 @@
+"""The learned BC1 path (ntg_compress_chain_learned): the pruned ordering search and its full-fit
+fallback are exact where they claim to be, and a trained network gains over the same search
+without it while staying within 0.5% of the plain cluster fit's RMSE."""
+import numpy as np
+import pytest
+
+import ntg
+from ntg import learned
+
+pytestmark = pytest.mark.gpu
+
+INF = float("inf")
+
+
+def _same(a, b):
+    return (a.view(-1, 8) == b.view(-1, 8)).all(dim=1).float().mean().item()
+
+
+@pytest.fixture(scope="module")
+def net():
+    n = ntg.MLP(seed=21)
+    yield n
+    n.close()
+
+
+@pytest.mark.parametrize("kind,size", [(0, 96), (1, 128), (1, 37)])
+def test_wide_radius_is_the_full_search(ctx, net, kind, size):
+    """Radius 16 covers every ordering: the pruned search is the full search, block for block."""
+    import torch
+    img = learned.generator_texture(kind, size, 40 + size)
+    opt = learned.generator_options(kind)
+    d = torch.from_numpy(np.ascontiguousarray(img)).cuda()
+    plain = ctx.compress_chain(d, size, size, opt)
+    out, st = ctx.compress_chain_learned(net, d, size, size, opt, radius=16, margin=INF)
+    assert _same(out, plain) == 1.0
+    assert st["full_fit"] == 0
+
+
+def test_true_orderings_at_radius_zero(ctx):
+    """The targets' orderings, fed back as proposals, pick exactly the full fit's blocks."""
+    import torch
+    size = 128
+    img = learned.generator_texture(1, size, 77)
+    opt = learned.generator_options(1)
+    d = torch.from_numpy(img).cuda()
+    plain = ctx.compress_chain(d, size, size, opt)
+    t = ctx.chain_targets(d, size, size, opt, plain)
+    y = torch.zeros((t.shape[0], 16), dtype=torch.float32, device="cuda")
+    y[:, :6] = t[:, :6]
+    out, _ = ctx.compress_chain_proposed(y, d, size, size, opt, radius=0, margin=INF)
+    assert _same(out, plain) == 1.0
+
+
+def test_fallback_list_is_the_full_fit(ctx, net):
+    """A margin of -1 sends every fitted block to the full fit through the device-side list."""
+    import torch
+    size = 96
+    img = learned.generator_texture(0, size, 5)
+    opt = learned.generator_options(0)
+    d = torch.from_numpy(img).cuda()
+    plain = ctx.compress_chain(d, size, size, opt)
+    out, st = ctx.compress_chain_learned(net, d, size, size, opt, radius=0, margin=-1.0)
+    assert _same(out, plain) == 1.0
+    assert st["full_fit"] > 0
+
+
+def test_features_and_targets(ctx):
+    import torch
+    size = 64
+    img = learned.generator_texture(1, size, 3)
+    opt = learned.generator_options(1)
+    d = torch.from_numpy(img).cuda()
+    x = ctx.chain_features(d, size, size, opt)
+    t = ctx.chain_targets(d, size, size, opt, ctx.compress_chain(d, size, size, opt))
+    n = sum(ntg.nblocks(w, h) for w, h in ntg.chain_levels(size, size))
+    assert x.shape == (n, 48) and t.shape == (n, 8)
+    assert float(x.min()) >= 0.0 and float(x.max()) <= 1.0
+    f = t[:, :5]
+    assert float(f.min()) >= 0.0 and float(f.max()) <= 1.0 + 1e-6
+    assert bool((t[:, 0] <= t[:, 1] + 1e-6).all()) and bool((t[:, 1] <= t[:, 2] + 1e-6).all())
+
+
+def test_trained_network_gains_over_no_network(ctx):
+    """Trained on chains of the two generators, evaluated on a separate seed: the learned pruned
+    search stays within 0.5% of the plain fit's RMSE and finds the full fit's exact block more
+    often than the same search seeded without the network."""
+    import torch
+    x, t = learned.training_set(ctx, 1 << 20, seed=0x7E57, size=1024)
+    net = ntg.MLP(seed=9)
+    try:
+        losses = learned.train(net, x, t, steps=1024, batch=8192, lr=2e-3)
+        assert losses[-64:].mean() < 0.5 * losses[:8].mean()
+        size = 512
+        img = learned.generator_texture(1, size, 0xE7A1)
+        opt = learned.generator_options(1)
+        d = torch.from_numpy(img).cuda()
+        plain = ctx.compress_chain(d, size, size, opt)
+        rp = learned.chain_rmse(ctx, d, size, size, opt, plain)
+        out, st = ctx.compress_chain_learned(net, d, size, size, opt, radius=2, margin=INF)
+        rl = learned.chain_rmse(ctx, d, size, size, opt, out)
+        assert rl <= 1.005 * rp, (rl, rp)
+        base, _ = ctx.compress_chain_proposed(learned.uniform_proposals(plain.numel() // 8), d, size, size, opt,
+                                              radius=2, margin=INF)
+        assert _same(out, plain) > _same(base, plain) + 0.05, (_same(out, plain), _same(base, plain))
+        assert st["orderings"] < 200 * (st["kept"] + st["full_fit"])  # versus up to 1120 per block in full
+    finally:
+        net.close()
