@@ -599,7 +599,10 @@ def run_reference_batch(args):
 # separate-seed 2048x2048 texture against the plain GPU cluster fit.
 
 LEARNED = {"train_blocks": 1 << 24, "train_size": 2048, "batch": 8192, "lr": 1e-3, "eval_size": 2048,
-           "radius": 1, "margin": 0.25}
+           "radius": 1, "margin": 0.5,
+           # the radius / margin trade-off, measured on the same texture and reported beside the headline
+           "frontier": [(1, 0.01), (1, 0.1), (1, 0.25), (1, 0.5), (1, float("inf")), (2, 0.01), (2, 0.25), (2, float("inf")),
+                        (3, 0.25)]}
 
 
 def run_gpu_learned(args):
@@ -653,6 +656,14 @@ def run_gpu_learned(args):
     rmse_learned = learned.chain_rmse(ctx, d, size, size, opt, out)
     same = float((out.view(-1, 8) == plain.view(-1, 8)).all(dim=1).float().mean().item())
     nb = plain.numel() // 8
+    frontier = []
+    for r_, m_ in cfg["frontier"]:
+        o_, st_ = ctx.compress_chain_learned(net, d, size, size, opt, radius=r_, margin=m_)
+        ms_ = learned.timed(lambda: ctx.compress_chain_learned(net, d, size, size, opt, radius=r_, margin=m_, out=o_,
+                                                               stats=False))
+        rl_ = learned.chain_rmse(ctx, d, size, size, opt, o_)
+        frontier.append({"radius": r_, "margin": m_ if m_ != float("inf") else "inf", "speedup_vs_plain": plain_ms / ms_,
+                         "rmse_delta_pct": 100 * (rl_ / rmse_plain - 1), "full_fit_fraction": st_["full_fit"] / (plain.numel() // 8)})
     # the network's inference kernel against the tensor-core peak (one call over every block)
     xf = ctx.chain_features(d, size, size, opt)
     y = net.infer(xf)
@@ -691,7 +702,8 @@ def run_gpu_learned(args):
             "learned": {"chain_ms": learned_ms, "plain_chain_ms": plain_ms, "speedup_vs_plain": plain_ms / learned_ms,
                         "rmse": rmse_learned, "plain_rmse": rmse_plain, "rmse_delta_pct": 100 * (rmse_learned / rmse_plain - 1),
                         "blocks_equal_to_plain": same, "full_fit_fraction": st["full_fit"] / nb,
-                        "orderings_per_block": st["orderings"] / max(1, st["kept"] + st["full_fit"])},
+                        "orderings_per_block": st["orderings"] / max(1, st["kept"] + st["full_fit"]),
+                        "frontier": frontier},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(img.nbytes),
                     "d2h_bytes_per_step": int(out.numel()), "matches_device_path": bool(torch.equal(h_out, out.cpu()))},
             "gpu_launches": None, "clocks": clk.summary(),

@@ -655,36 +655,45 @@ __device__ __forceinline__ Frame block_frame(const Lane<float4> &in, const Lane<
 
 // The network's input: the block's 16 texels as RGB in [0, 1] (as the encoder sees them), in
 // order of their projection on the block's principal axis v (stable; texels of weight 0 take the
-// block's mean colour).
+// block's mean colour). Each warp stages its 32 rows in shared memory and writes them out as one
+// contiguous, coalesced run.
+constexpr int FEAT_STRIDE = 49;  // floats per staged row (odd: conflict-free)
+
 __global__ void __launch_bounds__(64) k_bc1_features(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
                                                      float *__restrict__ x) {
     extern __shared__ float4 smem[];
-    const int T = blockDim.x, t = threadIdx.x;
+    const int T = blockDim.x, t = threadIdx.x, lane = t & 31;
     const long long gblk = (long long)blockIdx.x * T + t;
-    if (gblk >= nblocks) return;
-    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
-    Lane<float4> in{smem + t, T};
-    Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
-    gather_block(J, (int)(gblk - J.first_block), in, wi);
-    const Frame f = block_frame(in, wi, mk3(J.cw[0], J.cw[1], J.cw[2]));
-    float key[16];
+    float *stage = reinterpret_cast<float *>(smem + 16 * T) + 16 * T + (t >> 5) * 32 * FEAT_STRIDE;
+    if (gblk < nblocks) {
+        const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+        Lane<float4> in{smem + t, T};
+        Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
+        gather_block(J, (int)(gblk - J.first_block), in, wi);
+        const Frame f = block_frame(in, wi, mk3(J.cw[0], J.cw[1], J.cw[2]));
+        float key[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-        const f3 c = wi[k] > 0 ? xyz(in[k]) : f.mu;
-        in[k] = make_float4(c.x, c.y, c.z, 0.0f);
-        const float p = dot(c - f.mu, f.v);
-        key[k] = p == p ? p : 0.0f;  // NaN texels rank as the mean, so the ranks stay a permutation
+        for (int k = 0; k < 16; k++) {
+            const f3 c = wi[k] > 0 ? xyz(in[k]) : f.mu;
+            in[k] = make_float4(c.x, c.y, c.z, 0.0f);
+            const float p = dot(c - f.mu, f.v);
+            key[k] = p == p ? p : 0.0f;  // NaN texels rank as the mean, so the ranks stay a permutation
+        }
+        // stable ranks along the axis (ties keep the texel order), then each texel to its rank
+        float *row = stage + lane * FEAT_STRIDE;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            int rank = 0;
+#pragma unroll
+            for (int j = 0; j < 16; j++) rank += (key[j] < key[i]) | ((key[j] == key[i]) & (j < i));
+            const float4 v = in[i];
+            row[3 * rank] = v.x; row[3 * rank + 1] = v.y; row[3 * rank + 2] = v.z;
+        }
     }
-    // stable ranks along the axis (ties keep the texel order), then each texel to its rank
-    float *o = x + gblk * 48;
-#pragma unroll
-    for (int i = 0; i < 16; i++) {
-        int rank = 0;
-#pragma unroll
-        for (int j = 0; j < 16; j++) rank += (key[j] < key[i]) | ((key[j] == key[i]) & (j < i));
-        const float4 v = in[i];
-        o[3 * rank] = v.x; o[3 * rank + 1] = v.y; o[3 * rank + 2] = v.z;
-    }
+    __syncwarp();
+    const long long base = (long long)blockIdx.x * T + (t & ~31);
+    const int rows = (int)min(32LL, nblocks - base);
+    for (int q = lane; q < rows * 48; q += 32) x[base * 48 + q] = stage[(q / 48) * FEAT_STRIDE + q % 48];
 }
 
 // True when the cluster fit's axis order (ascending projection on its own, arbitrarily signed
@@ -941,7 +950,8 @@ static void allow_smem(K kernel, size_t bytes, std::atomic<unsigned long long> &
 int launch_bc1_features(const EncJob *d_jobs, int njobs, long long nblocks, float *x, cudaStream_t s) {
     if (nblocks == 0) return 0;
     const int T = 64;
-    k_bc1_features<<<(unsigned)((nblocks + T - 1) / T), T, (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float)), s>>>(
+    k_bc1_features<<<(unsigned)((nblocks + T - 1) / T), T,
+                     (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float) + FEAT_STRIDE * sizeof(float)), s>>>(
         d_jobs, njobs, nblocks, x);
     return launch_status();
 }

@@ -406,10 +406,11 @@ __device__ void load_operand(uint8_t *dst, const __nv_bfloat16 *src, int rows, i
     }
 }
 
-// Bias + GELU of this thread's 256 accumulator columns into its row of the activation operand.
-__device__ __forceinline__ void hidden_epilogue(uint32_t lane_addr, const float *bias, uint8_t *act, int row) {
+// Bias + GELU of this thread's half (128 columns from c_begin) of its row's accumulator, into its
+// row of the activation operand.
+__device__ __forceinline__ void hidden_epilogue(uint32_t lane_addr, const float *bias, uint8_t *act, int row, int c_begin) {
 #pragma unroll 1
-    for (int c0 = 0; c0 < HID; c0 += 16) {
+    for (int c0 = c_begin; c0 < c_begin + HID / 2; c0 += 16) {
         float v[16];
         tmem_ld16(lane_addr + c0, v);
         uint32_t p[8];
@@ -420,7 +421,7 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t lane_addr, const float 
     }
 }
 
-__global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16 *__restrict__ w1, const __nv_bfloat16 *__restrict__ w2,
+__global__ void __launch_bounds__(256, 1) k_mlp_infer(const __nv_bfloat16 *__restrict__ w1, const __nv_bfloat16 *__restrict__ w2,
                                                        const __nv_bfloat16 *__restrict__ w3, const float *__restrict__ b1,
                                                        const float *__restrict__ b2, const float *__restrict__ b3,
                                                        const float *__restrict__ x, long long rows, float *__restrict__ y,
@@ -430,7 +431,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16 *__res
     __shared__ uint32_t tmem_base;
     uint8_t *sw1 = smem + F_W1, *sw2 = smem + F_W2, *sw3 = smem + F_W3, *act = smem + F_ACT;
     float *sb = reinterpret_cast<float *>(smem + F_BIAS);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = threadIdx.x;
+    // 8 warps: thread t owns row t % 128 (TMEM lane) and half t / 128 of its columns
+    const int warp = threadIdx.x >> 5, row = threadIdx.x & 127, half = threadIdx.x >> 7;
     if (warp == 0) tmem_alloc(&tmem_base, 512);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
@@ -444,16 +446,16 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16 *__res
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = tmem_base, lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t tmem = tmem_base, lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const uint32_t a_act = smem_u32(act), a_w1 = smem_u32(sw1), a_w2 = smem_u32(sw2), a_w3 = smem_u32(sw3);
     uint32_t phase = 0;
     bool ok = true;
     const long long tiles = (rows + BM - 1) / BM;
     for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         const long long r = tile * BM + row;
-        // X: this thread's row as bf16 (rows past the end are zero)
+        // X: this thread's half of its row as bf16 (rows past the end are zero)
 #pragma unroll
-        for (int kc = 0; kc < IN / 8; kc++) {
+        for (int kc = half * (IN / 16); kc < (half + 1) * (IN / 16); kc++) {
             float4 a = make_float4(0, 0, 0, 0), b = a;
             if (r < rows) {
                 a = *reinterpret_cast<const float4 *>(x + r * IN + kc * 8);
@@ -491,8 +493,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(const __nv_bfloat16 *__res
             tc_fence_after();
             if (!ok) break;
             if (layer < 2) {
-                hidden_epilogue(lane_addr + (layer == 0 ? 0u : (uint32_t)HID), sb + layer * HID, act, row);
-            } else {
+                hidden_epilogue(lane_addr + (layer == 0 ? 0u : (uint32_t)HID), sb + layer * HID, act, row, half * (HID / 2));
+            } else if (half == 0) {
                 float v[16];
                 tmem_ld16(lane_addr, v);
                 if (r < rows) {
@@ -681,7 +683,7 @@ int mlp_forward_device(ntg_mlp *m, const float *d_x, long long rows, float *d_y,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
     const long long tiles = (rows + BM - 1) / BM;
     const int grid = (int)std::min<long long>(tiles, std::max(1, sms));
-    k_mlp_infer<<<grid, 128, F_BYTES, s>>>(m->w1, m->w2, m->w3, m->p + OFF_B1, m->p + OFF_B2, m->b3p, d_x, rows, d_y,
+    k_mlp_infer<<<grid, 256, F_BYTES, s>>>(m->w1, m->w2, m->w3, m->p + OFF_B1, m->p + OFF_B2, m->b3p, d_x, rows, d_y,
                                            m->status);
     MLP_LAUNCH(launch_status());
     return NTG_OK;
