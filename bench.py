@@ -52,7 +52,14 @@ BATCHES = {
     "c2": (256, 0xC2, 6, 11, 1, "256 textures 64..2048 px (80% square), 50/30/20 BC1/BC3/BC5, Triangle mips, "
                                 "one CUDA graph (ntg_batch), autotuned launch shapes"),
     "c2_small": (64, 0xC2, 6, 9, 1, "64 textures 64..512 px, 50/30/20 BC1/BC3/BC5, Triangle mips, one CUDA graph"),
+    "c4": (1024, 0xC4, 7, 12, 2, "1024 textures 128..4096 px (80% square), 50/30/20 BC1/BC3/BC5, Kaiser mips, one CUDA "
+                                 "graph (ntg_batch), autotuned; BC1 through the learned endpoint proposal"),
 }
+LEARNED_BATCHES = {"c4"}
+# operating point of the learned proposal inside the batched workload (its BC1 textures are linear,
+# noise-dominated colour: the fit's ordering is set by 565 quantisation there, so the network's
+# proposal needs a tighter fallback than on the sRGB workload)
+BATCH_PROPOSAL = {"radius": 2, "margin": 0.1}
 
 # FP32 operations of one cluster-split evaluation of squish's WeightedClusterFit::Compress4
 # (src/nvtt/squish/weightedclusterfit.cpp:505-545), each multiply/add/min/max/floor/divide counted
@@ -501,6 +508,49 @@ def run_gpu_batch(args):
     e2e_value = world * texels * args.steps / e2e_s / 1e6
     same = all(np.array_equal(y.numpy(), r) for y, r in zip(h_out, ref_out))
 
+    learned_info = None
+    if name in LEARNED_BATCHES:
+        from ntg import learned
+        cfg = LEARNED
+        x, t = learned.training_set(ctx, cfg["train_blocks"], seed=0x5EED, size=cfg["train_size"])
+        net = ntg.MLP(seed=0x4E4554)
+        learned.train(net, x, t, steps=cfg["train_blocks"] // cfg["batch"], batch=cfg["batch"], lr=cfg["lr"])
+        del x, t
+        plain_out = ref_out
+        batch.set_proposal(net, radius=BATCH_PROPOSAL["radius"], margin=BATCH_PROPOSAL["margin"])
+        for _ in range(args.warmup):
+            batch.launch()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            batch.launch()
+            b.record(stream)
+        torch.cuda.synchronize()
+        learned_ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+        pst = batch.proposal_stats()
+        # per-texture RMSE of the BC1 chains, learned against plain
+        deltas = []
+        for (w, h, fmt, o, img), tex, pl in zip(specs, textures, plain_out):
+            if fmt != 1:
+                continue
+            opt = tex[3]
+            rp = learned.chain_rmse(ctx, tex[0], w, h, opt, torch.from_numpy(pl).cuda())
+            rl = learned.chain_rmse(ctx, tex[0], w, h, opt, tex[4])
+            deltas.append(100 * (rl / rp - 1) if rp > 0 else 0.0)
+        bc1_blocks = sum(ntg.chain_bytes(w, h, batch_options(o)) // 8 for (w, h, fmt, o, img) in specs if fmt == 1)
+        learned_info = {"step_ms": learned_ms, "plain_step_ms": dev_ms / args.steps,
+                        "speedup_vs_plain": (dev_ms / args.steps) / learned_ms,
+                        "value": world * texels / (learned_ms / 1000.0) / 1e6,
+                        "radius": BATCH_PROPOSAL["radius"], "margin": BATCH_PROPOSAL["margin"],
+                        "bc1_full_fit_fraction": pst["full_fit"] / max(1, bc1_blocks),
+                        "bc1_textures": len(deltas), "rmse_delta_pct_max": max(deltas) if deltas else None,
+                        "rmse_delta_pct_mean": float(np.mean(deltas)) if deltas else None,
+                        "textures_within_0p5pct": float(np.mean([d_ <= 0.5 for d_ in deltas])) if deltas else None}
+        batch.set_proposal(None)
+        net.close()
+
     if rank == 0:
         phases, blocks = batch.time_phases()
         clocks = clk.summary()
@@ -531,7 +581,7 @@ def run_gpu_batch(args):
                         "matches_device_path": same},
                 "gpu_launches": info["launches"] * args.steps,
                 "clocks": clocks, "roofline": None, "roofline_mips": roof_mips,
-                "phase_ms": phases, "phase_blocks": blocks, "dominant_phase": dominant,
+                "phase_ms": phases, "phase_blocks": blocks, "dominant_phase": dominant, "learned": learned_info,
                 "wall_s_timed": wall, "cpu_baseline": None}
         if not args.no_cpu and world == 1:
             try:

@@ -188,6 +188,12 @@ int ntg_batch_info(const ntg_batch *batch, long long *texels, long long *blocks,
  * ms[0] = every mip launch, ms[1..3] = the BC1, BC3, BC5 encoder launches (0 when absent), and
  * blocks[0..2] = the 4x4 blocks of each format. Synchronises `stream`. */
 int ntg_batch_time_phases(ntg_batch *batch, void *stream, float ms[4], long long blocks[3]);
+/* Encodes the batch's BC1 Normal-quality blocks through the learned endpoint proposal (see
+ * ntg_compress_chain_learned; mlp NULL restores the full fit) and recaptures the graph; the network
+ * must outlive the batch. ntg_batch_proposal_stats reads the last run's {kept, full fit, orderings}
+ * (synchronises). */
+int ntg_batch_set_proposal(ntg_batch *batch, struct ntg_mlp *mlp, int radius, float margin);
+int ntg_batch_proposal_stats(ntg_batch *batch, unsigned long long stats[3]);
 int ntg_batch_destroy(ntg_batch *batch);
 
 /* ---- the learned endpoint proposal's network ----

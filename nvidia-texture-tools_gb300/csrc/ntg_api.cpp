@@ -936,6 +936,11 @@ struct ntg_batch {
     long long texels = 0, blocks = 0;
     int launches = 0;
     std::string key;                      // tuning-cache key (device | batch signature)
+    // learned endpoint proposal for the BC1 Normal blocks (none: the full fit)
+    ntg_mlp *mlp = nullptr;
+    int radius = 1;
+    float margin = 0.5f;
+    uint8_t *d_learn = nullptr;           // network inputs, outputs, full-fit list, statistics
 
     ~ntg_batch() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -943,12 +948,30 @@ struct ntg_batch {
         if (d_ws) cudaFree(d_ws);
         if (d_mip) cudaFree(d_mip);
         if (d_enc) cudaFree(d_enc);
+        if (d_learn) cudaFree(d_learn);
     }
 };
 
 namespace {
 
 int enc_slot(int format) { return format == NTG_FORMAT_BC1 ? 0 : format == NTG_FORMAT_BC3 ? 1 : 2; }
+
+// Byte offsets of the learned path's buffers for n blocks: x, y, list, stats.
+struct LearnLayout {
+    size_t x, y, list, stats, bytes;
+    explicit LearnLayout(long long n) {
+        x = 0;
+        y = align256(x + (size_t)n * 48 * 4);
+        list = align256(y + (size_t)n * 16 * 4);
+        stats = align256(list + (size_t)n * 8);
+        bytes = stats + 256;
+    }
+};
+
+bool learned_group(const ntg_batch *b, const ntg_batch::Enc &e) {
+    return b->mlp && e.format == NTG_FORMAT_BC1 && e.quality == NTG_QUALITY_NORMAL;
+}
+
 
 // Plans the mip stages and encode launches of a batch for its current tuning and uploads the job
 // lists (the workspace layout does not depend on the tuning).
@@ -1021,6 +1044,8 @@ int batch_plan(ntg_batch *b) {
     NTG_CUDA(cudaMalloc((void **)&b->d_enc, ejobs.size() * sizeof(EncJob)));
     NTG_CUDA(cudaMemcpy(b->d_enc, ejobs.data(), ejobs.size() * sizeof(EncJob), cudaMemcpyHostToDevice));
     b->launches = (int)b->set_images.size() + (int)b->encodes.size();
+    for (const auto &e : b->encodes)
+        if (learned_group(b, e)) b->launches += 3;  // features, network, pruned fit, full-fit list
     for (const auto &st : b->stages) b->launches += (int)st.size();
     return NTG_OK;
 }
@@ -1037,6 +1062,21 @@ int batch_mips(ntg_batch *b, cudaStream_t s) {
 int batch_encodes(ntg_batch *b, cudaStream_t s, int only_format = -1) {
     for (const auto &e : b->encodes) {
         if (only_format >= 0 && e.format != only_format) continue;
+        if (learned_group(b, e)) {
+            const LearnLayout L(e.nblocks);
+            float *x = (float *)(b->d_learn + L.x), *y = (float *)(b->d_learn + L.y);
+            long long *list = (long long *)(b->d_learn + L.list);
+            unsigned long long *stats = (unsigned long long *)(b->d_learn + L.stats);
+            const EncJob *jobs = b->d_enc + e.first;
+            NTG_TRY(launched(launch_bc1_features(jobs, e.njobs, e.nblocks, x, s), "block features"));
+            const int r = mlp_forward_device(b->mlp, x, e.nblocks, y, s);
+            if (r) return fail(r, std::string("proposal network: ") + ntg_last_error_string());
+            NTG_CUDA(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), s));
+            NTG_TRY(launched(launch_bc1_learned(jobs, e.njobs, e.nblocks, y, b->radius, b->margin, list, stats, s),
+                             "pruned fit"));
+            NTG_TRY(launched(launch_bc1_list(jobs, e.njobs, list, stats + 1, e.nblocks, s), "full fit of the listed blocks"));
+            continue;
+        }
         NTG_TRY(launch_encode(e.format, b->d_enc + e.first, e.njobs, e.nblocks, e.quality, s, b->enc_threads[enc_slot(e.format)]));
     }
     return NTG_OK;
@@ -1348,6 +1388,36 @@ int ntg_batch_time_phases(ntg_batch *b, void *stream, float ms[4], long long blo
         if (blocks) blocks[i] = nb;
         ms[1 + i] = nb ? time_ms(s, [&] { return batch_encodes(b, s, formats[i]); }, 1, &status) : 0.0f;
         NTG_TRY(status);
+    }
+    return NTG_OK;
+}
+
+int ntg_batch_set_proposal(ntg_batch *b, ntg_mlp *mlp, int radius, float margin) {
+    g_error.clear();
+    if (!b || radius < 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    NTG_TRY(ensure_device(b->ctx));
+    b->mlp = mlp;
+    b->radius = radius;
+    b->margin = margin;
+    long long nb = 0;
+    for (const auto &e : b->encodes)
+        if (learned_group(b, e)) nb = std::max(nb, e.nblocks);
+    if (b->d_learn) { cudaFree(b->d_learn); b->d_learn = nullptr; }
+    if (mlp && nb > 0) NTG_CUDA(cudaMalloc((void **)&b->d_learn, LearnLayout(nb).bytes));
+    NTG_TRY(batch_plan(b));
+    return batch_capture(b);
+}
+
+int ntg_batch_proposal_stats(ntg_batch *b, unsigned long long stats[3]) {
+    g_error.clear();
+    if (!b || !stats) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    stats[0] = stats[1] = stats[2] = 0;
+    for (const auto &e : b->encodes) {
+        if (!learned_group(b, e)) continue;
+        NTG_CUDA(cudaDeviceSynchronize());
+        NTG_CUDA(cudaMemcpy(stats, b->d_learn + LearnLayout(e.nblocks).stats, 3 * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost));
     }
     return NTG_OK;
 }

@@ -102,6 +102,8 @@ def lib():
                                 ctypes.POINTER(_i), ctypes.POINTER(_i)]),
         "ntg_batch_destroy": (_i, [_vp]),
         "ntg_batch_time_phases": (_i, [_vp, _vp, ctypes.POINTER(_f), ctypes.POINTER(ctypes.c_longlong)]),
+        "ntg_batch_set_proposal": (_i, [_vp, _vp, _i, _f]),
+        "ntg_batch_proposal_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "ntg_mlp_create": (_i, [_i, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
         "ntg_mlp_destroy": (_i, [_vp]),
         "ntg_mlp_param_count": (_i, []),
@@ -340,6 +342,16 @@ class Batch:
         _check(lib().ntg_batch_info(self.h, ctypes.byref(tex), ctypes.byref(blk), ctypes.byref(n), shape))
         keys = ("strip", "threads", "tail_texels", "bc1_blocks_per_cta", "bc3_blocks_per_cta", "bc5_blocks_per_cta")
         return {"texels": tex.value, "blocks": blk.value, "launches": n.value, "shape": dict(zip(keys, list(shape)))}
+
+    def set_proposal(self, mlp, radius=1, margin=0.5):
+        """Learned endpoint proposal for the batch's BC1 Normal blocks (mlp None: the full fit)."""
+        self._mlp = mlp
+        _check(lib().ntg_batch_set_proposal(self.h, mlp.h if mlp is not None else None, radius, margin))
+
+    def proposal_stats(self):
+        st = (ctypes.c_ulonglong * 3)()
+        _check(lib().ntg_batch_proposal_stats(self.h, st))
+        return {"kept": st[0], "full_fit": st[1], "orderings": st[2]}
 
     def time_phases(self, stream=None):
         """{mips, bc1, bc3, bc5} ms of one run of each phase outside the graph, and blocks per format."""

@@ -125,3 +125,37 @@ def timed(fn, reps: int = 5):
         torch.cuda.synchronize()
         best = min(best, a.elapsed_time(b))
     return best
+
+
+def _main(argv=None):
+    """python -m ntg.learned infer --rows N: the fused network inference on N random blocks (an
+    untrained network), for profiling; train --blocks N --steps S: a short training run."""
+    import argparse
+    import torch
+    ap = argparse.ArgumentParser(prog="python -m ntg.learned")
+    ap.add_argument("mode", choices=["infer", "train"])
+    ap.add_argument("--rows", type=int, default=1 << 20)
+    ap.add_argument("--blocks", type=int, default=1 << 20)
+    ap.add_argument("--steps", type=int, default=128)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    net = MLP(seed=1)
+    if a.mode == "infer":
+        g = torch.Generator(device="cuda").manual_seed(1)
+        x = torch.rand((a.rows, 48), generator=g, device="cuda")
+        y = net.infer(x)
+        ms = timed(lambda: net.infer(x, out=y), reps=a.reps)
+        flop = a.rows * 2 * (48 * 256 + 256 * 256 + 256 * 16)
+        print(f"infer {a.rows} rows: {ms:.3f} ms, {flop / ms / 1e9:.1f} TFLOP/s")
+    else:
+        ctx = Context(0)
+        x, t = training_set(ctx, a.blocks, size=1024)
+        t0 = time.perf_counter()
+        losses = train(net, x, t, steps=a.steps)
+        print(f"train {a.steps} steps: {time.perf_counter() - t0:.2f} s, loss {losses[0]:.4f} -> {losses[-1]:.4f}")
+        ctx.close()
+    net.close()
+
+
+if __name__ == "__main__":
+    _main()

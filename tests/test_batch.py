@@ -163,3 +163,28 @@ def test_batch_c2_mix_matches_oracle(ctx, oracle, tmp_path, monkeypatch):
 def test_batch_rejects_bad_input(ctx):
     with pytest.raises(ntg.NtgError):
         ntg.Batch(ctx, [])
+
+
+def test_batch_learned_proposal_wide_radius_is_exact(ctx, tmp_path, monkeypatch):
+    """With the proposal's search covering every ordering, the batch's BC1 blocks through the
+    learned path equal the full fit's; clearing the proposal restores the plain graph."""
+    monkeypatch.setenv("NTG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    _, textures, refs = make_batch(ctx, MIXED, 500)
+    net = ntg.MLP(seed=4)
+    b = ntg.Batch(ctx, textures)
+    try:
+        launches = b.info()["launches"]
+        b.set_proposal(net, radius=16, margin=float("inf"))
+        assert b.info()["launches"] == launches + 3
+        for t in textures:
+            t[4].zero_()
+        b.launch()
+        for t, r in zip(textures, refs):
+            assert np.array_equal(host(t[4]), r)
+        st = b.proposal_stats()
+        assert st["kept"] > 0 and st["full_fit"] == 0
+        b.set_proposal(None)
+        assert b.info()["launches"] == launches
+    finally:
+        b.close()
+        net.close()
