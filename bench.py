@@ -626,10 +626,11 @@ def run_reference_batch(args):
     name = args.workload
     specs = batch_textures(name)
     threads = os.cpu_count() or 1
-    sample = cpu_batch_sample(name, specs, threads, 5.0)
+    budget = args.cpu_seconds
+    sample = cpu_batch_sample(name, specs, threads, budget)
     for _ in range(args.warmup - 1):
-        cpu_batch_sample(name, specs, threads, 5.0)
-    vals = [cpu_batch_sample(name, specs, threads, 5.0) for _ in range(args.steps)]
+        cpu_batch_sample(name, specs, threads, budget)
+    vals = [cpu_batch_sample(name, specs, threads, budget) for _ in range(args.steps)]
     value = statistics.mean(v["value"] for v in vals)
     why = ("the reference library itself cannot be built on this host (its source tree is absent), so its C "
            "restatement in oracle/ runs: mips on one thread as the reference filters, encode on every core")
@@ -775,6 +776,7 @@ def main():
     ap.add_argument("--impl", default="ntg", choices=["ntg", "reference"])
     ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS) + sorted(BATCHES) + ["c3"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=5.0, help="CPU work per reference-arm step on batched workloads")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")
