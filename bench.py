@@ -300,11 +300,10 @@ def run_gpu(args):
     d_out = torch.empty(ntg.chain_bytes(w, h, opt), dtype=torch.uint8, device="cuda")
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
-    levels = len(ntg.chain_levels(w, h))
-    launches_per_step = (levels - 1) + 1 + (1 if filt == 0 and am == 0 else 0)
-
     for _ in range(args.warmup):
+        n0 = ntg.launch_count()
         ctx.compress_chain(d_bgra, w, h, opt, out=d_out)
+        launches_per_step = ntg.launch_count() - n0  # the library's own count of its kernel launches
     torch.cuda.synchronize()
 
     # device-resident timing: CUDA events around each step, L2 flushed in between
@@ -383,9 +382,21 @@ def run_gpu(args):
             mip_bytes += src + dst
         hbm = peaks.get("hbm_gbs", 6800.0)
         mip_gbs = mip_bytes / (mips_ms / 1000.0) / 1e9
+        # the filter's FP32 work: a 2:1 polyphase output costs 2 rows x taps x 8 (multiply and add per
+        # channel, no FMA contraction) for the X pass plus taps x 8 for the Y pass
+        width = {0: 0.5, 1: 1.0, 2: 3.0}[filt]
+        taps = int(np.ceil(width * 2 * 2)) + 1
+        outputs = sum(a * b for a, b in lv[1:])
+        mip_ops = outputs * (3 * taps * 8) if not (filt == 0 and am == 0) else outputs * 4 * 4
+        sm_mhz_m = clocks["sm_mhz"] or 2070.0
+        fp32_peak = 152 * 128 * sm_mhz_m * 1e6
         roof_hbm = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
-                    "traffic": None, "kernel": "k_poly (fused separable Kaiser, all levels)",
-                    "algorithmic_bytes": mip_bytes, "ms": mips_ms, "peak_source": peak_src}
+                    "traffic": None, "kernel": "mip launches of the chain (k_poly2x for the 2:1 steps, k_mip_tail for the "
+                                              "levels below 64x64)",
+                    "algorithmic_bytes": mip_bytes, "ms": mips_ms, "peak_source": peak_src,
+                    "fp32_ops": mip_ops, "fp32_frac": mip_ops / (mips_ms / 1000.0) / fp32_peak,
+                    "note": "the Kaiser filter is FP32-bound before it is HBM-bound: 312 FP32 instructions per output "
+                            "without FMA contraction"}
         cpu = None
         if not args.no_cpu and world == 1:
             try:

@@ -67,6 +67,9 @@ int ntg_create(int device, ntg_context **out);
 int ntg_destroy(ntg_context *ctx);
 const char *ntg_last_error_string(void);
 int ntg_version(void);
+/* Kernel launches this process has issued through the library so far (graph replays of a batch
+ * are not counted here: ntg_batch_info reports a batch's launches). No reference counterpart. */
+unsigned long long ntg_launch_count(void);
 
 /* ---- single steps on device buffers ---- */
 

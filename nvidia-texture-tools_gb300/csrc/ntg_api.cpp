@@ -7,6 +7,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -37,9 +38,15 @@ int cuda_fail(cudaError_t e, const char *what) {
     return fail(NTG_ERROR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Kernel launches the library has issued (each successful launcher call through launched()).
+std::atomic<unsigned long long> g_launches{0};
+
 // Maps a launcher status (ntg_internal.h) to an nvtt error code with a message.
 int launched(int status, const char *what) {
-    if (status == 0) return NTG_OK;
+    if (status == 0) {
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        return NTG_OK;
+    }
     if (status >= kLaunchErrorBase) return cuda_fail((cudaError_t)(status - kLaunchErrorBase), what);
     return fail(status, what);
 }
@@ -532,6 +539,8 @@ extern "C" {
 int ntg_version(void) { return NTG_VERSION; }
 
 const char *ntg_last_error_string(void) { return g_error.c_str(); }
+
+unsigned long long ntg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int ntg_create(int device, ntg_context **out) {
     g_error.clear();

@@ -76,6 +76,7 @@ def lib():
     L = ctypes.CDLL(LIB_PATH)
     sig = {
         "ntg_version": (_i, []),
+        "ntg_launch_count": (ctypes.c_ulonglong, []),
         "ntg_last_error_string": (ctypes.c_char_p, []),
         "ntg_create": (_i, [_i, ctypes.POINTER(_vp)]),
         "ntg_destroy": (_i, [_vp]),
@@ -138,6 +139,11 @@ def _stream_ptr(stream=None):
     import torch
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
+
+
+def launch_count() -> int:
+    """Kernel launches issued through the library by this process so far (ntg_launch_count)."""
+    return int(lib().ntg_launch_count())
 
 
 def chain_levels(w: int, h: int, max_levels: int = 0):
