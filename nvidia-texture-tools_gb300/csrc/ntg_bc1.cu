@@ -42,7 +42,7 @@ __device__ __forceinline__ unsigned to565(f3 v) {
 
 __device__ __forceinline__ float round5(float x) { return (float)(int)(x * 31.0f + 0.5f) * (1.0f / 31.0f); }
 __device__ __forceinline__ float round6(float x) { return (float)(int)(x * 63.0f + 0.5f) * (1.0f / 63.0f); }
-__device__ __forceinline__ f3 round_ept(f3 v) { return mk3(round5(ic_sat(v.x)), round6(ic_sat(v.y)), round5(ic_sat(v.z))); }
+__device__ __forceinline__ f3 round_ept(f3 v) { return mk3(round5(snap_clamp(v.x)), round6(snap_clamp(v.y)), round5(snap_clamp(v.z))); }
 __device__ __forceinline__ bool is_black(f3 c) { return c.x < 1.0f / 8 && c.y < 1.0f / 8 && c.z < 1.0f / 8; }
 __device__ __forceinline__ f3 xyz(float4 v) { return mk3(v.x, v.y, v.z); }
 

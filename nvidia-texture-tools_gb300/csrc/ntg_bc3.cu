@@ -189,7 +189,16 @@ __device__ __forceinline__ int float_to_int(float a, int limit) {
 // sums run in the same order; dead slots sort last behind +inf keys. Everything stays in
 // registers with static indices; `wp` is this thread's [17][thread] float4 staging for the
 // split loops, which index points by running counts.
-template <typename Arr>
+// Min(one, Max(zero, v)) then Floor(grid * v + half) * gridrcp
+// (src/nvtt/squish/weightedclusterfit.cpp:516-519) per channel, grid (31, 63, 31); the clamp is
+// snap_clamp, which gives the same snapped value as squish's Max/Min for every input.
+__device__ __forceinline__ f3 snap565(f3 v) {
+    const float x = snap_clamp(v.x), y = snap_clamp(v.y), z = snap_clamp(v.z);
+    return mk3(floorf(31.0f * x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * y + 0.5f) * (1.0f / 63.0f),
+               floorf(31.0f * z + 0.5f) * (1.0f / 31.0f));
+}
+
+template <bool UNIT_METRIC, typename Arr>
 __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f3 metric, Arr wp) {
     float X[16], Y[16], Z[16], W[16];
     uint32_t live = 0;        // bit i: slot i holds a point
@@ -284,7 +293,7 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
     // The split search keeps only the best error and its cluster sizes; the endpoints of the
     // winner are recomputed afterwards with the same sequence of operations.
     float besterr = FLT_MAX;
-    int b0 = 0, b1 = 0, b2 = 0;
+    int best = 0;  // winning split as c0 << 10 | c1 << 5 | c2
     f3 x0 = mk3(0, 0, 0);
     float w0 = 0.0f;
     for (int c0 = 0; c0 <= count; c0++) {
@@ -298,6 +307,7 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
             const float a2p = t01 + w1 * (4.0f / 9.0f);
             const float w1n = w1 * (1.0f / 9.0f);
             const f3 axp = x0 + (x1 * (2.0f / 3.0f));
+            int key = (c0 << 10) | (c1 << 5);
             for (int c2 = 0; c2 <= count - c0 - c1; c2++) {
                 const float w3 = wr - w2;
                 const float a2 = a2p + w2 * (1.0f / 9.0f);
@@ -308,14 +318,14 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
                 const f3 bx = xsum - ax;
                 f3 a = ((ax * b2s) - (bx * ab)) * f;
                 f3 b = ((bx * a2) - (ax * ab)) * f;
-                a = mk3(sq_min(1.0f, sq_max(0.0f, a.x)), sq_min(1.0f, sq_max(0.0f, a.y)), sq_min(1.0f, sq_max(0.0f, a.z)));
-                b = mk3(sq_min(1.0f, sq_max(0.0f, b.x)), sq_min(1.0f, sq_max(0.0f, b.y)), sq_min(1.0f, sq_max(0.0f, b.z)));
-                a = mk3(floorf(31.0f * a.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * a.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * a.z + 0.5f) * (1.0f / 31.0f));
-                b = mk3(floorf(31.0f * b.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * b.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * b.z + 0.5f) * (1.0f / 31.0f));
+                a = snap565(a);
+                b = snap565(b);
                 const f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
                 const f3 e1 = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
-                const float err = dot(e1, msq);
-                if (err < besterr) { besterr = err; b0 = c0; b1 = c1; b2 = c2; }
+                // x * 1.0f is x exactly: the default unit metric drops the three multiplies
+                const float err = UNIT_METRIC ? (e1.x + e1.y) + e1.z : dot(e1, msq);
+                if (err < besterr) { besterr = err; best = key; }
+                key++;
                 const float4 q = wp[c0 + c1 + c2];
                 x2 = x2 + mk3(q.x, q.y, q.z);
                 w2 += q.w;
@@ -329,6 +339,7 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
         w0 += q.w;
     }
     if (!(besterr < FLT_MAX)) return make_uint2(0, 0);
+    const int b0 = best >> 10, b1 = (best >> 5) & 31, b2 = best & 31;
     f3 bs, be;
     {
         // the running sums of the winning split, accumulated exactly as the search did
@@ -346,10 +357,8 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
         const f3 bx = xsum - ax;
         f3 a = ((ax * b2s) - (bx * ab)) * f;
         f3 b = ((bx * a2) - (ax * ab)) * f;
-        a = mk3(sq_min(1.0f, sq_max(0.0f, a.x)), sq_min(1.0f, sq_max(0.0f, a.y)), sq_min(1.0f, sq_max(0.0f, a.z)));
-        b = mk3(sq_min(1.0f, sq_max(0.0f, b.x)), sq_min(1.0f, sq_max(0.0f, b.y)), sq_min(1.0f, sq_max(0.0f, b.z)));
-        bs = mk3(floorf(31.0f * a.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * a.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * a.z + 0.5f) * (1.0f / 31.0f));
-        be = mk3(floorf(31.0f * b.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * b.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * b.z + 0.5f) * (1.0f / 31.0f));
+        bs = snap565(a);
+        be = snap565(b);
     }
     // cluster sizes -> point (slot) indices -> texel indices (ColourSet::RemapIndices)
     uint32_t slot_idx = 0;
@@ -494,8 +503,14 @@ __device__ __forceinline__ void load_block(const EncJob &J, int x, int y, uint32
     }
 }
 
+// Resident CTAs of 128 threads per SM the register allocation is sized for: 5 (96 registers, 252 B
+// of spill stores) measured 2.6% faster than 4 (127 registers) and 1.9% faster than 6 on C1.
+#ifndef NTG_BC3_MIN_CTAS
+#define NTG_BC3_MIN_CTAS 5
+#endif
+
 template <int QUALITY>
-__global__ void __launch_bounds__(128) k_bc3(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
+__global__ void __launch_bounds__(128, NTG_BC3_MIN_CTAS) k_bc3(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
     extern __shared__ float4 smem[];
     const int T = blockDim.x, t = threadIdx.x;
     const long long gblk = (long long)blockIdx.x * T + t;
@@ -518,7 +533,11 @@ __global__ void __launch_bounds__(128) k_bc3(const EncJob *__restrict__ jobs, in
     else if (QUALITY == 0) col = quick_dxt1(px);
     else {
         struct { float4 *b; int s; __device__ float4 &operator[](int k) const { return b[k * s]; } } wp{smem + t, T};
-        col = squish_compress4(px, J.alpha_mode == 1, mk3(J.cw[0], J.cw[1], J.cw[2]), wp);
+        const f3 metric = mk3(J.cw[0], J.cw[1], J.cw[2]);
+        if (metric.x == 1.0f && metric.y == 1.0f && metric.z == 1.0f)
+            col = squish_compress4<true>(px, J.alpha_mode == 1, metric, wp);
+        else
+            col = squish_compress4<false>(px, J.alpha_mode == 1, metric, wp);
     }
     *reinterpret_cast<uint2 *>(dst + 8) = col;
 }

@@ -22,6 +22,11 @@ __device__ __forceinline__ float ic_clamp(float x, float a, float b) { return ic
 __device__ __forceinline__ float ic_sat(float x) { return ic_clamp(x, 0.0f, 1.0f); }
 __device__ __forceinline__ float sq_max(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float sq_min(float a, float b) { return (b < a) ? b : a; }
+// Clamp to [0, 1] ahead of a grid snap (k * x + 0.5 truncated or floored). Both reference forms,
+// ic_sat(x) and sq_min(1, sq_max(0, x)), turn a NaN into 0 as fmaxf does, and agree with
+// fminf(fmaxf(x, 0), 1) everywhere else except in the sign of a zero result, which the snap
+// loses (k * -0 + 0.5 = 0.5). Only valid where the clamped value feeds such a snap.
+__device__ __forceinline__ float snap_clamp(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
 
 struct f3 { float x, y, z; };
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
