@@ -65,6 +65,7 @@ static int g_three_total[16];
 static float g_mid5[32], g_mid6[64];
 static uint8_t g_icbc_match5[256][2], g_icbc_match6[256][2];
 static uint8_t g_opt_match5[256][2], g_opt_match6[256][2];
+static uint8_t g_opt_alpha5[256][2], g_opt_alpha6[256][2];
 static pthread_once_t g_once = PTHREAD_ONCE_INIT;
 
 /* Cluster orderings of icbc init_cluster_tables (src/nvtt/icbc.h:1906-1975). For every point
@@ -124,19 +125,21 @@ static void init_icbc_single(void) {
     }
 }
 
-/* OMatch5/OMatch6 of OptimalCompress (src/nvtt/SingleColorLookup.cpp:32-89): one-third
- * interpolation error x100 plus 3 x endpoint distance. */
+/* OMatch5/OMatch6 and OMatchAlpha5/OMatchAlpha6 of OptimalCompress
+ * (src/nvtt/SingleColorLookup.cpp:32-89): interpolation error x100 (the one-third point, or the
+ * midpoint for the three-colour tables) plus 3 x endpoint distance. */
 static void init_opt_single(void) {
-    for (int pass = 0; pass < 2; pass++) {
-        const int size = pass == 0 ? 32 : 64;
-        uint8_t (*tab)[2] = pass == 0 ? g_opt_match5 : g_opt_match6;
+    for (int pass = 0; pass < 4; pass++) {
+        const int size = (pass & 1) == 0 ? 32 : 64;
+        const int alpha = pass >= 2;
+        uint8_t (*tab)[2] = pass == 0 ? g_opt_match5 : pass == 1 ? g_opt_match6 : pass == 2 ? g_opt_alpha5 : g_opt_alpha6;
         for (int i = 0; i < 256; i++) {
             int best = 256 * 100;
             for (int mn = 0; mn < size; mn++)
                 for (int mx = 0; mx < size; mx++) {
-                    int lo = pass == 0 ? ex5(mn) : ex6(mn);
-                    int hi = pass == 0 ? ex5(mx) : ex6(mx);
-                    int err = abs((hi * 2 + lo) / 3 - i) * 100 + abs(mx - mn) * 3;
+                    int lo = (pass & 1) == 0 ? ex5(mn) : ex6(mn);
+                    int hi = (pass & 1) == 0 ? ex5(mx) : ex6(mx);
+                    int err = (alpha ? abs((hi + lo) / 2 - i) : abs((hi * 2 + lo) / 3 - i)) * 100 + abs(mx - mn) * 3;
                     if (err < best) { tab[i][0] = (uint8_t)mx; tab[i][1] = (uint8_t)mn; best = err; }
                 }
         }
@@ -835,8 +838,20 @@ void ora_dxt1_single_color(int r, int g, int b, uint8_t *out8) {
     put16(out8, c0); put16(out8 + 2, c1); put32(out8 + 4, idx);
 }
 
+/* OptimalCompress::compressDXT1a(Color32, alphaMask) (src/nvtt/OptimalCompressDXT.cpp:271-292):
+ * without transparent texels the four-colour block above; otherwise the three-colour midpoint
+ * tables, endpoints ordered col0 <= col1, index 2 everywhere and 3 on the transparent texels. */
+void ora_dxt1a_single_color(int r, int g, int b, uint32_t alpha_mask, uint8_t *out8) {
+    ensure_init();
+    if (alpha_mask == 0) { ora_dxt1_single_color(r, g, b, out8); return; }
+    unsigned c0 = ((unsigned)g_opt_alpha5[r][0] << 11) | ((unsigned)g_opt_alpha6[g][0] << 5) | g_opt_alpha5[b][0];
+    unsigned c1 = ((unsigned)g_opt_alpha5[r][1] << 11) | ((unsigned)g_opt_alpha6[g][1] << 5) | g_opt_alpha5[b][1];
+    if (c0 > c1) { unsigned t = c0; c0 = c1; c1 = t; }
+    put16(out8, c0); put16(out8 + 2, c1); put32(out8 + 4, 0xaaaaaaaau | alpha_mask);
+}
+
 /* ------------------------------------------------------------------------------------------ */
-/* squish weighted cluster fit (BC3 colour), scalar build                                       */
+/* squish weighted cluster fit (BC3 colour, BC1a), scalar build                                 */
 
 /* ColourSet (src/nvtt/squish/colourset.cpp:35-139, no minimal set), WeightedClusterFit::
  * SetColourSet (src/nvtt/squish/weightedclusterfit.cpp:39-105), ComputeWeightedCovariance /
@@ -852,32 +867,47 @@ static int float_to_565(v3 c) {
     return (float_to_int(31.0f * c.x, 31) << 11) | (float_to_int(63.0f * c.y, 63) << 5) | float_to_int(31.0f * c.z, 31);
 }
 
-static void squish_compress4(const uint8_t *bgra, int weight_by_alpha, v3 metric, uint8_t *out8) {
+/* The colour set and the sorted, weighted points of one block. */
+typedef struct {
+    int count, transparent;
+    int remap[16];          /* point of each texel; -1 = transparent (DXT1 mode) */
+    int order[16];          /* point of each sorted position */
+    v3 wp[17];              /* weighted points in axis order (the tail entries are read, never used) */
+    float ww[17];
+    v3 xsum, msq;
+    float wsum;
+} squish_set;
+
+static void squish_prepare(const uint8_t *bgra, int weight_by_alpha, int dxt1, v3 metric, squish_set *S) {
     /* ColourSet with the header's default createMinimalSet = true
      * (src/nvtt/squish/colourset.h:40, src/nvtt/squish/colourset.cpp:44-90): texels with equal RGB
-     * bytes share one point whose weight is the sum of theirs, points in first-occurrence order. */
+     * bytes share one point whose weight is the sum of theirs, points in first-occurrence order.
+     * In DXT1 mode a texel with alpha 0 is left out (remap -1) and never matched. */
     v3 pts[16];
     float wts[16];
-    int remap[16];
     int count = 0;
+    S->transparent = 0;
     for (int i = 0; i < 16; i++) {
+        if (dxt1 && bgra[4 * i + 3] == 0) { S->remap[i] = -1; S->transparent = 1; continue; }
         const float wi = weight_by_alpha ? (float)(bgra[4 * i + 3] + 1) / 256.0f : 1.0f;
         for (int j = 0;; ++j) {
             if (j == i) {
                 pts[count] = mk3((float)bgra[4 * i + 2] / 255.0f, (float)bgra[4 * i + 1] / 255.0f, (float)bgra[4 * i + 0] / 255.0f);
                 wts[count] = wi;
-                remap[i] = count;
+                S->remap[i] = count;
                 ++count;
                 break;
             }
-            if (bgra[4 * i] == bgra[4 * j] && bgra[4 * i + 1] == bgra[4 * j + 1] && bgra[4 * i + 2] == bgra[4 * j + 2]) {
-                const int index = remap[j];
+            if (bgra[4 * i] == bgra[4 * j] && bgra[4 * i + 1] == bgra[4 * j + 1] && bgra[4 * i + 2] == bgra[4 * j + 2] &&
+                (bgra[4 * j + 3] != 0 || !dxt1)) {
+                const int index = S->remap[j];
                 wts[index] += wi;
-                remap[i] = index;
+                S->remap[i] = index;
                 break;
             }
         }
     }
+    S->count = count;
     /* weighted covariance */
     float total = 0.0f;
     v3 cen = mk3(0, 0, 0);
@@ -904,31 +934,41 @@ static void squish_compress4(const uint8_t *bgra, int weight_by_alpha, v3 metric
         v = mk3(x * iv, y * iv, z * iv);
     }
     /* order along the axis (stable) */
-    int order[16];
     float dps[16];
-    for (int i = 0; i < count; i++) { dps[i] = dot3(pts[i], v); order[i] = i; }
+    for (int i = 0; i < count; i++) { dps[i] = dot3(pts[i], v); S->order[i] = i; }
     for (int i = 0; i < count; i++)
         for (int j = i; j > 0 && dps[j] < dps[j - 1]; --j) {
             float t = dps[j]; dps[j] = dps[j - 1]; dps[j - 1] = t;
-            int o = order[j]; order[j] = order[j - 1]; order[j - 1] = o;
+            int o = S->order[j]; S->order[j] = S->order[j - 1]; S->order[j - 1] = o;
         }
-    v3 wp[17];
-    float ww[17];
-    v3 xsum = mk3(0, 0, 0);
-    float wsum = 0.0f;
+    S->xsum = mk3(0, 0, 0);
+    S->wsum = 0.0f;
     for (int i = 0; i < count; i++) {
-        int p = order[i];
-        wp[i] = scl3(pts[p], wts[p]);
-        xsum = add3(xsum, wp[i]);
-        ww[i] = wts[p];
-        wsum += ww[i];
+        int p = S->order[i];
+        S->wp[i] = scl3(pts[p], wts[p]);
+        S->xsum = add3(S->xsum, S->wp[i]);
+        S->ww[i] = wts[p];
+        S->wsum += S->ww[i];
     }
-    for (int i = count; i < 17; i++) { wp[i] = mk3(0, 0, 0); ww[i] = 0.0f; } /* read by loop tails, never used */
-    v3 msq = mul3(metric, metric);
+    for (int i = count; i < 17; i++) { S->wp[i] = mk3(0, 0, 0); S->ww[i] = 0.0f; }
+    S->msq = mul3(metric, metric);
+}
 
+/* Min(one, Max(zero, v)) then Floor(grid * v + half) * gridrcp, grid (31, 63, 31)
+ * (src/nvtt/squish/weightedclusterfit.cpp:516-519). */
+static v3 squish_snap(v3 a) {
+    a = mk3(sq_min(1.0f, sq_max(0.0f, a.x)), sq_min(1.0f, sq_max(0.0f, a.y)), sq_min(1.0f, sq_max(0.0f, a.z)));
+    return mk3(floorf(31.0f * a.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * a.y + 0.5f) * (1.0f / 63.0f),
+               floorf(31.0f * a.z + 0.5f) * (1.0f / 31.0f));
+}
+
+/* Compress4's split search (scalar, src/nvtt/squish/weightedclusterfit.cpp:476-545): the first
+ * strict minimum; the winner's endpoints and cluster sizes. */
+static float squish_search4(const squish_set *S, v3 *bs, v3 *be, int *b0, int *b1, int *b2) {
+    const int count = S->count;
     float besterr = FLT_MAX;
-    v3 bs = mk3(0, 0, 0), be = mk3(0, 0, 0);
-    int b0 = 0, b1 = 0, b2 = 0;
+    *bs = mk3(0, 0, 0); *be = mk3(0, 0, 0);
+    *b0 = *b1 = *b2 = 0;
     v3 x0 = mk3(0, 0, 0);
     float w0 = 0.0f;
     for (int c0 = 0; c0 <= count; c0++) {
@@ -938,47 +978,164 @@ static void squish_compress4(const uint8_t *bgra, int weight_by_alpha, v3 metric
             v3 x2 = mk3(0, 0, 0);
             float w2 = 0.0f;
             for (int c2 = 0; c2 <= count - c0 - c1; c2++) {
-                float w3 = wsum - w0 - w1 - w2;
+                float w3 = S->wsum - w0 - w1 - w2;
                 float a2 = w0 + w1 * (4.0f / 9.0f) + w2 * (1.0f / 9.0f);
                 float b2s = w3 + w2 * (4.0f / 9.0f) + w1 * (1.0f / 9.0f);
                 float ab = (w1 + w2) * (2.0f / 9.0f);
                 float f = 1.0f / (a2 * b2s - ab * ab);
                 v3 ax = add3(add3(x0, scl3(x1, 2.0f / 3.0f)), scl3(x2, 1.0f / 3.0f));
-                v3 bx = sub3(xsum, ax);
-                v3 a = scl3(sub3(scl3(ax, b2s), scl3(bx, ab)), f);
-                v3 b = scl3(sub3(scl3(bx, a2), scl3(ax, ab)), f);
-                a = mk3(sq_min(1.0f, sq_max(0.0f, a.x)), sq_min(1.0f, sq_max(0.0f, a.y)), sq_min(1.0f, sq_max(0.0f, a.z)));
-                b = mk3(sq_min(1.0f, sq_max(0.0f, b.x)), sq_min(1.0f, sq_max(0.0f, b.y)), sq_min(1.0f, sq_max(0.0f, b.z)));
-                a = mk3(floorf(31.0f * a.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * a.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * a.z + 0.5f) * (1.0f / 31.0f));
-                b = mk3(floorf(31.0f * b.x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * b.y + 0.5f) * (1.0f / 63.0f), floorf(31.0f * b.z + 0.5f) * (1.0f / 31.0f));
+                v3 bx = sub3(S->xsum, ax);
+                v3 a = squish_snap(scl3(sub3(scl3(ax, b2s), scl3(bx, ab)), f));
+                v3 b = squish_snap(scl3(sub3(scl3(bx, a2), scl3(ax, ab)), f));
                 v3 t = sub3(sub3(scl3(mul3(a, b), ab), mul3(a, ax)), mul3(b, bx));
                 v3 e1 = add3(add3(scl3(mul3(a, a), a2), scl3(mul3(b, b), b2s)), scl3(t, 2.0f));
-                float err = dot3(e1, msq);
-                if (err < besterr) { besterr = err; bs = a; be = b; b0 = c0; b1 = c1; b2 = c2; }
-                x2 = add3(x2, wp[c0 + c1 + c2]);
-                w2 += ww[c0 + c1 + c2];
+                float err = dot3(e1, S->msq);
+                if (err < besterr) { besterr = err; *bs = a; *be = b; *b0 = c0; *b1 = c1; *b2 = c2; }
+                x2 = add3(x2, S->wp[c0 + c1 + c2]);
+                w2 += S->ww[c0 + c1 + c2];
             }
-            x1 = add3(x1, wp[c0 + c1]);
-            w1 += ww[c0 + c1];
+            x1 = add3(x1, S->wp[c0 + c1]);
+            w1 += S->ww[c0 + c1];
         }
-        x0 = add3(x0, wp[c0]);
-        w0 += ww[c0];
+        x0 = add3(x0, S->wp[c0]);
+        w0 += S->ww[c0];
     }
-    uint8_t point_idx[16], idx[16];
-    if (!(besterr < FLT_MAX)) { memset(out8, 0, 8); return; }
-    /* cluster sizes -> point indices -> texel indices (ColourSet::RemapIndices) */
-    for (int i = 0; i < count; i++)
-        point_idx[order[i]] = i < b0 ? 0 : (i < b0 + b1 ? 2 : (i < b0 + b1 + b2 ? 3 : 1));
-    for (int i = 0; i < 16; i++) idx[i] = point_idx[remap[i]];
-    int a = float_to_565(bs), b = float_to_565(be);
-    uint8_t rem[16];
-    if (a < b) { int t = a; a = b; b = t; for (int i = 0; i < 16; i++) rem[i] = (idx[i] ^ 1) & 3; }
-    else if (a == b) { memset(rem, 0, 16); }
-    else memcpy(rem, idx, 16);
+    return besterr;
+}
+
+/* Compress3's split search (scalar, src/nvtt/squish/weightedclusterfit.cpp:372-431). */
+static float squish_search3(const squish_set *S, v3 *bs, v3 *be, int *b0, int *b1) {
+    const int count = S->count;
+    float besterr = FLT_MAX;
+    *bs = mk3(0, 0, 0); *be = mk3(0, 0, 0);
+    *b0 = *b1 = 0;
+    v3 x0 = mk3(0, 0, 0);
+    float w0 = 0.0f;
+    for (int c0 = 0; c0 <= count; c0++) {
+        v3 x1 = mk3(0, 0, 0);
+        float w1 = 0.0f;
+        for (int c1 = 0; c1 <= count - c0; c1++) {
+            float w2 = S->wsum - w0 - w1;
+            float a2 = w0 + w1 * 0.25f;
+            float b2s = w2 + w1 * 0.25f;
+            float ab = w1 * 0.25f;
+            float f = 1.0f / (a2 * b2s - ab * ab);
+            v3 ax = add3(x0, scl3(x1, 0.5f));
+            v3 bx = sub3(S->xsum, ax);
+            v3 a = squish_snap(scl3(sub3(scl3(ax, b2s), scl3(bx, ab)), f));
+            v3 b = squish_snap(scl3(sub3(scl3(bx, a2), scl3(ax, ab)), f));
+            v3 t = sub3(sub3(scl3(mul3(a, b), ab), mul3(a, ax)), mul3(b, bx));
+            v3 e1 = add3(add3(scl3(mul3(a, a), a2), scl3(mul3(b, b), b2s)), scl3(t, 2.0f));
+            float err = dot3(e1, S->msq);
+            if (err < besterr) { besterr = err; *bs = a; *be = b; *b0 = c0; *b1 = c1; }
+            x1 = add3(x1, S->wp[c0 + c1]);
+            w1 += S->ww[c0 + c1];
+        }
+        x0 = add3(x0, S->wp[c0]);
+        w0 += S->ww[c0];
+    }
+    return besterr;
+}
+
+/* Cluster of each sorted position -> point indices -> texel indices (ColourSet::RemapIndices,
+ * src/nvtt/squish/colourset.cpp:141-151: transparent texels take index 3). */
+static void squish_texel_indices(const squish_set *S, int b0, int b1, int b2, int three, uint8_t idx[16]) {
+    uint8_t point_idx[16];
+    for (int i = 0; i < S->count; i++)
+        point_idx[S->order[i]] = three ? (i < b0 ? 0 : (i < b0 + b1 ? 2 : 1))
+                                       : (i < b0 ? 0 : (i < b0 + b1 ? 2 : (i < b0 + b1 + b2 ? 3 : 1)));
+    for (int i = 0; i < 16; i++) idx[i] = S->remap[i] < 0 ? 3 : point_idx[S->remap[i]];
+}
+
+static void write_colour_block(int a, int b, const uint8_t rem[16], uint8_t *out8) {
     out8[0] = (uint8_t)(a & 0xff); out8[1] = (uint8_t)(a >> 8);
     out8[2] = (uint8_t)(b & 0xff); out8[3] = (uint8_t)(b >> 8);
     for (int i = 0; i < 4; i++)
         out8[4 + i] = (uint8_t)(rem[4 * i] | (rem[4 * i + 1] << 2) | (rem[4 * i + 2] << 4) | (rem[4 * i + 3] << 6));
+}
+
+/* WriteColourBlock4 (src/nvtt/squish/colourblock.cpp:108-139). */
+static void write_colour_block4(v3 s, v3 e, const uint8_t idx[16], uint8_t *out8) {
+    int a = float_to_565(s), b = float_to_565(e);
+    uint8_t rem[16];
+    if (a < b) { int t = a; a = b; b = t; for (int i = 0; i < 16; i++) rem[i] = (idx[i] ^ 1) & 3; }
+    else if (a == b) { memset(rem, 0, 16); }
+    else memcpy(rem, idx, 16);
+    write_colour_block(a, b, rem, out8);
+}
+
+/* WriteColourBlock3 (src/nvtt/squish/colourblock.cpp:75-106). */
+static void write_colour_block3(v3 s, v3 e, const uint8_t idx[16], uint8_t *out8) {
+    int a = float_to_565(s), b = float_to_565(e);
+    uint8_t rem[16];
+    if (a <= b) memcpy(rem, idx, 16);
+    else {
+        int t = a; a = b; b = t;
+        for (int i = 0; i < 16; i++) rem[i] = idx[i] == 0 ? 1 : (idx[i] == 1 ? 0 : idx[i]);
+    }
+    write_colour_block(a, b, rem, out8);
+}
+
+static void squish_compress4(const uint8_t *bgra, int weight_by_alpha, v3 metric, uint8_t *out8) {
+    squish_set S;
+    squish_prepare(bgra, weight_by_alpha, 0, metric, &S);
+    v3 bs, be;
+    int b0, b1, b2;
+    const float besterr = squish_search4(&S, &bs, &be, &b0, &b1, &b2);
+    if (!(besterr < FLT_MAX)) { memset(out8, 0, 8); return; }
+    uint8_t idx[16];
+    squish_texel_indices(&S, b0, b1, b2, 0, idx);
+    write_colour_block4(bs, be, idx, out8);
+}
+
+/* WeightedClusterFit with kDxt1 (ColourFit::Compress, src/nvtt/squish/colourfit.cpp:39-55):
+ * Compress3, then Compress4 unless a texel is transparent; a mode replaces the block only with a
+ * strictly smaller error. */
+static void squish_compress_dxt1(const uint8_t *bgra, int weight_by_alpha, v3 metric, uint8_t *out8) {
+    squish_set S;
+    squish_prepare(bgra, weight_by_alpha, 1, metric, &S);
+    float best = FLT_MAX;
+    v3 bs, be;
+    int b0, b1, b2;
+    uint8_t idx[16];
+    memset(out8, 0, 8);
+    const float e3 = squish_search3(&S, &bs, &be, &b0, &b1);
+    if (e3 < best) {
+        squish_texel_indices(&S, b0, b1, 0, 1, idx);
+        write_colour_block3(bs, be, idx, out8);
+        best = e3;
+    }
+    if (!S.transparent) {
+        const float e4 = squish_search4(&S, &bs, &be, &b0, &b1, &b2);
+        if (e4 < best) {
+            squish_texel_indices(&S, b0, b1, b2, 0, idx);
+            write_colour_block4(bs, be, idx, out8);
+        }
+    }
+}
+
+/* CompressorDXT1a::compressBlock (src/nvtt/CompressorDX9.cpp:83-111) for Normal quality and
+ * above: the single-colour test looks at RGB only (ColorBlock::isSingleColor,
+ * src/nvimage/ColorBlock.cpp:136-149). */
+void ora_bc1a_block(const uint8_t *bgra, int alpha_mode, const float *cw3, uint8_t *out8) {
+    ensure_init();
+    uint32_t mask = 0;
+    for (int i = 0; i < 16; i++)
+        if (bgra[4 * i + 3] == 0) mask |= 3u << (2 * i);
+    int single = 1;
+    for (int i = 1; i < 16; i++)
+        if (bgra[4 * i] != bgra[0] || bgra[4 * i + 1] != bgra[1] || bgra[4 * i + 2] != bgra[2]) single = 0;
+    if (single) ora_dxt1a_single_color(bgra[2], bgra[1], bgra[0], mask, out8);
+    else squish_compress_dxt1(bgra, alpha_mode == ORA_ALPHA_TRANSPARENCY, mk3(cw3[0], cw3[1], cw3[2]), out8);
+}
+
+/* FastCompressorBC4 / ProductionCompressorBC4 (src/nvtt/CompressorDX10.cpp:40-72): the red
+ * channel as an interpolated-alpha block; Fastest and Normal use the quick fit. */
+void ora_bc4_block(const uint8_t *bgra, int quality, uint8_t *out8) {
+    uint8_t r[16];
+    for (int i = 0; i < 16; i++) r[i] = bgra[4 * i + 2];
+    if (quality == ORA_Q_FASTEST || quality == ORA_Q_NORMAL) ora_dxt5a_quick(r, out8);
+    else ora_dxt5a_optimal(r, out8);
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -1203,6 +1360,32 @@ void ora_bc5_image(const float *rgba, int w, int h, int quality, uint8_t *out, i
     ensure_init();
     img_ctx c = {rgba, NULL, w, h, (w + 3) / 4, 0, quality, 0, {1, 1, 1}, out};
     run_jobs(bc5_task, &c, c.bw * ((h + 3) / 4), threads);
+}
+
+static void bc1a_task(void *p, int i) {
+    img_ctx *c = (img_ctx *)p;
+    uint8_t blk[64];
+    ora_colorblock_gather(c->rgba, c->w, c->h, 4 * (i % c->bw), 4 * (i / c->bw), blk);
+    ora_bc1a_block(blk, c->alpha_mode, c->cw, c->out + 8 * (size_t)i);
+}
+
+void ora_bc1a_image(const float *rgba, int w, int h, int alpha_mode, const float *cw3, uint8_t *out, int threads) {
+    ensure_init();
+    img_ctx c = {rgba, NULL, w, h, (w + 3) / 4, alpha_mode, 1, 0, {cw3[0], cw3[1], cw3[2]}, out};
+    run_jobs(bc1a_task, &c, c.bw * ((h + 3) / 4), threads);
+}
+
+static void bc4_task(void *p, int i) {
+    img_ctx *c = (img_ctx *)p;
+    uint8_t blk[64];
+    ora_colorblock_gather(c->rgba, c->w, c->h, 4 * (i % c->bw), 4 * (i / c->bw), blk);
+    ora_bc4_block(blk, c->quality, c->out + 8 * (size_t)i);
+}
+
+void ora_bc4_image(const float *rgba, int w, int h, int quality, uint8_t *out, int threads) {
+    ensure_init();
+    img_ctx c = {rgba, NULL, w, h, (w + 3) / 4, 0, quality, 0, {1, 1, 1}, out};
+    run_jobs(bc4_task, &c, c.bw * ((h + 3) / 4), threads);
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -1578,12 +1761,17 @@ static void decode_alpha(const uint8_t *b, uint8_t out[16]) {
 int ora_decode(int format, const uint8_t *blocks, int w, int h, float *rgba) {
     const int bw = (w + 3) / 4, bh = (h + 3) / 4;
     const size_t n = (size_t)w * h;
-    const int bs = format == ORA_FMT_BC1 ? 8 : 16;
+    const int bs = format == ORA_FMT_BC1 || format == ORA_FMT_BC1A || format == ORA_FMT_BC4 ? 8 : 16;
     for (int by = 0; by < bh; by++)
         for (int bx = 0; bx < bw; bx++) {
             const uint8_t *b = blocks + (size_t)(by * bw + bx) * bs;
             uint8_t px[16][4];
-            if (format == ORA_FMT_BC1) decode_bc1(b, px);
+            if (format == ORA_FMT_BC1 || format == ORA_FMT_BC1A) decode_bc1(b, px);
+            else if (format == ORA_FMT_BC4) {  /* BlockATI1::decodeBlock (src/nvimage/BlockDXT.cpp:513-526) */
+                uint8_t x[16];
+                decode_alpha(b, x);
+                for (int i = 0; i < 16; i++) { px[i][0] = px[i][1] = px[i][2] = x[i]; px[i][3] = 255; }
+            }
             else if (format == ORA_FMT_BC3) {
                 uint8_t a[16];
                 decode_bc1(b + 8, px);

@@ -21,7 +21,7 @@ extern "C" {
 #endif
 
 /* nvtt enums, numerically as the reference declares them. */
-enum { ORA_FMT_BC1 = 1, ORA_FMT_BC3 = 4, ORA_FMT_BC5 = 7 };
+enum { ORA_FMT_BC1 = 1, ORA_FMT_BC1A = 2, ORA_FMT_BC3 = 4, ORA_FMT_BC4 = 6, ORA_FMT_BC5 = 7 };
 enum { ORA_Q_FASTEST = 0, ORA_Q_NORMAL = 1, ORA_Q_PRODUCTION = 2, ORA_Q_HIGHEST = 3 };
 enum { ORA_WRAP_CLAMP = 0, ORA_WRAP_REPEAT = 1, ORA_WRAP_MIRROR = 2 };
 enum { ORA_FILTER_BOX = 0, ORA_FILTER_TRIANGLE = 1, ORA_FILTER_KAISER = 2 };
@@ -48,6 +48,12 @@ void ora_bc5_block(const uint8_t *bgra64, int quality, uint8_t *out16);
 void ora_bc3_image(const float *rgba, int w, int h, int alpha_mode, int quality, const float *cw3,
                    uint8_t *out, int threads);
 void ora_bc5_image(const float *rgba, int w, int h, int quality, uint8_t *out, int threads);
+/* BC1a (Normal quality and above) and BC4. */
+void ora_dxt1a_single_color(int r, int g, int b, uint32_t alpha_mask, uint8_t *out8);
+void ora_bc1a_block(const uint8_t *bgra64, int alpha_mode, const float *cw3, uint8_t *out8);
+void ora_bc4_block(const uint8_t *bgra64, int quality, uint8_t *out8);
+void ora_bc1a_image(const float *rgba, int w, int h, int alpha_mode, const float *cw3, uint8_t *out, int threads);
+void ora_bc4_image(const float *rgba, int w, int h, int quality, uint8_t *out, int threads);
 /* BC3/BC5 from an already quantised BGRA8 image (ColorBlock path without the float stage). */
 void ora_bc3_image_u8(const uint8_t *bgra, int w, int h, int alpha_mode, int quality, const float *cw3,
                       uint8_t *out, int threads);

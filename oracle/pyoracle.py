@@ -66,6 +66,11 @@ class Oracle:
         self._bc5_image = _bind(lib, "ora_bc5_image", None, [_vp, _i, _i, _i, _vp, _i])
         self._bc3_block = _bind(lib, "ora_bc3_block", None, [_vp, _i, _i, _vp, _vp])
         self._bc5_block = _bind(lib, "ora_bc5_block", None, [_vp, _i, _vp])
+        self._bc1a_block = _bind(lib, "ora_bc1a_block", None, [_vp, _i, _vp, _vp])
+        self._bc4_block = _bind(lib, "ora_bc4_block", None, [_vp, _i, _vp])
+        self._bc1a_image = _bind(lib, "ora_bc1a_image", None, [_vp, _i, _i, _i, _vp, _vp, _i])
+        self._bc4_image = _bind(lib, "ora_bc4_image", None, [_vp, _i, _i, _i, _vp, _i])
+        self._dxt1a_single = _bind(lib, "ora_dxt1a_single_color", None, [_i, _i, _i, ctypes.c_uint32, _vp])
         self._dxt5a_quick = _bind(lib, "ora_dxt5a_quick", None, [_vp, _vp])
         self._dxt5a_optimal = _bind(lib, "ora_dxt5a_optimal", None, [_vp, _vp])
         self._dxt1_single = _bind(lib, "ora_dxt1_single_color", None, [_i, _i, _i, _vp])
@@ -112,6 +117,23 @@ class Oracle:
         self._bc5_block(_ptr(b), quality, _ptr(out))
         return out
 
+    def bc1a_block(self, bgra64, alpha_mode=0, cw=(1, 1, 1)):
+        b = np.ascontiguousarray(bgra64, np.uint8).reshape(64)
+        out = np.zeros(8, np.uint8)
+        self._bc1a_block(_ptr(b), alpha_mode, _ptr(np.asarray(cw, np.float32)), _ptr(out))
+        return out
+
+    def bc4_block(self, bgra64, quality=1):
+        b = np.ascontiguousarray(bgra64, np.uint8).reshape(64)
+        out = np.zeros(8, np.uint8)
+        self._bc4_block(_ptr(b), quality, _ptr(out))
+        return out
+
+    def dxt1a_single_color(self, r, g, b, alpha_mask):
+        out = np.zeros(8, np.uint8)
+        self._dxt1a_single(r, g, b, alpha_mask, _ptr(out))
+        return out
+
     def dxt5a_quick(self, a16):
         a = np.ascontiguousarray(a16, np.uint8)
         out = np.zeros(8, np.uint8)
@@ -142,6 +164,18 @@ class Oracle:
         return out
 
     # -- images --
+    def bc1a_image(self, rgba, w, h, alpha_mode=0, cw=(1, 1, 1), threads=1):
+        r = np.ascontiguousarray(rgba, np.float32)
+        out = np.zeros(8 * self.nblocks(w, h), np.uint8)
+        self._bc1a_image(_ptr(r), w, h, alpha_mode, _ptr(np.asarray(cw, np.float32)), _ptr(out), threads)
+        return out
+
+    def bc4_image(self, rgba, w, h, quality=1, threads=1):
+        r = np.ascontiguousarray(rgba, np.float32)
+        out = np.zeros(8 * self.nblocks(w, h), np.uint8)
+        self._bc4_image(_ptr(r), w, h, quality, _ptr(out), threads)
+        return out
+
     @staticmethod
     def nblocks(w, h):
         return ((w + 3) // 4) * ((h + 3) // 4)
@@ -260,6 +294,8 @@ class Reference:
         self._compress = _bind(lib, "ref_compress_planar", _ll, [_vp, _i, _i, _i, _i, _i, _vp, _vp, _ll])
         self._bc3_block = _bind(lib, "ref_bc3_block", None, [_vp, _i, _i, _vp, _vp])
         self._bc5_block = _bind(lib, "ref_bc5_block", None, [_vp, _i, _vp])
+        self._bc1a_block = _bind(lib, "ref_bc1a_block", None, [_vp, _i, _vp, _vp])
+        self._bc4_block = _bind(lib, "ref_bc4_block", None, [_vp, _i, _vp])
         self._dxt5a_quick = _bind(lib, "ref_dxt5a_quick", None, [_vp, _vp])
         self._dxt5a_optimal = _bind(lib, "ref_dxt5a_optimal", None, [_vp, _vp])
         self._dxt1_single = _bind(lib, "ref_dxt1_single_color", None, [_i, _i, _i, _vp])
@@ -286,7 +322,7 @@ class Reference:
 
     def compress(self, rgba, w, h, fmt, quality=1, alpha_mode=0, cw=(1, 1, 1, 1)):
         r = np.ascontiguousarray(rgba, np.float32)
-        bs = 8 if fmt == 1 else 16
+        bs = 8 if fmt in (1, 2, 6) else 16
         out = np.zeros(bs * Oracle.nblocks(w, h), np.uint8)
         n = self._compress(_ptr(r), w, h, alpha_mode, fmt, quality, _ptr(np.asarray(cw, np.float32)), _ptr(out), out.size)
         assert n == out.size, n
@@ -302,6 +338,18 @@ class Reference:
         b = np.ascontiguousarray(bgra64, np.uint8).reshape(64)
         out = np.zeros(16, np.uint8)
         self._bc5_block(_ptr(b), quality, _ptr(out))
+        return out
+
+    def bc1a_block(self, bgra64, alpha_mode=0, cw=(1, 1, 1, 1)):
+        b = np.ascontiguousarray(bgra64, np.uint8).reshape(64)
+        out = np.zeros(8, np.uint8)
+        self._bc1a_block(_ptr(b), alpha_mode, _ptr(np.asarray(cw, np.float32)), _ptr(out))
+        return out
+
+    def bc4_block(self, bgra64, quality=1):
+        b = np.ascontiguousarray(bgra64, np.uint8).reshape(64)
+        out = np.zeros(8, np.uint8)
+        self._bc4_block(_ptr(b), quality, _ptr(out))
         return out
 
     def dxt5a_quick(self, a16):

@@ -136,6 +136,31 @@ void ref_bc5_block(const unsigned char * bgra64, int quality, unsigned char * ou
     }
 }
 
+// One BC1a block through CompressorDXT1a::compressBlock (src/nvtt/CompressorDX9.cpp:83-111),
+// the compressor chooseCpuCompressor picks above Fastest (src/nvtt/Context.cpp:1058-1066).
+void ref_bc1a_block(const unsigned char * bgra64, int alpha_mode, const float * cw4, unsigned char * out8) {
+    nv::ColorBlock cb((const uint *)bgra64);
+    CompressionOptions co;
+    fill_options(co, Format_BC1a, Quality_Normal, cw4);
+    memset(out8, 0, 8);
+    nv::CompressorDXT1a c;
+    c.compressBlock(cb, (AlphaMode)alpha_mode, co.m, out8);
+}
+
+// One BC4 block through FastCompressorBC4 / ProductionCompressorBC4 (src/nvtt/CompressorDX10.cpp).
+void ref_bc4_block(const unsigned char * bgra64, int quality, unsigned char * out8) {
+    nv::ColorBlock cb((const uint *)bgra64);
+    CompressionOptions co;
+    fill_options(co, Format_BC4, quality, NULL);
+    if (quality == Quality_Fastest || quality == Quality_Normal) {
+        nv::FastCompressorBC4 c;
+        c.compressBlock(cb, AlphaMode_None, co.m, out8);
+    } else {
+        nv::ProductionCompressorBC4 c;
+        c.compressBlock(cb, AlphaMode_None, co.m, out8);
+    }
+}
+
 void ref_dxt5a_quick(const unsigned char * a16, unsigned char * out8) {
     nv::AlphaBlock4x4 ab;
     for (int i = 0; i < 16; i++) { ab.alpha[i] = a16[i]; ab.weights[i] = 1.0f; }

@@ -49,17 +49,48 @@ def float_blocks(n, seed):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=pyoracle.REF_SRC)
-    ap.add_argument("--only", choices=["blocks", "dds"], help="write only the block/chain or only the DDS fixtures")
+    ap.add_argument("--only", choices=["blocks", "dds", "bc1a_bc4"],
+                    help="write only the block/chain, the DDS or the BC1a/BC4 block fixtures")
     args = ap.parse_args()
     path = pyoracle.build_reference(args.ref)
     if path is None:
         sys.exit("reference source tree not found")
     R = pyoracle.Reference(path)
-    if args.only != "dds":
+    if args.only in (None, "blocks"):
         write_block_fixtures(R)
-    if args.only != "blocks":
+    if args.only in (None, "dds"):
         write_dds_fixtures(R)
+    if args.only in (None, "bc1a_bc4"):
+        write_bc1a_bc4_fixtures(R)
     print("fixtures written to", HERE)
+
+
+def transparent_blocks(n, seed):
+    """Synthetic 4x4 BGRA8 blocks with zero-alpha texels planted: none, a seeded few, about a
+    third, or all sixteen (the BC1a cases)."""
+    rng = np.random.default_rng(seed)
+    blocks = synth.random_blocks(n, seed).reshape(n, 64).copy()
+    for t in range(n):
+        a = blocks[t, 3::4]
+        k = t % 4
+        if k == 1:
+            a[rng.integers(0, 16, 3)] = 0
+        elif k == 2:
+            a[rng.random(16) < 0.35] = 0
+        elif k == 3:
+            a[:] = 0
+        blocks[t, 3::4] = a
+    return blocks
+
+
+def write_bc1a_bc4_fixtures(R):
+    blocks = transparent_blocks(400, 77)
+    out = {"inputs": blocks}
+    for am in (0, 1):
+        out[f"bc1a_{am}"] = np.array([R.bc1a_block(b, am) for b in blocks])
+    for q in (1, 2):
+        out[f"bc4_{q}"] = np.array([R.bc4_block(b, q) for b in blocks])
+    np.savez_compressed(os.path.join(HERE, "bc1a_bc4_blocks.npz"), **out)
 
 
 def write_block_fixtures(R):
