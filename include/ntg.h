@@ -36,7 +36,9 @@ extern "C" {
 
 /* nvtt::Format subset */
 #define NTG_FORMAT_BC1 1   /* Format_DXT1 */
+#define NTG_FORMAT_BC1A 2  /* Format_DXT1a: Normal quality and above (CompressorDXT1a) */
 #define NTG_FORMAT_BC3 4   /* Format_DXT5 */
+#define NTG_FORMAT_BC4 6   /* Format_BC4 */
 #define NTG_FORMAT_BC5 7   /* Format_BC5 */
 /* nvtt::Quality */
 #define NTG_QUALITY_FASTEST 0

@@ -81,7 +81,12 @@ std::vector<Level> chain_levels(int w, int h, int max_levels) {
     return v;
 }
 
-int block_bytes(int format) { return format == NTG_FORMAT_BC1 ? 8 : 16; }
+int block_bytes(int format) {
+    return format == NTG_FORMAT_BC1 || format == NTG_FORMAT_BC1A || format == NTG_FORMAT_BC4 ? 8 : 16;
+}
+bool known_format(int f) {
+    return f == NTG_FORMAT_BC1 || f == NTG_FORMAT_BC1A || f == NTG_FORMAT_BC3 || f == NTG_FORMAT_BC4 || f == NTG_FORMAT_BC5;
+}
 long long blocks_of(int w, int h) { return (long long)((w + 3) / 4) * ((h + 3) / 4); }
 
 // Filter defaults of Surface::buildNextMipmap (getDefaultFilterWidthAndParams,
@@ -236,9 +241,14 @@ int max_window(const AxisTable &t, int tile) {
 
 int check_opts(const ntg_chain_options *opt) {
     if (!opt) return fail(NTG_ERROR_INVALID_INPUT, "null options");
-    if (opt->format != NTG_FORMAT_BC1 && opt->format != NTG_FORMAT_BC3 && opt->format != NTG_FORMAT_BC5)
-        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "format not supported (BC1, BC3, BC5)");
+    if (!known_format(opt->format))
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "format not supported (BC1, BC1a, BC3, BC4, BC5)");
     if (opt->quality < 0 || opt->quality > 3) return fail(NTG_ERROR_INVALID_INPUT, "bad quality");
+    // FastCompressorDXT1a (QuickCompress::compressDXT1a, src/nvtt/QuickCompressDXT.cpp:716-763)
+    // computes the indices of a block with transparent texels over 16 entries of an array that
+    // holds only the opaque ones: the rest is uninitialised, so there is no output to reproduce.
+    if (opt->format == NTG_FORMAT_BC1A && opt->quality == NTG_QUALITY_FASTEST)
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "BC1a at Fastest quality is not supported (use Normal or above)");
     if (opt->filter < 0 || opt->filter > 2) return fail(NTG_ERROR_INVALID_INPUT, "bad filter");
     if (opt->wrap < 0 || opt->wrap > 2) return fail(NTG_ERROR_INVALID_INPUT, "bad wrap mode");
     if (opt->in_xform < 0 || opt->in_xform > 2 || opt->out_xform < 0 || opt->out_xform > 2)
@@ -477,9 +487,11 @@ int upload_jobs(ntg_context *ctx, const std::vector<EncJob> &jobs, cudaStream_t 
 
 int launch_encode(int format, const EncJob *d_jobs, int njobs, long long nblocks, int quality, cudaStream_t s,
                   int threads = 0) {
-    int r = format == NTG_FORMAT_BC1 ? launch_bc1(d_jobs, njobs, nblocks, quality, threads, s)
-            : format == NTG_FORMAT_BC3 ? launch_bc3(d_jobs, njobs, nblocks, quality, threads, s)
-                                       : launch_bc5(d_jobs, njobs, nblocks, quality, threads, s);
+    int r = format == NTG_FORMAT_BC1    ? launch_bc1(d_jobs, njobs, nblocks, quality, threads, s)
+            : format == NTG_FORMAT_BC3  ? launch_bc3(d_jobs, njobs, nblocks, quality, threads, s)
+            : format == NTG_FORMAT_BC1A ? launch_bc1a(d_jobs, njobs, nblocks, quality, threads, s)
+            : format == NTG_FORMAT_BC4  ? launch_bc4(d_jobs, njobs, nblocks, quality, threads, s)
+                                        : launch_bc5(d_jobs, njobs, nblocks, quality, threads, s);
     return launched(r, "encoder launch");
 }
 
@@ -632,7 +644,7 @@ int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, 
     cudaStream_t s = S(stream);
     uint32_t *q = nullptr;
     if (format != NTG_FORMAT_BC1 && out_xform != NTG_XFORM_NONE) {
-        // BC3/BC5 quantise the transformed level first (ColorBlock::init on the toGamma'd copy)
+        // the 8-bit formats quantise the transformed level first (ColorBlock::init on the toGamma'd copy)
         const XformTables *xt = ctx->xform(NTG_XFORM_NONE, out_xform, gamma);
         if (!xt) return fail(NTG_ERROR_CUDA, "table upload failed");
         if (out_xform == NTG_XFORM_GAMMA && gamma != 2.2f)
@@ -902,8 +914,7 @@ int ntg_profile_read(ntg_context *ctx, float *mips_ms, float *encode_ms) {
 int ntg_decode(ntg_context *ctx, int format, const void *d_blocks, int w, int h, float *d_rgba, void *stream) {
     g_error.clear();
     if (!ctx || !d_blocks || !d_rgba || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
-    if (format != NTG_FORMAT_BC1 && format != NTG_FORMAT_BC3 && format != NTG_FORMAT_BC5)
-        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "format not supported");
+    if (!known_format(format)) return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "format not supported");
     NTG_TRY(ensure_device(ctx));
     return launched(launch_decode(format, (const uint8_t *)d_blocks, w, h, d_rgba, S(stream)), "decode");
 }
@@ -939,7 +950,7 @@ struct ntg_batch {
     };
     std::vector<Enc> encodes;
     MipTuning tune;
-    int enc_threads[3] = {64, 128, 128};  // blocks per CTA of the BC1, BC3, BC5 encoders
+    int enc_threads[3] = {64, 128, 128};  // blocks per CTA of the BC1, BC3 + BC1a, BC5 + BC4 encoders
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long texels = 0, blocks = 0;
@@ -963,7 +974,11 @@ struct ntg_batch {
 
 namespace {
 
-int enc_slot(int format) { return format == NTG_FORMAT_BC1 ? 0 : format == NTG_FORMAT_BC3 ? 1 : 2; }
+// Encoder families sharing one launch shape: BC1 (icbc); BC3 and BC1a (squish fit in shared
+// memory); BC5 and BC4 (interpolated-alpha blocks).
+int enc_slot(int format) {
+    return format == NTG_FORMAT_BC1 ? 0 : (format == NTG_FORMAT_BC3 || format == NTG_FORMAT_BC1A) ? 1 : 2;
+}
 
 // Byte offsets of the learned path's buffers for n blocks: x, y, list, stats.
 struct LearnLayout {
@@ -1068,9 +1083,9 @@ int batch_mips(ntg_batch *b, cudaStream_t s) {
     return run_stages(b->stages, b->d_mip, s);
 }
 
-int batch_encodes(ntg_batch *b, cudaStream_t s, int only_format = -1) {
+int batch_encodes(ntg_batch *b, cudaStream_t s, int only_slot = -1) {
     for (const auto &e : b->encodes) {
-        if (only_format >= 0 && e.format != only_format) continue;
+        if (only_slot >= 0 && enc_slot(e.format) != only_slot) continue;
         if (learned_group(b, e)) {
             const LearnLayout L(e.nblocks);
             float *x = (float *)(b->d_learn + L.x), *y = (float *)(b->d_learn + L.y);
@@ -1329,17 +1344,16 @@ int ntg_batch_autotune(ntg_batch *b, void *stream) {
     NTG_TRY(batch_plan(b));
     // encoder blocks per CTA, per format present
     float enc_total = 0;
-    for (int format : {NTG_FORMAT_BC1, NTG_FORMAT_BC3, NTG_FORMAT_BC5}) {
+    for (int slot = 0; slot < 3; slot++) {
         bool present = false;
-        for (const auto &e : b->encodes) present = present || e.format == format;
+        for (const auto &e : b->encodes) present = present || enc_slot(e.format) == slot;
         if (!present) continue;
-        const int slot = enc_slot(format);
         int best_t = b->enc_threads[slot];
         float best_e = 1e30f;
         for (int threads : {32, 64, 128}) {
-            if (format == NTG_FORMAT_BC1 && threads > 64) continue;
+            if (slot == 0 && threads > 64) continue;
             b->enc_threads[slot] = threads;
-            const float ms = time_ms(s, [&] { return batch_encodes(b, s, format); }, 3, &status);
+            const float ms = time_ms(s, [&] { return batch_encodes(b, s, slot); }, 3, &status);
             NTG_TRY(status);
             if (ms < best_e) { best_e = ms; best_t = threads; }
         }
@@ -1389,13 +1403,12 @@ int ntg_batch_time_phases(ntg_batch *b, void *stream, float ms[4], long long blo
     int status = NTG_OK;
     ms[0] = time_ms(s, [&] { return batch_mips(b, s); }, 1, &status);
     NTG_TRY(status);
-    const int formats[3] = {NTG_FORMAT_BC1, NTG_FORMAT_BC3, NTG_FORMAT_BC5};
     for (int i = 0; i < 3; i++) {
         long long nb = 0;
         for (const auto &e : b->encodes)
-            if (e.format == formats[i]) nb += e.nblocks;
+            if (enc_slot(e.format) == i) nb += e.nblocks;
         if (blocks) blocks[i] = nb;
-        ms[1 + i] = nb ? time_ms(s, [&] { return batch_encodes(b, s, formats[i]); }, 1, &status) : 0.0f;
+        ms[1 + i] = nb ? time_ms(s, [&] { return batch_encodes(b, s, i); }, 1, &status) : 0.0f;
         NTG_TRY(status);
     }
     return NTG_OK;

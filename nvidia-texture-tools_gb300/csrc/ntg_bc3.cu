@@ -1,4 +1,4 @@
-// BC3 and BC5 encoders for sm_103a.
+// BC3, BC5, BC1a and BC4 encoders for sm_103a.
 //
 // BC3 = CompressorDXT5::compressBlock (src/nvtt/CompressorDX9.cpp:145-176):
 //   alpha : QuickCompress::compressDXT5A (Normal/Production) or OptimalCompress::compressDXT5A
@@ -13,6 +13,7 @@
 // shared memory as [element][thread] because the cluster-split loops index them by running
 // counts. Blocks with 16 distinct colours (the common case) all run the same 969-split schedule,
 // so those warps do not diverge in the search. Built with --fmad=false.
+#include "ntg.h"
 #include "ntg_device.cuh"
 #include "ntg_internal.h"
 
@@ -179,16 +180,18 @@ __device__ __forceinline__ int float_to_int(float a, int limit) {
 // squish WeightedClusterFit, scalar build: ColourSet with the header's default
 // createMinimalSet = true (src/nvtt/squish/colourset.h:40, colourset.cpp:44-90), SetColourSet
 // (src/nvtt/squish/weightedclusterfit.cpp:39-105), ComputeWeightedCovariance /
-// ComputePrincipleComponent (src/nvtt/squish/maths.cpp:32-135), Compress4
-// (src/nvtt/squish/weightedclusterfit.cpp:476-589), WriteColourBlock4
-// (src/nvtt/squish/colourblock.cpp:108-139).
+// ComputePrincipleComponent (src/nvtt/squish/maths.cpp:32-135), Compress4 / Compress3
+// (src/nvtt/squish/weightedclusterfit.cpp:476-589, 372-470), WriteColourBlock4 / 3
+// (src/nvtt/squish/colourblock.cpp:108-139, 75-106).
 //
 // The minimal set is kept in texel slots instead of being compacted: a slot is live when its
 // texel is the first with that RGB, and its weight collects the weights of the later duplicates
 // in texel order. Live slots in slot order are exactly the reference's points in order, so the
 // sums run in the same order; dead slots sort last behind +inf keys. Everything stays in
 // registers with static indices; `wp` is this thread's [17][thread] float4 staging for the
-// split loops, which index points by running counts.
+// split loops, which index points by running counts. In DXT1 mode (BC1a) a texel with alpha 0
+// is never live and never matched, and takes index 3 at the end.
+
 // Min(one, Max(zero, v)) then Floor(grid * v + half) * gridrcp
 // (src/nvtt/squish/weightedclusterfit.cpp:516-519) per channel, grid (31, 63, 31); the clamp is
 // snap_clamp, which gives the same snapped value as squish's Max/Min for every input.
@@ -198,25 +201,39 @@ __device__ __forceinline__ f3 snap565(f3 v) {
                floorf(31.0f * z + 0.5f) * (1.0f / 31.0f));
 }
 
-template <bool UNIT_METRIC, typename Arr>
-__device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f3 metric, Arr wp) {
+// The colour set of a block, sorted along its principal axis and staged in `wp`.
+struct SquishSet {
+    int count;
+    uint32_t transparent;  // bit i: texel i has alpha 0 (DXT1 mode only)
+    uint64_t first;        // 4 bits per texel: slot of its point
+    uint64_t order;        // 4 bits per sorted position: slot
+    f3 xsum;
+    float wsum;
+};
+
+template <bool DXT1, typename Arr>
+__device__ __forceinline__ void squish_prepare(const uint32_t px[16], bool weight_by_alpha, f3 metric, Arr wp,
+                                               SquishSet &S) {
     float X[16], Y[16], Z[16], W[16];
-    uint32_t live = 0;        // bit i: slot i holds a point
-    uint64_t first = 0;       // 4 bits per texel: slot of its point
+    uint32_t live = 0;  // bit i: slot i holds a point
+    uint32_t transp = 0;
+    uint64_t first = 0;
 #pragma unroll
     for (int i = 0; i < 16; i++) {
         X[i] = (float)((px[i] >> 16) & 255) / 255.0f;
         Y[i] = (float)((px[i] >> 8) & 255) / 255.0f;
         Z[i] = (float)(px[i] & 255) / 255.0f;
         W[i] = weight_by_alpha ? (float)((px[i] >> 24) + 1) / 256.0f : 1.0f;
+        if (DXT1 && (px[i] >> 24) == 0) transp |= 1u << i;
     }
 #pragma unroll
     for (int i = 0; i < 16; i++) {
-        bool found = false;
+        const bool skip = DXT1 && ((transp >> i) & 1u);
+        bool found = skip;
         int slot = i;
 #pragma unroll
         for (int j = 0; j < i; j++) {
-            const bool m = !found && ((px[i] & 0xFFFFFF) == (px[j] & 0xFFFFFF));
+            const bool m = !found && !(DXT1 && ((transp >> j) & 1u)) && ((px[i] & 0xFFFFFF) == (px[j] & 0xFFFFFF));
             if (m) { W[j] += W[i]; slot = j; }
             found = found || m;
         }
@@ -288,12 +305,24 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
         if (i < count) { xsum = xsum + p; wsum += W[i]; }
     }
     wp[16] = make_float4(0, 0, 0, 0);
-    const f3 msq = metric * metric;
+    S.count = count;
+    S.transparent = transp;
+    S.first = first;
+    S.order = order;
+    S.xsum = xsum;
+    S.wsum = wsum;
+}
 
-    // The split search keeps only the best error and its cluster sizes; the endpoints of the
-    // winner are recomputed afterwards with the same sequence of operations.
+// Compress4's split search: the first strict minimum, as best error and split key
+// c0 << 10 | c1 << 5 | c2 (the endpoints of the winner are recomputed afterwards with the same
+// sequence of operations).
+template <bool UNIT_METRIC, typename Arr>
+__device__ __forceinline__ float squish_search4(const SquishSet &S, f3 msq, Arr wp, int &best) {
+    const int count = S.count;
+    const f3 xsum = S.xsum;
+    const float wsum = S.wsum;
     float besterr = FLT_MAX;
-    int best = 0;  // winning split as c0 << 10 | c1 << 5 | c2
+    best = 0;
     f3 x0 = mk3(0, 0, 0);
     float w0 = 0.0f;
     for (int c0 = 0; c0 <= count; c0++) {
@@ -316,10 +345,8 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
                 const float f = 1.0f / (a2 * b2s - ab * ab);
                 const f3 ax = axp + (x2 * (1.0f / 3.0f));
                 const f3 bx = xsum - ax;
-                f3 a = ((ax * b2s) - (bx * ab)) * f;
-                f3 b = ((bx * a2) - (ax * ab)) * f;
-                a = snap565(a);
-                b = snap565(b);
+                const f3 a = snap565(((ax * b2s) - (bx * ab)) * f);
+                const f3 b = snap565(((bx * a2) - (ax * ab)) * f);
                 const f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
                 const f3 e1 = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
                 // x * 1.0f is x exactly: the default unit metric drops the three multiplies
@@ -338,43 +365,166 @@ __device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f
         x0 = x0 + mk3(q.x, q.y, q.z);
         w0 += q.w;
     }
-    if (!(besterr < FLT_MAX)) return make_uint2(0, 0);
-    const int b0 = best >> 10, b1 = (best >> 5) & 31, b2 = best & 31;
-    f3 bs, be;
-    {
-        // the running sums of the winning split, accumulated exactly as the search did
-        f3 x0b = mk3(0, 0, 0), x1b = mk3(0, 0, 0), x2b = mk3(0, 0, 0);
-        float w0b = 0.0f, w1b = 0.0f, w2b = 0.0f;
-        for (int i = 0; i < b0; i++) { const float4 q = wp[i]; x0b = x0b + mk3(q.x, q.y, q.z); w0b += q.w; }
-        for (int i = b0; i < b0 + b1; i++) { const float4 q = wp[i]; x1b = x1b + mk3(q.x, q.y, q.z); w1b += q.w; }
-        for (int i = b0 + b1; i < b0 + b1 + b2; i++) { const float4 q = wp[i]; x2b = x2b + mk3(q.x, q.y, q.z); w2b += q.w; }
-        const float w3 = wsum - w0b - w1b - w2b;
-        const float a2 = w0b + w1b * (4.0f / 9.0f) + w2b * (1.0f / 9.0f);
-        const float b2s = w3 + w2b * (4.0f / 9.0f) + w1b * (1.0f / 9.0f);
-        const float ab = (w1b + w2b) * (2.0f / 9.0f);
-        const float f = 1.0f / (a2 * b2s - ab * ab);
-        const f3 ax = (x0b + (x1b * (2.0f / 3.0f))) + (x2b * (1.0f / 3.0f));
-        const f3 bx = xsum - ax;
-        f3 a = ((ax * b2s) - (bx * ab)) * f;
-        f3 b = ((bx * a2) - (ax * ab)) * f;
-        bs = snap565(a);
-        be = snap565(b);
+    return besterr;
+}
+
+// Compress3's split search (two clusters ends, key c0 << 5 | c1).
+template <bool UNIT_METRIC, typename Arr>
+__device__ __forceinline__ float squish_search3(const SquishSet &S, f3 msq, Arr wp, int &best) {
+    const int count = S.count;
+    float besterr = FLT_MAX;
+    best = 0;
+    f3 x0 = mk3(0, 0, 0);
+    float w0 = 0.0f;
+    for (int c0 = 0; c0 <= count; c0++) {
+        f3 x1 = mk3(0, 0, 0);
+        float w1 = 0.0f;
+        int key = c0 << 5;
+        for (int c1 = 0; c1 <= count - c0; c1++) {
+            const float w2 = S.wsum - w0 - w1;
+            const float a2 = w0 + w1 * 0.25f;
+            const float b2s = w2 + w1 * 0.25f;
+            const float ab = w1 * 0.25f;
+            const float f = 1.0f / (a2 * b2s - ab * ab);
+            const f3 ax = x0 + x1 * 0.5f;
+            const f3 bx = S.xsum - ax;
+            const f3 a = snap565(((ax * b2s) - (bx * ab)) * f);
+            const f3 b = snap565(((bx * a2) - (ax * ab)) * f);
+            const f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
+            const f3 e1 = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
+            const float err = UNIT_METRIC ? (e1.x + e1.y) + e1.z : dot(e1, msq);
+            if (err < besterr) { besterr = err; best = key; }
+            key++;
+            const float4 q = wp[c0 + c1];
+            x1 = x1 + mk3(q.x, q.y, q.z);
+            w1 += q.w;
+        }
+        const float4 q = wp[c0];
+        x0 = x0 + mk3(q.x, q.y, q.z);
+        w0 += q.w;
     }
-    // cluster sizes -> point (slot) indices -> texel indices (ColourSet::RemapIndices)
+    return besterr;
+}
+
+// The running sums of a winning split (cluster sizes b0, b1, b2), accumulated as the search did.
+template <typename Arr>
+__device__ __forceinline__ void split_sums(Arr wp, int b0, int b1, int b2, f3 &x0, f3 &x1, f3 &x2, float &w0, float &w1,
+                                           float &w2) {
+    x0 = mk3(0, 0, 0); x1 = mk3(0, 0, 0); x2 = mk3(0, 0, 0);
+    w0 = 0.0f; w1 = 0.0f; w2 = 0.0f;
+    for (int i = 0; i < b0; i++) { const float4 q = wp[i]; x0 = x0 + mk3(q.x, q.y, q.z); w0 += q.w; }
+    for (int i = b0; i < b0 + b1; i++) { const float4 q = wp[i]; x1 = x1 + mk3(q.x, q.y, q.z); w1 += q.w; }
+    for (int i = b0 + b1; i < b0 + b1 + b2; i++) { const float4 q = wp[i]; x2 = x2 + mk3(q.x, q.y, q.z); w2 += q.w; }
+}
+
+// Sorted-position clusters -> slot indices -> texel indices (ColourSet::RemapIndices,
+// src/nvtt/squish/colourset.cpp:141-151; transparent texels take 3). Four-colour clusters are
+// 0, 2, 3, 1 in order; three-colour ones 0, 2, 1.
+template <bool THREE>
+__device__ __forceinline__ uint32_t texel_indices(const SquishSet &S, int b0, int b1, int b2) {
     uint32_t slot_idx = 0;
 #pragma unroll
     for (int i = 0; i < 16; i++) {
-        const uint32_t c = i < b0 ? 0u : (i < b0 + b1 ? 2u : (i < b0 + b1 + b2 ? 3u : 1u));
-        if (i < count) slot_idx |= c << (2 * (int)((order >> (4 * i)) & 15));
+        const uint32_t c = i < b0 ? 0u : (i < b0 + b1 ? 2u : ((!THREE && i < b0 + b1 + b2) ? 3u : 1u));
+        if (i < S.count) slot_idx |= c << (2 * (int)((S.order >> (4 * i)) & 15));
     }
     uint32_t idx = 0;
 #pragma unroll
-    for (int i = 0; i < 16; i++) idx |= ((slot_idx >> (2 * (int)((first >> (4 * i)) & 15))) & 3u) << (2 * i);
-    int ea = (float_to_int(31.0f * bs.x, 31) << 11) | (float_to_int(63.0f * bs.y, 63) << 5) | float_to_int(31.0f * bs.z, 31);
-    int eb = (float_to_int(31.0f * be.x, 31) << 11) | (float_to_int(63.0f * be.y, 63) << 5) | float_to_int(31.0f * be.z, 31);
+    for (int i = 0; i < 16; i++) {
+        const uint32_t v = ((S.transparent >> i) & 1u) ? 3u : ((slot_idx >> (2 * (int)((S.first >> (4 * i)) & 15))) & 3u);
+        idx |= v << (2 * i);
+    }
+    return idx;
+}
+
+__device__ __forceinline__ int squish_565(f3 c) {
+    return (float_to_int(31.0f * c.x, 31) << 11) | (float_to_int(63.0f * c.y, 63) << 5) | float_to_int(31.0f * c.z, 31);
+}
+
+template <bool UNIT_METRIC, typename Arr>
+__device__ __forceinline__ uint2 squish_block4(const SquishSet &S, f3 msq, Arr wp, float &err) {
+    int best;
+    err = squish_search4<UNIT_METRIC>(S, msq, wp, best);
+    if (!(err < FLT_MAX)) return make_uint2(0, 0);
+    const int b0 = best >> 10, b1 = (best >> 5) & 31, b2 = best & 31;
+    f3 x0, x1, x2;
+    float w0, w1, w2;
+    split_sums(wp, b0, b1, b2, x0, x1, x2, w0, w1, w2);
+    const float w3 = S.wsum - w0 - w1 - w2;
+    const float a2 = w0 + w1 * (4.0f / 9.0f) + w2 * (1.0f / 9.0f);
+    const float b2s = w3 + w2 * (4.0f / 9.0f) + w1 * (1.0f / 9.0f);
+    const float ab = (w1 + w2) * (2.0f / 9.0f);
+    const float f = 1.0f / (a2 * b2s - ab * ab);
+    const f3 ax = (x0 + (x1 * (2.0f / 3.0f))) + (x2 * (1.0f / 3.0f));
+    const f3 bx = S.xsum - ax;
+    const f3 bs = snap565(((ax * b2s) - (bx * ab)) * f);
+    const f3 be = snap565(((bx * a2) - (ax * ab)) * f);
+    uint32_t idx = texel_indices<false>(S, b0, b1, b2);
+    int ea = squish_565(bs), eb = squish_565(be);
     if (ea < eb) { int t = ea; ea = eb; eb = t; idx ^= 0x55555555u; }
     else if (ea == eb) idx = 0;
     return make_uint2((uint32_t)ea | ((uint32_t)eb << 16), idx);
+}
+
+template <bool UNIT_METRIC, typename Arr>
+__device__ __forceinline__ uint2 squish_block3(const SquishSet &S, f3 msq, Arr wp, float &err) {
+    int best;
+    err = squish_search3<UNIT_METRIC>(S, msq, wp, best);
+    if (!(err < FLT_MAX)) return make_uint2(0, 0);
+    const int b0 = best >> 5, b1 = best & 31;
+    f3 x0, x1, x2;
+    float w0, w1, w2;
+    split_sums(wp, b0, b1, 0, x0, x1, x2, w0, w1, w2);
+    const float w2r = S.wsum - w0 - w1;
+    const float a2 = w0 + w1 * 0.25f;
+    const float b2s = w2r + w1 * 0.25f;
+    const float ab = w1 * 0.25f;
+    const float f = 1.0f / (a2 * b2s - ab * ab);
+    const f3 ax = x0 + x1 * 0.5f;
+    const f3 bx = S.xsum - ax;
+    const f3 bs = snap565(((ax * b2s) - (bx * ab)) * f);
+    const f3 be = snap565(((bx * a2) - (ax * ab)) * f);
+    uint32_t idx = texel_indices<true>(S, b0, b1, 0);
+    int ea = squish_565(bs), eb = squish_565(be);
+    // WriteColourBlock3: endpoints ascending; swapping exchanges indices 0 and 1
+    if (ea > eb) { int t = ea; ea = eb; eb = t; idx ^= (~idx >> 1) & 0x55555555u; }
+    return make_uint2((uint32_t)ea | ((uint32_t)eb << 16), idx);
+}
+
+// BC3 colour: Compress4 over the full colour set.
+template <bool UNIT_METRIC, typename Arr>
+__device__ uint2 squish_compress4(const uint32_t px[16], bool weight_by_alpha, f3 metric, Arr wp) {
+    SquishSet S;
+    squish_prepare<false>(px, weight_by_alpha, metric, wp, S);
+    float err;
+    return squish_block4<UNIT_METRIC>(S, metric * metric, wp, err);
+}
+
+// BC1a colour (ColourFit::Compress with kDxt1, src/nvtt/squish/colourfit.cpp:39-55): Compress3,
+// then Compress4 unless a texel is transparent; a later mode replaces the block only with a
+// strictly smaller error.
+template <bool UNIT_METRIC, typename Arr>
+__device__ uint2 squish_compress_dxt1(const uint32_t px[16], bool weight_by_alpha, f3 metric, Arr wp) {
+    SquishSet S;
+    squish_prepare<true>(px, weight_by_alpha, metric, wp, S);
+    const f3 msq = metric * metric;
+    float e3, e4;
+    uint2 out = squish_block3<UNIT_METRIC>(S, msq, wp, e3);
+    if (!(e3 < FLT_MAX)) e3 = FLT_MAX;
+    if (S.transparent == 0) {
+        const uint2 four = squish_block4<UNIT_METRIC>(S, msq, wp, e4);
+        if (e4 < e3) out = four;
+    }
+    return out;
+}
+
+// OptimalCompress::compressDXT1a(Color32, alphaMask) (src/nvtt/OptimalCompressDXT.cpp:271-292).
+__device__ __forceinline__ uint2 dxt1a_single_color(int r, int g, int b, uint32_t alpha_mask) {
+    if (alpha_mask == 0) return dxt1_single_color(r, g, b);
+    unsigned c0 = ((unsigned)c_tab.opt_alpha5[r][0] << 11) | ((unsigned)c_tab.opt_alpha6[g][0] << 5) | c_tab.opt_alpha5[b][0];
+    unsigned c1 = ((unsigned)c_tab.opt_alpha5[r][1] << 11) | ((unsigned)c_tab.opt_alpha6[g][1] << 5) | c_tab.opt_alpha5[b][1];
+    if (c0 > c1) { unsigned t = c0; c0 = c1; c1 = t; }
+    return make_uint2(c0 | (c1 << 16), 0xaaaaaaaau | alpha_mask);
 }
 
 // QuickCompress::compressDXT1 (src/nvtt/QuickCompressDXT.cpp:653-713) with roundAndExpand
@@ -560,6 +710,55 @@ __global__ void __launch_bounds__(128) k_bc5(const EncJob *__restrict__ jobs, in
     pack_alpha(QUALITY >= 2 ? dxt5a_optimal(ch) : dxt5a_quick(ch), dst + 8);
 }
 
+// BC1a = CompressorDXT1a::compressBlock (src/nvtt/CompressorDX9.cpp:83-111), Normal quality and
+// above: single RGB colour -> OptimalCompress::compressDXT1a with the mask of zero-alpha texels,
+// otherwise the squish fit in DXT1 mode.
+__global__ void __launch_bounds__(128, NTG_BC3_MIN_CTAS) k_bc1a(const EncJob *__restrict__ jobs, int njobs,
+                                                               long long nblocks) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    uint32_t px[16];
+    load_block(J, 4 * (blk % J.bw), 4 * (blk / J.bw), px);
+    uint32_t mask = 0;
+    bool single = true;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        if ((px[i] >> 24) == 0) mask |= 3u << (2 * i);
+        single = single && ((px[i] & 0xFFFFFF) == (px[0] & 0xFFFFFF));
+    }
+    uint2 col;
+    if (single) col = dxt1a_single_color((px[0] >> 16) & 255, (px[0] >> 8) & 255, px[0] & 255, mask);
+    else {
+        struct { float4 *b; int s; __device__ float4 &operator[](int k) const { return b[k * s]; } } wp{smem + t, T};
+        const f3 metric = mk3(J.cw[0], J.cw[1], J.cw[2]);
+        if (metric.x == 1.0f && metric.y == 1.0f && metric.z == 1.0f)
+            col = squish_compress_dxt1<true>(px, J.alpha_mode == 1, metric, wp);
+        else
+            col = squish_compress_dxt1<false>(px, J.alpha_mode == 1, metric, wp);
+    }
+    *reinterpret_cast<uint2 *>(J.out + 8 * (size_t)blk) = col;
+}
+
+// BC4 = FastCompressorBC4 / ProductionCompressorBC4 (src/nvtt/CompressorDX10.cpp:40-72): the red
+// channel (AlphaBlock4x4::init(src, 0)) as an interpolated-alpha block.
+template <int QUALITY>
+__global__ void __launch_bounds__(128) k_bc4(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
+    const long long gblk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    uint32_t px[16];
+    load_block(J, 4 * (blk % J.bw), 4 * (blk / J.bw), px);
+    int ch[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) ch[i] = (int)((px[i] >> 16) & 255);
+    pack_alpha(QUALITY >= 2 ? dxt5a_optimal(ch) : dxt5a_quick(ch), J.out + 8 * (size_t)blk);
+}
+
 int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
     const int T = threads == 32 || threads == 64 ? threads : 128;  // blocks per CTA
@@ -579,6 +778,24 @@ int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, 
     const unsigned grid = (unsigned)((nblocks + T - 1) / T);
     if (quality >= 2) k_bc5<2><<<grid, T, 0, stream>>>(d_jobs, njobs, nblocks);
     else k_bc5<1><<<grid, T, 0, stream>>>(d_jobs, njobs, nblocks);
+    return launch_status();
+}
+
+int launch_bc1a(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
+    if (nblocks == 0) return 0;
+    if (quality == 0) return NTG_ERROR_UNSUPPORTED_FEATURE;  // see ntg_encode's check
+    const int T = threads == 32 || threads == 64 ? threads : 128;  // blocks per CTA
+    const size_t sm = (size_t)T * 17 * sizeof(float4);
+    k_bc1a<<<(unsigned)((nblocks + T - 1) / T), T, sm, stream>>>(d_jobs, njobs, nblocks);
+    return launch_status();
+}
+
+int launch_bc4(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
+    if (nblocks == 0) return 0;
+    const int T = threads == 32 || threads == 64 ? threads : 128;  // blocks per CTA
+    const unsigned grid = (unsigned)((nblocks + T - 1) / T);
+    if (quality >= 2) k_bc4<2><<<grid, T, 0, stream>>>(d_jobs, njobs, nblocks);
+    else k_bc4<1><<<grid, T, 0, stream>>>(d_jobs, njobs, nblocks);
     return launch_status();
 }
 

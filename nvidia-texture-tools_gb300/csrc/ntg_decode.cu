@@ -23,8 +23,13 @@ __global__ void k_decode(int format, const uint8_t *__restrict__ blocks, int w, 
     const int bx = (int)(blk % bw), by = (int)(blk / bw);
     const size_t n = (size_t)w * h;
     uint8_t r[16], g[16], b[16], a[16];
-    if (format == 1 || format == 4) {
-        const uint2 c = *reinterpret_cast<const uint2 *>(blocks + (format == 1 ? 8 : 16) * (size_t)blk + (format == 1 ? 0 : 8));
+    const bool bc1 = format == 1 || format == 2;  // BC1a has BC1's block layout
+    if (format == 6) {  // BlockATI1::decodeBlock (src/nvimage/BlockDXT.cpp:513-526)
+        decode_alpha8(*reinterpret_cast<const uint2 *>(blocks + 8 * (size_t)blk), r);
+#pragma unroll
+        for (int i = 0; i < 16; i++) { g[i] = r[i]; b[i] = r[i]; a[i] = 255; }
+    } else if (bc1 || format == 4) {
+        const uint2 c = *reinterpret_cast<const uint2 *>(blocks + (bc1 ? 8 : 16) * (size_t)blk + (bc1 ? 0 : 8));
         const unsigned c0 = c.x & 0xFFFF, c1 = c.x >> 16;
         Pal8 p;
         palette_d3d10(c0, c1, p);

@@ -61,16 +61,19 @@ void build_device_tables(HostTables &t) {
                 if (err < best) { best = err; t.icbc_match6[i][0] = (uint8_t)mx; t.icbc_match6[i][1] = (uint8_t)mn; }
             }
     }
-    // OMatch5 / OMatch6 (src/nvtt/SingleColorLookup.cpp:32-89)
-    for (int pass = 0; pass < 2; pass++) {
-        const int size = pass == 0 ? 32 : 64;
-        uint8_t(*tab)[2] = pass == 0 ? t.opt_match5 : t.opt_match6;
+    // OMatch5 / OMatch6 and OMatchAlpha5 / OMatchAlpha6 (src/nvtt/SingleColorLookup.cpp:32-89):
+    // the one-third point, or the midpoint for the three-colour tables
+    for (int pass = 0; pass < 4; pass++) {
+        const int size = (pass & 1) == 0 ? 32 : 64;
+        const bool mid = pass >= 2;
+        uint8_t(*tab)[2] = pass == 0 ? t.opt_match5 : pass == 1 ? t.opt_match6 : pass == 2 ? t.opt_alpha5 : t.opt_alpha6;
         for (int i = 0; i < 256; i++) {
             int best = 256 * 100;
             for (int mn = 0; mn < size; mn++)
                 for (int mx = 0; mx < size; mx++) {
-                    int lo = pass == 0 ? ex5(mn) : ex6(mn), hi = pass == 0 ? ex5(mx) : ex6(mx);
-                    int err = std::abs((hi * 2 + lo) / 3 - i) * 100 + std::abs(mx - mn) * 3;
+                    int lo = (pass & 1) == 0 ? ex5(mn) : ex6(mn), hi = (pass & 1) == 0 ? ex5(mx) : ex6(mx);
+                    int err = (mid ? std::abs((hi + lo) / 2 - i) : std::abs((hi * 2 + lo) / 3 - i)) * 100 +
+                              std::abs(mx - mn) * 3;
                     if (err < best) { tab[i][0] = (uint8_t)mx; tab[i][1] = (uint8_t)mn; best = err; }
                 }
         }

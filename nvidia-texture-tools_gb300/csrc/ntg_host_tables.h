@@ -18,6 +18,8 @@ struct HostTables {
     uint8_t icbc_match6[256][2];
     uint8_t opt_match5[256][2];    // OptimalCompress single-colour tables
     uint8_t opt_match6[256][2];
+    uint8_t opt_alpha5[256][2];    // the three-colour (midpoint) variants, for BC1a
+    uint8_t opt_alpha6[256][2];
     float pow_5_11[512];           // exponent tables of the gamma-2.2 helpers
     float pow_11_5[512];
 };

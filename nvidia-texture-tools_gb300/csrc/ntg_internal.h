@@ -45,6 +45,8 @@ struct EncJob {
 int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
+int launch_bc1a(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
+int launch_bc4(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 
 // Learned endpoint proposal, BC1 Normal quality: the network's inputs (x [nblocks x 48]), training
 // targets from encoded blocks (tg [nblocks x 8]), the pruned fit from the network's outputs

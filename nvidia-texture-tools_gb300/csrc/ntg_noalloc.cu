@@ -90,10 +90,13 @@ extern "C" int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_r
         return report(NTG_ERROR_INVALID_INPUT, "ntg_encode_noalloc: level of " + std::to_string(w) + "x" +
                                                    std::to_string(h) + " texels exceeds its scratch limit of " +
                                                    std::to_string(kMaxTexels) + " texels (use ntg_encode)");
-    if (format != NTG_FORMAT_BC1 && format != NTG_FORMAT_BC3 && format != NTG_FORMAT_BC5)
-        return report(NTG_ERROR_UNSUPPORTED_FEATURE, "format not supported (BC1, BC3, BC5)");
+    if (format != NTG_FORMAT_BC1 && format != NTG_FORMAT_BC1A && format != NTG_FORMAT_BC3 && format != NTG_FORMAT_BC4 &&
+        format != NTG_FORMAT_BC5)
+        return report(NTG_ERROR_UNSUPPORTED_FEATURE, "format not supported (BC1, BC1a, BC3, BC4, BC5)");
     if (quality < 0 || quality > 3 || out_xform < 0 || out_xform > 2)
         return report(NTG_ERROR_INVALID_INPUT, "bad quality or colour transform");
+    if (format == NTG_FORMAT_BC1A && quality == NTG_QUALITY_FASTEST)
+        return report(NTG_ERROR_UNSUPPORTED_FEATURE, "BC1a at Fastest quality is not supported (use Normal or above)");
     // Surface::toGamma returns early for gamma == 1 (src/nvtt/Surface.cpp:1480-1488)
     const bool unit = std::fabs(gamma - 1.0f) <= 0.0001f * std::fmax(1.0f, std::fabs(gamma));
     if (out_xform == NTG_XFORM_GAMMA && unit) out_xform = NTG_XFORM_NONE;
@@ -134,8 +137,10 @@ extern "C" int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_r
     if (cudaMemcpyAsync(d_job, &j, sizeof j, cudaMemcpyHostToDevice, s) != cudaSuccess)
         return report_status(ntg::launch_status(), "copy of the job record");
     const long long nblocks = (long long)((w + 3) / 4) * ((h + 3) / 4);
-    st = format == NTG_FORMAT_BC1 ? ntg::launch_bc1(d_job, 1, nblocks, quality, 0, s)
-         : format == NTG_FORMAT_BC3 ? ntg::launch_bc3(d_job, 1, nblocks, quality, 0, s)
-                                    : ntg::launch_bc5(d_job, 1, nblocks, quality, 0, s);
+    st = format == NTG_FORMAT_BC1    ? ntg::launch_bc1(d_job, 1, nblocks, quality, 0, s)
+         : format == NTG_FORMAT_BC3  ? ntg::launch_bc3(d_job, 1, nblocks, quality, 0, s)
+         : format == NTG_FORMAT_BC1A ? ntg::launch_bc1a(d_job, 1, nblocks, quality, 0, s)
+         : format == NTG_FORMAT_BC4  ? ntg::launch_bc4(d_job, 1, nblocks, quality, 0, s)
+                                     : ntg::launch_bc5(d_job, 1, nblocks, quality, 0, s);
     return report_status(st, "encoder launch");
 }

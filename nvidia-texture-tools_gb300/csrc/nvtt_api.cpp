@@ -62,12 +62,14 @@ Buf make_buf(size_t bytes) {
     return b->p ? b : nullptr;
 }
 
-int block_bytes(nvtt::Format f) { return f == nvtt::Format_BC1 ? 8 : 16; }
+int block_bytes(nvtt::Format f) { return f == nvtt::Format_BC1 || f == nvtt::Format_BC1a || f == nvtt::Format_BC4 ? 8 : 16; }
 long long blocks_of(int w, int h) { return (long long)((w + 3) / 4) * ((h + 3) / 4); }
 
 int ntg_format(nvtt::Format f) {
     if (f == nvtt::Format_BC1) return NTG_FORMAT_BC1;
+    if (f == nvtt::Format_BC1a) return NTG_FORMAT_BC1A;
     if (f == nvtt::Format_BC3) return NTG_FORMAT_BC3;
+    if (f == nvtt::Format_BC4) return NTG_FORMAT_BC4;
     if (f == nvtt::Format_BC5) return NTG_FORMAT_BC5;
     return -1;
 }
@@ -427,10 +429,11 @@ bool Surface::setImage(InputFormat format, int w, int h, int d, const void *r, c
     return true;
 }
 
-// Surface::setImage2D (src/nvtt/Surface.cpp:908-1116), D3D10 decoder, BC1/BC3/BC5.
+// Surface::setImage2D (src/nvtt/Surface.cpp:908-1116), D3D10 decoder, BC1/BC3/BC4/BC5 (the
+// reference refuses BC1a here).
 bool Surface::setImage2D(Format format, Decoder, int w, int h, const void *data) {
     const int f = ntg_format(format);
-    if (f < 0 || w <= 0 || h <= 0 || !data || !global_ctx()) return false;
+    if (f < 0 || format == Format_BC1a || w <= 0 || h <= 0 || !data || !global_ctx()) return false;
     const size_t bytes = (size_t)blocks_of(w, h) * block_bytes(format);
     Buf blocks = make_buf(bytes), b = make_buf((size_t)w * h * 4 * sizeof(float));
     if (!blocks || !b || cudaMemcpy(blocks->p, data, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return false;
@@ -555,7 +558,7 @@ bool dds_header(Format format, int w, int h, int mipmapCount, bool isNormalMap, 
     enum : uint32_t {
         CAPS = 0x1, HEIGHT = 0x2, WIDTH = 0x4, PIXELFORMAT = 0x1000, MIPMAPCOUNT = 0x20000, LINEARSIZE = 0x80000,
         CAPS_COMPLEX = 0x8, CAPS_TEXTURE = 0x1000, CAPS_MIPMAP = 0x400000,
-        PF_FOURCC = 0x4, PF_NORMAL = 0x80000000u, PF_SRGB = 0x40000000u,
+        PF_ALPHAPIXELS = 0x1, PF_FOURCC = 0x4, PF_NORMAL = 0x80000000u, PF_SRGB = 0x40000000u,
     };
     words.assign(37, 0);                            // magic + 124-byte header + 20-byte DX10 extension
     words[0] = fourcc('D', 'D', 'S', ' ');
@@ -580,16 +583,22 @@ bool dds_header(Format format, int w, int h, int mipmapCount, bool isNormalMap, 
     if (oo.container == Container_DDS10) {
         pf[1] = PF_FOURCC;
         pf[2] = fourcc('D', 'X', '1', '0');
-        if (format == Format_BC1) { h10[0] = oo.srgb ? 72 : 71; if (isNormalMap) pf[1] |= PF_NORMAL; }
+        if (format == Format_BC1 || format == Format_BC1a) {
+            h10[0] = oo.srgb ? 72 : 71;
+            if (format == Format_BC1a) pf[1] |= PF_ALPHAPIXELS;
+            if (isNormalMap) pf[1] |= PF_NORMAL;
+        }
         else if (format == Format_BC3) h10[0] = oo.srgb ? 78 : 77;
+        else if (format == Format_BC4) h10[0] = 80;
         else if (format == Format_BC5) { h10[0] = 83; if (isNormalMap) pf[1] |= PF_NORMAL; }
         else return false;
     } else {
         flags |= LINEARSIZE;
         words[5] = (uint32_t)(blocks_of(w, h) * block_bytes(format));
         pf[1] = PF_FOURCC;
-        if (format == Format_BC1) { pf[2] = fourcc('D', 'X', 'T', '1'); if (isNormalMap) pf[1] |= PF_NORMAL; }
+        if (format == Format_BC1 || format == Format_BC1a) { pf[2] = fourcc('D', 'X', 'T', '1'); if (isNormalMap) pf[1] |= PF_NORMAL; }
         else if (format == Format_BC3) pf[2] = fourcc('D', 'X', 'T', '5');
+        else if (format == Format_BC4) pf[2] = fourcc('A', 'T', 'I', '1');
         else if (format == Format_BC5) {
             pf[2] = fourcc('A', 'T', 'I', '2');
             if (isNormalMap) { pf[1] |= PF_NORMAL; pf[3] = fourcc('A', '2', 'X', 'Y'); }

@@ -13,14 +13,14 @@ import numpy as np
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "_build", "libntg.so")
 
-FORMAT_BC1, FORMAT_BC3, FORMAT_BC5 = 1, 4, 7
+FORMAT_BC1, FORMAT_BC1A, FORMAT_BC3, FORMAT_BC4, FORMAT_BC5 = 1, 2, 4, 6, 7
 QUALITY_FASTEST, QUALITY_NORMAL, QUALITY_PRODUCTION, QUALITY_HIGHEST = 0, 1, 2, 3
 WRAP_CLAMP, WRAP_REPEAT, WRAP_MIRROR = 0, 1, 2
 FILTER_BOX, FILTER_TRIANGLE, FILTER_KAISER = 0, 1, 2
 ALPHA_NONE, ALPHA_TRANSPARENCY = 0, 1
 XFORM_NONE, XFORM_GAMMA, XFORM_SRGB = 0, 1, 2
 
-BLOCK_BYTES = {FORMAT_BC1: 8, FORMAT_BC3: 16, FORMAT_BC5: 16}
+BLOCK_BYTES = {FORMAT_BC1: 8, FORMAT_BC1A: 8, FORMAT_BC3: 16, FORMAT_BC4: 8, FORMAT_BC5: 16}
 
 _vp, _i, _f, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_size_t
 

@@ -145,7 +145,7 @@ def write_dds_fixtures(R):
         out[f"params_{i}"] = np.array(json.dumps(case))
         out[f"input_{i}"] = data
         out[f"dds_{i}"] = res if isinstance(res, np.ndarray) else np.array([res], np.int64)
-        if case.get("input_format", 0) == 0 and case["format"] in (1, 4, 7):
+        if case.get("input_format", 0) == 0 and case["format"] in (1, 4, 6, 7):
             # rmsError / rmsAlphaError of level 0 encoded without transforms, against its input
             w, h = case["w"], case["h"]
             bgra = data[:4 * w * h].reshape(h, w, 4)
@@ -158,7 +158,8 @@ def write_dds_fixtures(R):
 
 
 # Compressor::process cases for the nvtt:: drop-in API: containers, header flags, filters, gammas,
-# source mipmaps, float input, and one format the DDS container rejects (BC7 -> Error 6).
+# source mipmaps, float input, one format the DDS container rejects (BC7 -> Error 6), and BC1a /
+# BC4 (BC4 at Normal and Fastest only: the reference's Production BC4 varies from run to run).
 DDS_CASES = [
     dict(w=61, h=37, format=1, quality=1, mip_filter=0),
     dict(w=64, h=64, format=4, quality=1, mip_filter=2, alpha_mode=1, srgb=1, version=7),
@@ -172,6 +173,10 @@ DDS_CASES = [
     dict(w=3, h=5, format=1, quality=1),
     dict(w=20, h=12, format=7, quality=1, mip_filter=0, normal_map=1, normalize_mips=0),
     dict(w=16, h=16, format=11, quality=1),
+    dict(w=40, h=28, format=2, quality=1, mip_filter=2, alpha_mode=1),
+    dict(w=32, h=20, format=2, quality=2, container=1, srgb=1),
+    dict(w=36, h=36, format=6, quality=1, mip_filter=1),
+    dict(w=16, h=24, format=6, quality=0, container=1),
 ]
 
 

@@ -42,6 +42,9 @@ MIXED = [
     (64, 64, 4, 1, 2, 1, 0, 0, 2, 1),     # alpha-weighted Kaiser taps
     (128, 32, 1, 1, 1, 1, 2, 2, 2, 1),    # alpha-weighted triangle, BC1 + sRGB
     (256, 128, 1, 1, 2, 0, 2, 2, 0, 0),   # Kaiser clamp, BC1 + sRGB
+    (128, 64, 2, 1, 2, 1, 2, 2, 2, 0),    # BC1a, Kaiser / sRGB / transparency
+    (64, 64, 6, 1, 1, 0, 0, 0, 2, 0),     # BC4, triangle
+    (32, 48, 6, 2, 0, 0, 0, 0, 2, 0),     # BC4 Production, box
 ]
 
 

@@ -83,6 +83,68 @@ def test_bc5_encode_matches_oracle(ctx, oracle, quality):
             assert np.array_equal(ours, oracle.bc5_image(img, w, h, quality, threads=4))
 
 
+@pytest.mark.parametrize("quality", [1, 2, 3])
+@pytest.mark.parametrize("alpha_mode", [0, 1])
+def test_bc1a_encode_matches_oracle(ctx, oracle, quality, alpha_mode):
+    """CompressorDXT1a: three-colour fit with transparent texels (alpha 0 after ColorBlock's
+    truncation), four-colour fit as well where there are none."""
+    for (w, h, seed) in [(64, 32, 1), (13, 7, 2), (3, 5, 3), (1, 1, 4)]:
+        for img in (float_image(w, h, seed, alpha_zero_frac=0.3), blocky_image(w, h, seed + 20),
+                    float_image(w, h, seed + 5, lo=-0.3, hi=1.4), float_image(w, h, seed + 8, alpha_zero_frac=1.0)):
+            ours = host(ctx.encode(ntg.FORMAT_BC1A, dev(img), w, h, quality=quality, alpha_mode=alpha_mode))
+            ref = oracle.bc1a_image(img, w, h, alpha_mode, threads=4)
+            assert np.array_equal(ours, ref), (w, h, seed)
+
+
+def test_bc1a_colour_weights(ctx, oracle):
+    w, h = 32, 16
+    img = float_image(w, h, 78, alpha_zero_frac=0.25)
+    for cw in [(0.3, 0.59, 0.11), (2.0, 0.5, 1.0)]:
+        ours = host(ctx.encode(ntg.FORMAT_BC1A, dev(img), w, h, quality=1, cw=cw))
+        assert np.array_equal(ours, oracle.bc1a_image(img, w, h, 0, cw=cw, threads=4))
+
+
+def test_bc1a_fastest_is_refused(ctx):
+    with pytest.raises(ntg.NtgError) as e:
+        ctx.encode(ntg.FORMAT_BC1A, dev(np.zeros(64, np.float32)), 4, 4, quality=0)
+    assert e.value.code == 2
+
+
+@pytest.mark.parametrize("quality", [0, 1, 2, 3])
+def test_bc4_encode_matches_oracle(ctx, oracle, quality):
+    for (w, h, seed) in [(64, 32, 1), (13, 7, 2), (1, 3, 3)]:
+        for img in (float_image(w, h, seed), blocky_image(w, h, seed + 7)):
+            ours = host(ctx.encode(ntg.FORMAT_BC4, dev(img), w, h, quality=quality))
+            assert np.array_equal(ours, oracle.bc4_image(img, w, h, quality, threads=4))
+
+
+def _tiled(blocks64):
+    """BGRA8 image whose 4x4 blocks, in raster order, are the given 64-byte blocks (one row of blocks)."""
+    n = len(blocks64)
+    b = np.asarray(blocks64, np.uint8).reshape(n, 4, 4, 4)
+    return np.ascontiguousarray(b.transpose(1, 0, 2, 3).reshape(4, 4 * n, 4))
+
+
+def test_bc1a_bc4_golden_blocks(ctx):
+    """The reference's own BC1a and BC4 blocks (tests/golden/bc1a_bc4_blocks.npz), encoded here from
+    the same bytes through the 8-bit path of a one-level chain."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "bc1a_bc4_blocks.npz"))
+    inputs = g["inputs"]
+    img = _tiled(inputs)
+    w, h = 4 * len(inputs), 4
+    for key in g.files:
+        if key == "inputs":
+            continue
+        kind, param = key.split("_")
+        if kind == "bc1a":
+            opt = ntg.ChainOptions.make(format=ntg.FORMAT_BC1A, quality=1, alpha_mode=int(param), max_levels=1)
+        else:
+            opt = ntg.ChainOptions.make(format=ntg.FORMAT_BC4, quality=int(param), max_levels=1)
+        out = host(ctx.compress_chain(dev(img), w, h, opt)).reshape(-1, 8)
+        assert np.array_equal(out, g[key]), key
+
+
 @pytest.mark.parametrize("fmt", [ntg.FORMAT_BC1, ntg.FORMAT_BC3])
 @pytest.mark.parametrize("out_xform", [ntg.XFORM_GAMMA, ntg.XFORM_SRGB])
 def test_encode_with_output_transform(ctx, oracle, fmt, out_xform):
@@ -144,6 +206,10 @@ CHAINS = [
     (1, 64, 4, 1, 0, 1, 0, 0, 2),       # 1-D, box polyphase (transparency)
     (64, 1, 1, 0, 0, 0, 0, 0, 2),       # 1-D fast box, range fit
     (31, 31, 4, 3, 2, 0, 2, 2, 1),      # odd, Highest quality alpha
+    (96, 64, 2, 1, 2, 1, 2, 2, 2),      # BC1a, Kaiser/sRGB, transparency
+    (45, 27, 2, 2, 0, 0, 0, 0, 1),      # BC1a, box, odd sizes
+    (64, 48, 6, 1, 1, 0, 0, 0, 2),      # BC4, triangle
+    (37, 37, 6, 2, 2, 0, 1, 1, 0),      # BC4 Production, Kaiser, gamma
 ]
 
 
@@ -156,6 +222,10 @@ def oracle_chain(oracle, bgra, w, h, fmt, quality, filt, am, ix, ox, wrap):
         flat = l.reshape(-1)
         if fmt == 1:
             out.append(oracle.bc1_image(flat, lw, lh, am, quality, threads=8))
+        elif fmt == 2:
+            out.append(oracle.bc1a_image(flat, lw, lh, am, threads=8))
+        elif fmt == 6:
+            out.append(oracle.bc4_image(flat, lw, lh, quality, threads=8))
         elif fmt == 4:
             out.append(oracle.bc3_image(flat, lw, lh, am, quality, threads=8))
         else:
@@ -204,11 +274,13 @@ def test_chain_golden_fixture(ctx):
 # ---------------------------------------------------------------------------------------------
 # decode and error
 
-@pytest.mark.parametrize("fmt", [1, 4, 7])
+@pytest.mark.parametrize("fmt", [1, 2, 4, 6, 7])
 def test_decode_and_error_sums(ctx, oracle, fmt):
     w, h = 45, 27
-    img = float_image(w, h, fmt)
-    blocks = oracle.bc1_image(img, w, h) if fmt == 1 else (oracle.bc3_image(img, w, h, 1) if fmt == 4 else oracle.bc5_image(img, w, h))
+    img = float_image(w, h, fmt, alpha_zero_frac=0.2)
+    blocks = {1: lambda: oracle.bc1_image(img, w, h), 2: lambda: oracle.bc1a_image(img, w, h),
+              4: lambda: oracle.bc3_image(img, w, h, 1), 6: lambda: oracle.bc4_image(img, w, h),
+              7: lambda: oracle.bc5_image(img, w, h)}[fmt]()
     dec = host(ctx.decode(fmt, dev(blocks), w, h))
     assert np.array_equal(dec.view(np.uint32), oracle.decode(fmt, blocks, w, h).view(np.uint32))
     am = 1 if fmt == 4 else 0
@@ -222,7 +294,7 @@ def test_decode_and_error_sums(ctx, oracle, fmt):
 # errors are reported, not hidden
 
 def test_invalid_arguments_report_errors(ctx):
-    opt = ntg.ChainOptions.make(format=2)  # BC1a is outside the path
+    opt = ntg.ChainOptions.make(format=3)  # BC2 (DXT3) is outside the path
     with pytest.raises(ntg.NtgError) as e:
         ctx.compress_chain(dev(np.zeros((4, 4, 4), np.uint8)), 4, 4, opt)
     assert e.value.code == 2
