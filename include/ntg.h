@@ -80,6 +80,20 @@ unsigned long long ntg_launch_count(void);
 int ntg_set_image_bgra8(ntg_context *ctx, const void *d_bgra, int w, int h, int in_xform, float gamma,
                         float *d_rgba, void *stream);
 
+/* Surface::resize(w, h, 1, filter, width, params) (src/nvtt/Surface.cpp:1152-1230) of a planar FP32
+ * image w x h into dw x dh (FloatImage::resize, src/nvimage/FloatImage.cpp:761-808, 877-925: X pass,
+ * then Y pass, any scale, up or down). filter 0 box / 1 triangle / 2 kaiser (Mitchell is not
+ * supported); width 0 picks getDefaultFilterWidthAndParams (src/nvtt/Surface.cpp:1121-1141). Equal
+ * extents copy the image unchanged, as Surface::resize returns early. Uses the context workspace
+ * for the intermediate dw x h plane. */
+int ntg_resize(ntg_context *ctx, const float *d_src, int w, int h, float *d_dst, int dw, int dh, int filter, float width,
+               const float *params, int wrap, int alpha_mode, void *stream);
+
+/* nv::getTargetExtent (src/nvtt/Surface.cpp:220-326) for a 2D texture: the level-0 extent that
+ * Compressor::process resizes to for InputOptions::setMaxExtent / setRoundMode (round_mode is an
+ * nvtt::RoundMode). A result may be 0 (ToPreviousMultipleOfFour below 4), as in the reference. */
+int ntg_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, int *out_h);
+
 /* Surface::buildNextMipmap (src/nvtt/Surface.cpp:1344-1406): one level down from a planar FP32
  * level to max(1, w/2) x max(1, h/2). params = {kaiser alpha, kaiser stretch} (ignored otherwise).
  * weighted != 0 selects the alpha-weighted kernels of FloatImage::applyKernelX/Y

@@ -254,6 +254,14 @@ struct Surface {
     bool setImage(InputFormat format, int w, int h, int d, const void *r, const void *g, const void *b, const void *a);
     bool setImage2D(Format format, Decoder decoder, int w, int h, const void *data);
 
+    // Resizing (Surface::resize, src/nvtt/Surface.cpp:1143-1268): box, triangle and Kaiser filters;
+    // Mitchell leaves the surface unchanged and reports nothing, as there is no error channel here.
+    void resize(int w, int h, int d, ResizeFilter filter);
+    void resize(int w, int h, int d, ResizeFilter filter, float filterWidth, const float *params = 0);
+    void resize(int maxExtent, RoundMode mode, ResizeFilter filter);
+    void resize(int maxExtent, RoundMode mode, ResizeFilter filter, float filterWidth, const float *params = 0);
+    void resizeMakeSquare(int maxExtent, RoundMode roundMode, ResizeFilter filter);
+
     bool buildNextMipmap(MipmapFilter filter, int min_size = 1);
     bool buildNextMipmap(MipmapFilter filter, float filterWidth, const float *params = 0, int min_size = 1);
     bool canMakeNextMipmap(int min_size = 1);

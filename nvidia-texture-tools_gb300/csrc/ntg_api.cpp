@@ -629,6 +629,67 @@ int ntg_mip_level(ntg_context *ctx, const float *d_src, int w, int h, float *d_d
     return run_stages(stages, ctx->d_mipjobs, s);
 }
 
+int ntg_resize(ntg_context *ctx, const float *d_src, int w, int h, float *d_dst, int dw, int dh, int filter, float width,
+               const float *params, int wrap, int alpha_mode, void *stream) {
+    g_error.clear();
+    if (!ctx || !d_src || !d_dst || w <= 0 || h <= 0 || dw <= 0 || dh <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    if (filter < 0 || filter > 2) return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "resize filter not supported (box, triangle, kaiser)");
+    if (wrap < 0 || wrap > 2 || alpha_mode < 0 || alpha_mode > 2) return fail(NTG_ERROR_INVALID_INPUT, "bad wrap or alpha mode");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    cudaStream_t s = S(stream);
+    if (dw == w && dh == h) {  // Surface::resize returns early: the image is unchanged
+        if (d_dst != d_src) NTG_CUDA(cudaMemcpyAsync(d_dst, d_src, (size_t)w * h * 4 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        return NTG_OK;
+    }
+    ntg_chain_options o;
+    std::memset(&o, 0, sizeof o);
+    o.filter = filter; o.filter_width = width;
+    if (params) { o.params[0] = params[0]; o.params[1] = params[1]; }
+    float fw, p[2];
+    filter_defaults(o, fw, p);
+    const AxisTable *ax = ctx->axis(filter, fw, p[0], p[1], w, dw);
+    const AxisTable *ay = ctx->axis(filter, fw, p[0], p[1], h, dh);
+    if (!ax || !ay) return fail(NTG_ERROR_CUDA, "polyphase table upload failed");
+    uint8_t *tmp = nullptr;
+    NTG_TRY(ctx->workspace((size_t)dw * h * 4 * sizeof(float), s, &tmp));
+    return launched(launch_resize(d_src, w, h, (float *)tmp, dw, dh, ax->d_w, ax->d_left, ax->ws, ay->d_w, ay->d_left,
+                                  ay->ws, wrap, d_dst, s), "resize");
+}
+
+// nv::getTargetExtent (src/nvtt/Surface.cpp:220-326), 2D, no shape restriction, with the rounding
+// helpers of src/nvtt/Surface.cpp:60-105. Its else-if chain tests RoundMode_ToNextMultipleOfFour
+// twice, so RoundMode_ToNearestMultipleOfFour leaves the extents unchanged; kept that way.
+int ntg_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, int *out_h) {
+    g_error.clear();
+    if (w <= 0 || h <= 0 || !out_w || !out_h || round_mode < 0 || round_mode > 6)
+        return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    auto next_pow2 = [](unsigned x) {
+        x--;
+        x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
+        return x + 1;
+    };
+    auto prev_pow2 = [&](unsigned v) { return next_pow2(v + 1) / 2; };
+    auto nearest_pow2 = [&](unsigned v) {
+        const unsigned up = next_pow2(v), down = prev_pow2(v);
+        return up - v <= v - down ? up : down;
+    };
+    if (round_mode != 0 && max_extent > 0) max_extent = (int)prev_pow2((unsigned)max_extent);
+    const int m = std::max(w, h);
+    if (max_extent > 0 && m > max_extent) {
+        w = std::max((w * max_extent) / m, 1);
+        h = std::max((h * max_extent) / m, 1);
+    }
+    if (round_mode == 1) { w = (int)next_pow2((unsigned)w); h = (int)next_pow2((unsigned)h); }
+    else if (round_mode == 2) { w = (int)nearest_pow2((unsigned)w); h = (int)nearest_pow2((unsigned)h); }
+    else if (round_mode == 3) { w = (int)prev_pow2((unsigned)w); h = (int)prev_pow2((unsigned)h); }
+    else if (round_mode == 4) { w = (w + 3) & ~3; h = (h + 3) & ~3; }
+    else if (round_mode == 6) { w &= ~3; h &= ~3; }
+    *out_w = w;
+    *out_h = h;
+    return NTG_OK;
+}
+
 int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,
                int out_xform, float gamma, const float *cw, void *d_blocks, void *stream) {
     g_error.clear();

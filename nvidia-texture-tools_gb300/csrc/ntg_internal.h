@@ -46,6 +46,9 @@ int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, 
 int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 int launch_bc1a(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
+// Separable polyphase resize of a planar FP32 image (two launches through `tmp`, w * H * 16 bytes).
+int launch_resize(const float *src, int W, int H, float *tmp, int w, int h, const float *kx, const int *lx, int wsx,
+                  const float *ky, const int *ly, int wsy, int wrap, float *dst, cudaStream_t s);
 int launch_bc4(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 
 // Learned endpoint proposal, BC1 Normal quality: the network's inputs (x [nblocks x 48]), training

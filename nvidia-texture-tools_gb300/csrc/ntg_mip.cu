@@ -670,6 +670,62 @@ static int launch_poly2x_ws(const MipLaunch &m, const MipJob *jobs, cudaStream_t
 
 bool poly2x_supported(int ws) { return ws == 3 || ws == 5 || ws == 13; }
 
+// ---------------------------------------------------------------------------------------------
+// Surface::resize (src/nvtt/Surface.cpp:1152-1230) -> FloatImage::resize (src/nvimage/FloatImage.cpp:
+// 761-808, and the alpha-first variant :877-925, which computes every channel the same way): the X
+// pass into a w x H planar buffer, then the Y pass, taps summed in window order
+// (applyKernelX/Y, :1115-1176). One thread per texel; any scale and window, so it also covers the
+// ratios whose tiles would not fit the mip kernels' shared memory. Used once per texture, for the
+// InputOptions resize step.
+__global__ void k_resize_x(const float *__restrict__ src, int W, int H, const float *__restrict__ kx,
+                           const int *__restrict__ lx, int ws, int wrap, float *__restrict__ tmp, int w) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n = (long long)w * H;
+    if (i >= n) return;
+    const int x = (int)(i % w), y = (int)(i / w);
+    const size_t sn = (size_t)W * H;
+    const float *k = kx + (size_t)x * ws;
+    const int left = lx[x];
+    float4 sum = make_float4(0, 0, 0, 0);
+    float norm = 0;
+    for (int j = 0; j < ws; j++) {
+        const size_t s = (size_t)y * W + wrap_index(left + j, W, wrap);
+        tap<false>(sum, norm, __ldg(k + j), make_float4(__ldg(src + s), __ldg(src + sn + s), __ldg(src + 2 * sn + s),
+                                                        __ldg(src + 3 * sn + s)));
+    }
+    tmp[i] = sum.x; tmp[n + i] = sum.y; tmp[2 * n + i] = sum.z; tmp[3 * n + i] = sum.w;
+}
+
+__global__ void k_resize_y(const float *__restrict__ tmp, int w, int H, const float *__restrict__ ky,
+                           const int *__restrict__ ly, int ws, int wrap, float *__restrict__ dst, int h) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n = (long long)w * h;
+    if (o >= n) return;
+    const int x = (int)(o % w), y = (int)(o / w);
+    const size_t tn = (size_t)w * H;
+    const float *k = ky + (size_t)y * ws;
+    const int left = ly[y];
+    float4 sum = make_float4(0, 0, 0, 0);
+    float norm = 0;
+    for (int j = 0; j < ws; j++) {
+        const size_t s = (size_t)wrap_index(left + j, H, wrap) * w + x;
+        tap<false>(sum, norm, __ldg(k + j), make_float4(__ldg(tmp + s), __ldg(tmp + tn + s), __ldg(tmp + 2 * tn + s),
+                                                        __ldg(tmp + 3 * tn + s)));
+    }
+    dst[o] = sum.x; dst[n + o] = sum.y; dst[2 * n + o] = sum.z; dst[3 * n + o] = sum.w;
+}
+
+int launch_resize(const float *src, int W, int H, float *tmp, int w, int h, const float *kx, const int *lx, int wsx,
+                  const float *ky, const int *ly, int wsy, int wrap, float *dst, cudaStream_t s) {
+    const long long nt = (long long)w * H, nd = (long long)w * h;
+    if (nt == 0 || nd == 0) return 0;
+    k_resize_x<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(src, W, H, kx, lx, wsx, wrap, tmp, w);
+    const int st = launch_status();
+    if (st) return st;
+    k_resize_y<<<(unsigned)((nd + 255) / 256), 256, 0, s>>>(tmp, w, H, ky, ly, wsy, wrap, dst, h);
+    return launch_status();
+}
+
 size_t poly_smem_bytes(int rx_max, int ry_max) {
     return (size_t)ry_max * rx_max * sizeof(float4) + (size_t)ry_max * PTW * sizeof(float4) +
            (size_t)(rx_max + ry_max) * sizeof(int);

@@ -473,6 +473,59 @@ bool Surface::buildNextMipmap(MipmapFilter filter, float filterWidth, const floa
     return true;
 }
 
+// getDefaultFilterWidthAndParams (src/nvtt/Surface.cpp:1121-1141) for the resize filters.
+static void resize_defaults(ResizeFilter filter, float &width, float params[2]) {
+    width = filter == ResizeFilter_Box ? 0.5f : filter == ResizeFilter_Triangle ? 1.0f : filter == ResizeFilter_Kaiser ? 3.0f : 2.0f;
+    params[0] = filter == ResizeFilter_Mitchell ? 1.0f / 3.0f : 4.0f;
+    params[1] = filter == ResizeFilter_Mitchell ? 1.0f / 3.0f : 1.0f;
+}
+
+void Surface::resize(int w, int h, int d, ResizeFilter filter) {
+    float width, params[2];
+    resize_defaults(filter, width, params);
+    resize(w, h, d, filter, width, params);
+}
+
+// Surface::resize(w, h, d, filter, filterWidth, params) (src/nvtt/Surface.cpp:1152-1230).
+void Surface::resize(int w, int h, int d, ResizeFilter filter, float filterWidth, const float *params) {
+    if (!m->data || (w == m->w && h == m->h && d == 1) || d != 1 || w <= 0 || h <= 0 || filter == ResizeFilter_Mitchell ||
+        !global_ctx())
+        return;
+    if (!m->materialize()) return;
+    Buf b = make_buf((size_t)w * h * 4 * sizeof(float));
+    if (!b) return;
+    float p[2] = {4.0f, 1.0f};
+    if (params) { p[0] = params[0]; p[1] = params[1]; }
+    if (ntg_resize(global_ctx(), m->dev(), m->w, m->h, (float *)b->p, w, h, (int)filter, filterWidth, p, (int)m->wrapMode,
+                   (int)m->alphaMode, nullptr) != NTG_OK || cudaDeviceSynchronize() != cudaSuccess)
+        return;
+    m->w = w; m->h = h; m->data = b; m->src8.reset(); m->hostValid = false;
+}
+
+void Surface::resize(int maxExtent, RoundMode mode, ResizeFilter filter) {
+    float width, params[2];
+    resize_defaults(filter, width, params);
+    resize(maxExtent, mode, filter, width, params);
+}
+
+void Surface::resize(int maxExtent, RoundMode mode, ResizeFilter filter, float filterWidth, const float *params) {
+    if (!m->data) return;
+    int w = 0, h = 0;
+    if (ntg_target_extent(m->w, m->h, maxExtent, (int)mode, &w, &h) != NTG_OK) return;
+    resize(w, h, 1, filter, filterWidth, params);
+}
+
+// Surface::resizeMakeSquare (src/nvtt/Surface.cpp:1220-1246): the target extent, squared to the smaller side.
+void Surface::resizeMakeSquare(int maxExtent, RoundMode roundMode, ResizeFilter filter) {
+    if (!m->data) return;
+    float width, params[2];
+    resize_defaults(filter, width, params);
+    int w = 0, h = 0;
+    if (ntg_target_extent(m->w, m->h, maxExtent, (int)roundMode, &w, &h) != NTG_OK) return;
+    const int md = std::min(w, h);
+    resize(md, md, 1, filter, width, params);
+}
+
 void Surface::toLinear(float gamma) {
     if (!m->data || nv_equal(gamma, 1.0f)) return;
     if (!m->materialize()) return;
@@ -683,10 +736,15 @@ int Compressor::estimateSize(int w, int h, int d, int mipmapCount, const Compres
 int Compressor::estimateSize(const Surface &img, int mipmapCount, const CompressionOptions &co) const {
     return estimateSize(img.width(), img.height(), 1, mipmapCount, co);
 }
+// Compressor::estimateSize(InputOptions) (src/nvtt/Context.cpp:122-137), at the target extent.
 int Compressor::estimateSize(const InputOptions &io, const CompressionOptions &co) const {
-    int mc = io.m.generateMipmaps ? count_mipmaps(io.m.width, io.m.height) : 1;
+    int w = io.m.width, h = io.m.height;
+    if (w <= 0 || h <= 0 || ntg_target_extent(io.m.width, io.m.height, io.m.maxExtent, (int)io.m.roundMode, &w, &h) != NTG_OK ||
+        w <= 0 || h <= 0)
+        return 0;
+    int mc = io.m.generateMipmaps ? count_mipmaps(w, h) : 1;
     if (io.m.generateMipmaps && io.m.maxLevel > 0) mc = std::min(mc, io.m.maxLevel);
-    return io.m.faceCount * estimateSize(io.m.width, io.m.height, io.m.depth, mc, co);
+    return io.m.faceCount * estimateSize(w, h, io.m.depth, mc, co);
 }
 
 bool Compressor::outputHeader(TextureType type, int w, int h, int d, int arraySize, int mipmapCount, bool isNormalMap,
@@ -720,18 +778,25 @@ bool Compressor::process(const InputOptions &inputOptions, const CompressionOpti
     const OutputOptions::Private &oo = outputOptions.m;
     if (!oo.hasValidOutputHandler()) { oo.error(Error_FileOpen); return false; }
     if (!m.ctx) { oo.error(Error_CudaError); return false; }
-    const int w = io.width, h = io.height;
+    // the InputOptions resize step: nv::getTargetExtent, then Surface::resize(box) of level 0
+    int w = io.width, h = io.height;
+    if (io.width <= 0 || io.height <= 0 || ntg_target_extent(io.width, io.height, io.maxExtent, (int)io.roundMode, &w, &h) != NTG_OK) {
+        oo.error(Error_InvalidInput);
+        return false;
+    }
+    const bool resized = w != io.width || h != io.height;
     int mipmapCount = 1;
     if (io.generateMipmaps) {
         mipmapCount = count_mipmaps(w, h);
         if (io.maxLevel > 0) mipmapCount = std::min(mipmapCount, io.maxLevel);
     }
     if (!m.outputHeader(io.textureType, w, h, io.depth, 1, mipmapCount, io.isNormalMap, co, oo)) return false;
-    // outside this path: input resizing, normal-map generation / renormalisation, dithering, 3D/cube
+    // (an extent rounded to 0, ToPreviousMultipleOfFour below 4 texels, fails in outputHeader with
+    // Error_InvalidInput, as in the reference)
+    // outside this path: normal-map generation / renormalisation, dithering, 3D/cube
     const bool normalMips = io.isNormalMap && io.normalizeMipmaps && mipmapCount > 1;
-    if (io.textureType != TextureType_2D || io.depth != 1 || io.convertToNormalMap || normalMips || io.maxExtent > 0 ||
-        io.roundMode != RoundMode_None || co.colorDithering || co.alphaDithering || co.binaryAlpha ||
-        ntg_format(co.format) < 0) {
+    if (io.textureType != TextureType_2D || io.depth != 1 || io.convertToNormalMap || normalMips ||
+        co.colorDithering || co.alphaDithering || co.binaryAlpha || ntg_format(co.format) < 0) {
         oo.error(Error_UnsupportedFeature);
         return false;
     }
@@ -746,7 +811,7 @@ bool Compressor::process(const InputOptions &inputOptions, const CompressionOpti
         if (base.empty()) { oo.error(Error_InvalidInput); return false; }
         bool sourceMips = false;
         for (int l = 1; l < mipmapCount; l++) sourceMips = sourceMips || !io.images[(size_t)l * io.faceCount + f].empty();
-        if (!sourceMips && io.inputFormat == InputFormat_BGRA_8UB) {
+        if (!sourceMips && !resized && io.inputFormat == InputFormat_BGRA_8UB) {
             // the whole chain in one fused call: levels stay in GPU memory, one encoder launch
             ntg_chain_options opt;
             std::memset(&opt, 0, sizeof opt);
@@ -781,14 +846,18 @@ bool Compressor::process(const InputOptions &inputOptions, const CompressionOpti
             }
             continue;
         }
-        // float input or some source mipmaps supplied: the reference's level loop, step by step
+        // float input, source mipmaps or a resize: the reference's level loop, step by step
         Surface img;
         img.setWrapMode(io.wrapMode);
         img.setAlphaMode(io.alphaMode);
         img.setNormalMap(io.isNormalMap);
-        if (!img.setImage(io.inputFormat, w, h, 1, base.data())) { oo.error(Error_CudaError); return false; }
+        if (!img.setImage(io.inputFormat, io.width, io.height, 1, base.data())) { oo.error(Error_CudaError); return false; }
         if (!linearIn) img.toLinear(io.inputGamma);
-        bool useSource = true;
+        if (resized) {
+            img.resize(w, h, 1, ResizeFilter_Box);
+            if (img.width() != w || img.height() != h) { oo.error(Error_CudaError); return false; }
+        }
+        bool useSource = !resized;  // source mipmaps only when the extents are unchanged
         for (int l = 0; l < mipmapCount; l++) {
             if (l > 0) {
                 const std::vector<unsigned char> &src = io.images[(size_t)l * io.faceCount + f];

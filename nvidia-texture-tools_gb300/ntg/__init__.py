@@ -82,6 +82,8 @@ def lib():
         "ntg_destroy": (_i, [_vp]),
         "ntg_set_image_bgra8": (_i, [_vp, _vp, _i, _i, _i, _f, _vp, _vp]),
         "ntg_mip_level": (_i, [_vp, _vp, _i, _i, _vp, _i, _f, _vp, _i, _i, _i, _vp]),
+        "ntg_resize": (_i, [_vp, _vp, _i, _i, _vp, _i, _i, _i, _f, _vp, _i, _i, _vp]),
+        "ntg_target_extent": (_i, [_i, _i, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
         "ntg_encode": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
         "ntg_encode_noalloc": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
         "ntg_chain_levels": (_i, [_i, _i, _i]),
@@ -141,6 +143,13 @@ def _stream_ptr(stream=None):
     return ctypes.c_void_p(s.cuda_stream)
 
 
+def target_extent(w: int, h: int, max_extent: int, round_mode: int):
+    """nv::getTargetExtent for a 2D texture (ntg_target_extent)."""
+    ow, oh = _i(), _i()
+    _check(lib().ntg_target_extent(w, h, max_extent, round_mode, ctypes.byref(ow), ctypes.byref(oh)))
+    return ow.value, oh.value
+
+
 def launch_count() -> int:
     """Kernel launches issued through the library by this process so far (ntg_launch_count)."""
     return int(lib().ntg_launch_count())
@@ -198,6 +207,16 @@ class Context:
         p = (ctypes.c_float * 2)(*params)
         _check(lib().ntg_mip_level(self.h, src.data_ptr(), w, h, out.data_ptr(), filter, width, ctypes.cast(p, _vp),
                                    wrap, alpha_mode, weighted, _stream_ptr(stream)))
+        return out
+
+    def resize(self, src, w, h, dw, dh, filter=FILTER_BOX, width=0.0, params=(0.0, 0.0), wrap=WRAP_MIRROR,
+               alpha_mode=ALPHA_NONE, out=None, stream=None):
+        """Surface::resize of a planar FP32 image to dw x dh (ntg_resize)."""
+        import torch
+        out = out if out is not None else torch.empty(4 * dw * dh, dtype=torch.float32, device=src.device)
+        p = (ctypes.c_float * 2)(*params)
+        _check(lib().ntg_resize(self.h, src.data_ptr(), w, h, out.data_ptr(), dw, dh, filter, width, ctypes.cast(p, _vp),
+                                wrap, alpha_mode, _stream_ptr(stream)))
         return out
 
     def encode(self, fmt, rgba, w, h, quality=QUALITY_NORMAL, alpha_mode=ALPHA_NONE, out_xform=XFORM_NONE, gamma=2.2,

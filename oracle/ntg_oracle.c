@@ -1734,6 +1734,41 @@ int ora_mip_chain(const uint8_t *bgra, int w, int h, int filter, float width, fl
 }
 
 /* ------------------------------------------------------------------------------------------ */
+/* Target extent of the InputOptions resize step (nv::getTargetExtent, src/nvtt/Surface.cpp:220-326,
+ * 2D textures, no shape restriction) with the rounding helpers of src/nvtt/Surface.cpp:60-105 and
+ * nextPowerOfTwo (src/nvcore/Utils.h:205-229). The reference tests RoundMode_ToNextMultipleOfFour
+ * twice in its else-if chain, so RoundMode_ToNearestMultipleOfFour leaves the extents as they are. */
+static unsigned next_pow2(unsigned x) {
+    x--;
+    x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
+    return x + 1;
+}
+static unsigned prev_pow2(unsigned v) { return next_pow2(v + 1) / 2; }
+static unsigned nearest_pow2(unsigned v) {
+    const unsigned np2 = next_pow2(v), pp2 = prev_pow2(v);
+    return np2 - v <= v - pp2 ? np2 : pp2;
+}
+
+void ora_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, int *out_h) {
+    if (round_mode != 0 && max_extent > 0) max_extent = (int)prev_pow2((unsigned)max_extent);
+    const int m = w > h ? w : h;
+    if (max_extent > 0 && m > max_extent) {
+        w = (w * max_extent) / m; if (w < 1) w = 1;
+        h = (h * max_extent) / m; if (h < 1) h = 1;
+    }
+    switch (round_mode) {
+        case 1: w = (int)next_pow2((unsigned)w); h = (int)next_pow2((unsigned)h); break;
+        case 2: w = (int)nearest_pow2((unsigned)w); h = (int)nearest_pow2((unsigned)h); break;
+        case 3: w = (int)prev_pow2((unsigned)w); h = (int)prev_pow2((unsigned)h); break;
+        case 4: w = (int)(((unsigned)w + 3) & ~3u); h = (int)(((unsigned)h + 3) & ~3u); break;
+        case 6: w = (int)((unsigned)w & ~3u); h = (int)((unsigned)h & ~3u); break;
+        default: break;
+    }
+    *out_w = w;
+    *out_h = h;
+}
+
+/* ------------------------------------------------------------------------------------------ */
 /* Decode (Surface::setImage2D, D3D10) and RMSE                                                 */
 
 static void decode_bc1(const uint8_t *b, uint8_t rgba[16][4]) {

@@ -54,6 +54,8 @@ void ora_bc1a_block(const uint8_t *bgra64, int alpha_mode, const float *cw3, uin
 void ora_bc4_block(const uint8_t *bgra64, int quality, uint8_t *out8);
 void ora_bc1a_image(const float *rgba, int w, int h, int alpha_mode, const float *cw3, uint8_t *out, int threads);
 void ora_bc4_image(const float *rgba, int w, int h, int quality, uint8_t *out, int threads);
+/* Target extent of the InputOptions resize step (2D). */
+void ora_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, int *out_h);
 /* BC3/BC5 from an already quantised BGRA8 image (ColorBlock path without the float stage). */
 void ora_bc3_image_u8(const uint8_t *bgra, int w, int h, int alpha_mode, int quality, const float *cw3,
                       uint8_t *out, int threads);

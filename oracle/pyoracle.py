@@ -71,6 +71,7 @@ class Oracle:
         self._bc1a_image = _bind(lib, "ora_bc1a_image", None, [_vp, _i, _i, _i, _vp, _vp, _i])
         self._bc4_image = _bind(lib, "ora_bc4_image", None, [_vp, _i, _i, _i, _vp, _i])
         self._dxt1a_single = _bind(lib, "ora_dxt1a_single_color", None, [_i, _i, _i, ctypes.c_uint32, _vp])
+        self._target_extent = _bind(lib, "ora_target_extent", None, [_i, _i, _i, _i, _vp, _vp])
         self._dxt5a_quick = _bind(lib, "ora_dxt5a_quick", None, [_vp, _vp])
         self._dxt5a_optimal = _bind(lib, "ora_dxt5a_optimal", None, [_vp, _vp])
         self._dxt1_single = _bind(lib, "ora_dxt1_single_color", None, [_i, _i, _i, _vp])
@@ -128,6 +129,11 @@ class Oracle:
         out = np.zeros(8, np.uint8)
         self._bc4_block(_ptr(b), quality, _ptr(out))
         return out
+
+    def target_extent(self, w, h, max_extent, round_mode):
+        ow, oh = _i(), _i()
+        self._target_extent(w, h, max_extent, round_mode, ctypes.byref(ow), ctypes.byref(oh))
+        return ow.value, oh.value
 
     def dxt1a_single_color(self, r, g, b, alpha_mask):
         out = np.zeros(8, np.uint8)
@@ -297,6 +303,8 @@ class Reference:
         self._bc1a_block = _bind(lib, "ref_bc1a_block", None, [_vp, _i, _vp, _vp])
         self._bc4_block = _bind(lib, "ref_bc4_block", None, [_vp, _i, _vp])
         self._dxt5a_quick = _bind(lib, "ref_dxt5a_quick", None, [_vp, _vp])
+        self._surface_resize = _bind(lib, "ref_surface_resize", None, [_vp, _i, _i, _i, _i, _i, _f, _f, _f, _i, _i, _vp])
+        self._target_extent = _bind(lib, "ref_target_extent", None, [_i, _i, _i, _i, _vp, _vp])
         self._dxt5a_optimal = _bind(lib, "ref_dxt5a_optimal", None, [_vp, _vp])
         self._dxt1_single = _bind(lib, "ref_dxt1_single_color", None, [_i, _i, _i, _vp])
         self._quick_dxt1 = _bind(lib, "ref_quick_dxt1", None, [_vp, _vp])
@@ -319,6 +327,17 @@ class Reference:
         out = np.zeros(8, np.uint8)
         err = self._icbc(level, _ptr(c), _ptr(w), _ptr(np.asarray(cw, np.float32)), three, black, _ptr(out))
         return out, err
+
+    def surface_resize(self, rgba, w, h, dw, dh, filt, width, p0=0.0, p1=0.0, wrap=2, alpha_mode=0):
+        r = np.ascontiguousarray(rgba, np.float32)
+        out = np.zeros(4 * dw * dh, np.float32)
+        self._surface_resize(_ptr(r), w, h, dw, dh, filt, width, p0, p1, wrap, alpha_mode, _ptr(out))
+        return out
+
+    def target_extent(self, w, h, max_extent, round_mode):
+        ow, oh = _i(), _i()
+        self._target_extent(w, h, max_extent, round_mode, ctypes.byref(ow), ctypes.byref(oh))
+        return ow.value, oh.value
 
     def compress(self, rgba, w, h, fmt, quality=1, alpha_mode=0, cw=(1, 1, 1, 1)):
         r = np.ascontiguousarray(rgba, np.float32)
@@ -443,13 +462,14 @@ class Reference:
 
     def process_ex(self, data, w, h, fmt, input_format=0, nsrc_levels=1, quality=1, mip_filter=0, alpha_mode=0,
                    wrap=2, max_level=-1, header=True, kaiser=(3.0, 4.0, 1.0), gamma=(2.2, 2.2), cw=(1, 1, 1, 1),
-                   container=0, srgb=0, version=0, normal_map=0, normalize_mips=1):
+                   container=0, srgb=0, version=0, normal_map=0, normalize_mips=1, max_extent=0, round_mode=0):
         """Compressor::process with containers, flags, Kaiser parameters, source mipmaps and float
         input; returns the bytes, or the negative nvtt::Error - 100 on failure."""
         b = np.ascontiguousarray(data).view(np.uint8)
         opts = np.array(list(kaiser) + list(gamma) + list(cw), np.float32)
-        flags = np.array([container, srgb, version, normal_map, normalize_mips], np.int32)
-        cap = 16 * Oracle.nblocks(w, h) * 2 + 4096
+        flags = np.array([container, srgb, version, normal_map, normalize_mips, max_extent, round_mode], np.int32)
+        side = 1 << (max(w, h) - 1).bit_length()  # rounding modes may grow the extents up to the next power of two
+        cap = 16 * Oracle.nblocks(side, side) * 2 + 4096
         out = np.zeros(cap, np.uint8)
         n = self._process_ex(_ptr(b), w, h, input_format, nsrc_levels, fmt, quality, mip_filter, alpha_mode, wrap,
                              max_level, int(header), _ptr(opts), _ptr(flags), _ptr(out), cap)

@@ -15,6 +15,7 @@
 #include "nvtt/CompressorDX9.h"
 #include "nvtt/CompressorDX10.h"
 #include "nvtt/CompressionOptions.h"
+#include "nvtt/Surface.h"
 #include "nvimage/ColorBlock.h"
 #include "nvimage/BlockDXT.h"
 #include "nvimage/Filter.h"
@@ -286,6 +287,28 @@ void ref_resize_weighted(const float * rgba, int w, int h, int dw, int dh, int f
     delete f;
 }
 
+// Surface::resize(w, h, d, filter, filterWidth, params) (src/nvtt/Surface.cpp:1152-1230) of a
+// planar FP32 image, with the surface's wrap and alpha modes. filter is an nvtt::ResizeFilter.
+void ref_surface_resize(const float * rgba, int w, int h, int dw, int dh, int filter, float width, float p0, float p1,
+                        int wrap, int alpha_mode, float * out) {
+    Surface s;
+    const size_t n = (size_t)w * h;
+    s.setImage(InputFormat_RGBA_32F, w, h, 1, rgba, rgba + n, rgba + 2 * n, rgba + 3 * n);
+    s.setWrapMode((WrapMode)wrap);
+    s.setAlphaMode((AlphaMode)alpha_mode);
+    const float params[2] = {p0, p1};
+    s.resize(dw, dh, 1, (ResizeFilter)filter, width, params);
+    memcpy(out, s.data(), sizeof(float) * 4 * (size_t)dw * dh);
+}
+
+// nv::getTargetExtent (src/nvtt/Surface.cpp:220-326) for a 2D texture.
+void ref_target_extent(int w, int h, int max_extent, int round_mode, int * out_w, int * out_h) {
+    int d = 1;
+    nv::getTargetExtent(&w, &h, &d, max_extent, (RoundMode)round_mode, TextureType_2D);
+    *out_w = w;
+    *out_h = h;
+}
+
 // Decode blocks with Surface::setImage2D (src/nvtt/Surface.cpp:908) into planar FP32.
 int ref_decode(int format, const unsigned char * blocks, int w, int h, float * out) {
     Surface s;
@@ -364,6 +387,8 @@ long long ref_process_ex(const void * data, int w, int h, int input_format, int 
     io.setMipmapGeneration(max_level != 0, max_level);
     io.setNormalMap(flags[3] != 0);
     io.setNormalizeMipmaps(flags[4] != 0);
+    io.setMaxExtents(flags[5]);
+    io.setRoundMode((RoundMode)flags[6]);
     CompressionOptions co;
     fill_options(co, format, quality, opts + 5);
     MemoryOutput mem;

@@ -132,6 +132,8 @@ int main(int argc, char **argv) {
         io.setMipmapGeneration(maxLevel != 0, maxLevel);
         io.setNormalMap(normal);
         io.setNormalizeMipmaps(num("normalize", 1) != 0);
+        io.setMaxExtents((int)num("max_extent", 0));
+        io.setRoundMode((nvtt::RoundMode)(int)num("round_mode", 0));
         estimate = compressor.estimateSize(io, co);
         if (!compressor.process(io, co, oo)) return fail(err);
     } else if (mode == "surface" || mode == "rms") {
@@ -151,6 +153,16 @@ int main(int argc, char **argv) {
         if (!normal) {
             if (srgbCurve) img.toLinearFromSrgb();
             else img.toLinear(gin);
+        }
+        const int maxExtent = (int)num("max_extent", 0), roundMode = (int)num("round_mode", 0);
+        if (maxExtent > 0 || roundMode != 0) {  // the InputOptions resize step, through the Surface API
+            img.resize(maxExtent, (nvtt::RoundMode)roundMode, nvtt::ResizeFilter_Box);
+            if (maxLevel != 0) {
+                int x = img.width(), y = img.height();
+                mipmapCount = 1;
+                while (x != 1 || y != 1) { x = x > 1 ? x / 2 : 1; y = y > 1 ? y / 2 : 1; mipmapCount++; }
+                if (maxLevel > 0 && maxLevel < mipmapCount) mipmapCount = maxLevel;
+            }
         }
         estimate = compressor.estimateSize(img, mipmapCount, co);
         if (!compressor.outputHeader(img, mipmapCount, co, oo)) return fail(err);

@@ -159,7 +159,8 @@ def write_dds_fixtures(R):
 
 # Compressor::process cases for the nvtt:: drop-in API: containers, header flags, filters, gammas,
 # source mipmaps, float input, one format the DDS container rejects (BC7 -> Error 6), and BC1a /
-# BC4 (BC4 at Normal and Fastest only: the reference's Production BC4 varies from run to run).
+# BC4 (BC4 at Normal and Fastest only: the reference's Production BC4 varies from run to run), and the
+# InputOptions resize step (max extent, round modes).
 DDS_CASES = [
     dict(w=61, h=37, format=1, quality=1, mip_filter=0),
     dict(w=64, h=64, format=4, quality=1, mip_filter=2, alpha_mode=1, srgb=1, version=7),
@@ -177,6 +178,13 @@ DDS_CASES = [
     dict(w=32, h=20, format=2, quality=2, container=1, srgb=1),
     dict(w=36, h=36, format=6, quality=1, mip_filter=1),
     dict(w=16, h=24, format=6, quality=0, container=1),
+    dict(w=61, h=37, format=1, quality=1, mip_filter=2, round_mode=1),                 # up to 64 x 64
+    dict(w=100, h=60, format=4, quality=1, mip_filter=1, alpha_mode=1, max_extent=40),  # down to 40 x 24
+    dict(w=70, h=50, format=7, quality=1, max_extent=64, round_mode=3, wrap=1),         # 64 x 32 after rounding
+    dict(w=23, h=41, format=1, quality=0, round_mode=4, gamma=(1.0, 1.0), container=1),  # 24 x 44
+    dict(w=30, h=18, format=2, quality=1, round_mode=2, alpha_mode=1),                  # 32 x 16
+    dict(w=45, h=27, format=4, quality=1, round_mode=5, max_level=1),                   # unchanged (reference quirk)
+    dict(w=3, h=9, format=1, quality=1, round_mode=6),                                  # width 0: rejected
 ]
 
 

@@ -272,6 +272,25 @@ def test_chain_golden_fixture(ctx):
 
 
 # ---------------------------------------------------------------------------------------------
+# resize (Surface::resize, the InputOptions resize step)
+
+@pytest.mark.parametrize("w,h,dw,dh", [(61, 37, 64, 64), (100, 60, 40, 24), (64, 64, 16, 16), (4096 // 16, 48, 10, 7),
+                                       (13, 9, 16, 16), (7, 3, 8, 4), (3, 200, 1, 50), (40, 40, 40, 10)])
+@pytest.mark.parametrize("filt,width,p0,p1", [(0, 0.5, 0, 0), (1, 1.0, 0, 0), (2, 3.0, 4.0, 1.0)])
+def test_resize_matches_oracle(ctx, oracle, w, h, dw, dh, filt, width, p0, p1):
+    img = float_image(w, h, w * 7 + h + filt)
+    for wrap in (0, 1, 2):
+        ours = host(ctx.resize(dev(img), w, h, dw, dh, filter=filt, width=width, params=(p0, p1), wrap=wrap))
+        ref = oracle.resize(img, w, h, dw, dh, filt, width, p0, p1, wrap)
+        assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), wrap
+
+
+def test_resize_to_same_extent_is_a_copy(ctx):
+    img = float_image(9, 5, 3)
+    assert np.array_equal(host(ctx.resize(dev(img), 9, 5, 9, 5)), img)
+
+
+# ---------------------------------------------------------------------------------------------
 # decode and error
 
 @pytest.mark.parametrize("fmt", [1, 2, 4, 6, 7])

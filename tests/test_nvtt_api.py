@@ -34,7 +34,8 @@ def harness_args(c, **extra):
     """Harness key=value arguments for a fixture case (the keyword names of Reference.process_ex)."""
     names = dict(w="w", h="h", format="format", quality="quality", mip_filter="filter", alpha_mode="alpha",
                  wrap="wrap", max_level="max_level", container="container", srgb="srgb", version="version",
-                 normal_map="normal", normalize_mips="normalize", input_format="input_format", nsrc_levels="nsrc")
+                 normal_map="normal", normalize_mips="normalize", input_format="input_format", nsrc_levels="nsrc",
+                 max_extent="max_extent", round_mode="round_mode")
     args = {}
     for k, v in c.items():
         if k in names:
@@ -93,9 +94,19 @@ def test_harness_compiles_and_links(harness):
     assert os.path.getsize(harness) > 0
 
 
+def target_args(i):
+    """For a case with the InputOptions resize step: the extents the header carries (nv::getTargetExtent)."""
+    import ntg
+    c = case(i)
+    if not c.get("max_extent") and not c.get("round_mode"):
+        return {}
+    w, h = ntg.target_extent(c["w"], c["h"], c.get("max_extent", 0), c.get("round_mode", 0))
+    return dict(w=w, h=h, max_extent=0, round_mode=0)
+
+
 @pytest.mark.parametrize("i", range(NCASES))
 def test_header_matches_reference(harness, tmp_path, i):
-    rc, log, data = run(harness, "header", i, tmp_path)
+    rc, log, data = run(harness, "header", i, tmp_path, **target_args(i))
     err = expected_error(i)
     if err is not None:  # the reference's DDS container rejects the format before writing anything
         assert rc == 10 + err, log

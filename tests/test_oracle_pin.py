@@ -185,6 +185,32 @@ def test_images_vs_reference(oracle, reference, fmt, quality, alpha_mode):
         assert np.array_equal(ours, ref)
 
 
+def test_target_extent_vs_reference(oracle, reference):
+    """nv::getTargetExtent for every round mode, with and without a maximum extent (the library's
+    own ntg_target_extent is held to the same values)."""
+    import ntg
+    for w in list(range(1, 40)) + [63, 64, 65, 100, 127, 1000, 4095]:
+        for h in (1, 2, 3, 7, 64, 300):
+            for me in (0, 1, 5, 16, 48, 64, 1000):
+                for rm in range(7):
+                    ref = reference.target_extent(w, h, me, rm)
+                    assert oracle.target_extent(w, h, me, rm) == ref
+                    assert ntg.target_extent(w, h, me, rm) == ref
+
+
+@pytest.mark.parametrize("alpha_mode", [0, 1])
+def test_resize_vs_reference(oracle, reference, alpha_mode):
+    """FloatImage::resize through Surface::resize, down and up, every wrap mode."""
+    rng = np.random.default_rng(12)
+    for (w, h, dw, dh) in [(61, 37, 64, 32), (64, 64, 16, 16), (100, 50, 64, 32), (13, 9, 16, 16), (7, 3, 8, 4)]:
+        img = rng.random(4 * w * h).astype(np.float32)
+        for filt, width, p0, p1 in [(0, 0.5, 0, 0), (1, 1.0, 0, 0), (2, 3.0, 4.0, 1.0)]:
+            for wrap in (0, 1, 2):
+                a = oracle.resize(img, w, h, dw, dh, filt, width, p0, p1, wrap)
+                b = reference.surface_resize(img, w, h, dw, dh, filt, width, p0, p1, wrap, alpha_mode)
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
 def test_decode_and_rms_vs_reference(oracle, reference):
     rng = np.random.default_rng(4)
     for fmt in (1, 2, 4, 6, 7):
