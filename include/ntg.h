@@ -89,6 +89,11 @@ int ntg_set_image_bgra8(ntg_context *ctx, const void *d_bgra, int w, int h, int 
 int ntg_resize(ntg_context *ctx, const float *d_src, int w, int h, float *d_dst, int dw, int dh, int filter, float width,
                const float *params, int wrap, int alpha_mode, void *stream);
 
+/* Self-test of the mip kernels' sRGB quantiser (a bucket table plus one step comparison) against the
+ * plain search over the toSrgb step table, on every float bit pattern of both signs: writes the
+ * number of disagreements (0 expected). No reference counterpart; synchronous. */
+int ntg_selftest_srgb_quantizer(ntg_context *ctx, unsigned long long *mismatches);
+
 /* nv::getTargetExtent (src/nvtt/Surface.cpp:220-326) for a 2D texture: the level-0 extent that
  * Compressor::process resizes to for InputOptions::setMaxExtent / setRoundMode (round_mode is an
  * nvtt::RoundMode). A result may be 0 (ToPreviousMultipleOfFour below 4), as in the reference. */

@@ -116,10 +116,10 @@ struct AxisTable {
     int left0 = 0;
 };
 
-// Launch shape of the 2:1 mip kernel (output rows per warp strip, threads per CTA).
+// Launch shape of the 2:1 mip kernel (output rows per tile, threads per CTA).
 struct MipTuning {
-    int strip = 32;
-    int threads = 128;
+    int strip = 16;
+    int threads = 512;
     long long tail_texels = 4096;  // a chain's remaining levels go to one tail CTA from a source this small
 };
 
@@ -128,7 +128,7 @@ struct XformTables {
     float *d_in = nullptr;       // input transform of 8-bit RGB values [256], then v / 255 for alpha [256]
     float *d_comp = nullptr;     // output(input(v/255)) for the BC1 level-0 path
     uint8_t *d_comp8 = nullptr;  // quantised composition (RGB) + alpha quantiser, 512 bytes
-    float *d_steps = nullptr;    // sRGB quantiser steps
+    float *d_steps = nullptr;    // sRGB quantiser steps (256 floats), then its bucket table (kSrgbBuckets bytes)
 };
 
 }  // namespace
@@ -213,14 +213,19 @@ struct ntg_context {
         for (int v = 0; v < 256; v++) lin[256 + v] = (float)v / 255.0f;
         build_composed_lut(in_x, out_x, gamma, tables, comp);
         build_composed_lut8(in_x, out_x, gamma, tables, comp8);
+        // the quantiser steps, followed by the bucket table of the fast sRGB path
+        static_assert(sizeof(float) * 256 % 4 == 0, "bucket table alignment");
+        std::vector<uint8_t> quant(sizeof(float) * 256 + kSrgbBuckets);
         build_srgb_steps(steps);
+        if (!build_srgb_buckets(steps, quant.data() + sizeof steps)) return nullptr;
+        std::memcpy(quant.data(), steps, sizeof steps);
         if (alloc((void **)&t.d_in, sizeof lin) || alloc((void **)&t.d_comp, sizeof comp) ||
-            alloc((void **)&t.d_comp8, sizeof comp8) || alloc((void **)&t.d_steps, sizeof steps))
+            alloc((void **)&t.d_comp8, sizeof comp8) || alloc((void **)&t.d_steps, quant.size()))
             return nullptr;
         if (cudaMemcpy(t.d_in, lin, sizeof lin, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(t.d_comp, comp, sizeof comp, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(t.d_comp8, comp8, sizeof comp8, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(t.d_steps, steps, sizeof steps, cudaMemcpyHostToDevice) != cudaSuccess)
+            cudaMemcpy(t.d_steps, quant.data(), quant.size(), cudaMemcpyHostToDevice) != cudaSuccess)
             return nullptr;
         return &(xforms[key] = t);
     }
@@ -354,18 +359,9 @@ void group_launches(const std::vector<std::pair<MipKey, MipJob>> &items, const M
         m.first_job = (int)all.size();
         m.njobs = (int)g.second.size();
         m.threads = tune.threads;
-        if (m.kernel == MIP_POLY2X) {
-            // a warp sweeps its strip serially: shorten the strips until the launch has enough warps
-            const long long target = 152LL * 16;
-            int strip = tune.strip;
-            for (;;) {
-                long long n = 0;
-                for (const MipJob &J : g.second) n += (long long)J.tiles_x * ((J.h + strip - 1) / strip);
-                if (strip <= 2 || n >= target) break;
-                strip /= 2;
-            }
-            for (MipJob &J : g.second) J.strip = strip;
-        }
+        const int tile_h = std::min(32, std::max(4, tune.strip));
+        if (m.kernel == MIP_POLY2X)
+            for (MipJob &J : g.second) J.strip = tile_h;
         long long units = 0;
         int rx = 0, ry = 0;
         for (MipJob J : g.second) {
@@ -376,7 +372,7 @@ void group_launches(const std::vector<std::pair<MipKey, MipJob>> &items, const M
             all.push_back(J);
         }
         m.units = units;
-        m.smem = m.kernel == MIP_POLY ? poly_smem_bytes(rx, ry) : m.kernel == MIP_POLY2X ? poly2x_smem_bytes(m.ws, m.threads) : 0;
+        m.smem = m.kernel == MIP_POLY ? poly_smem_bytes(rx, ry) : m.kernel == MIP_POLY2X ? poly2x_smem_bytes(m.ws, tile_h) : 0;
         out.push_back(m);
     }
 }
@@ -655,6 +651,21 @@ int ntg_resize(ntg_context *ctx, const float *d_src, int w, int h, float *d_dst,
     NTG_TRY(ctx->workspace((size_t)dw * h * 4 * sizeof(float), s, &tmp));
     return launched(launch_resize(d_src, w, h, (float *)tmp, dw, dh, ax->d_w, ax->d_left, ax->ws, ay->d_w, ay->d_left,
                                   ay->ws, wrap, d_dst, s), "resize");
+}
+
+int ntg_selftest_srgb_quantizer(ntg_context *ctx, unsigned long long *mismatches) {
+    g_error.clear();
+    if (!ctx || !mismatches) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    const XformTables *xt = ctx->xform(NTG_XFORM_NONE, NTG_XFORM_SRGB, 2.2f);
+    if (!xt) return fail(NTG_ERROR_CUDA, "table upload failed");
+    unsigned long long *d = nullptr;
+    NTG_CUDA(cudaMalloc((void **)&d, sizeof *d));
+    int r = launched(launch_check_srgb(xt->d_steps, d, nullptr), "quantiser check");
+    if (r == NTG_OK && cudaMemcpy(mismatches, d, sizeof *d, cudaMemcpyDeviceToHost) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "copy");
+    cudaFree(d);
+    return r;
 }
 
 // nv::getTargetExtent (src/nvtt/Surface.cpp:220-326), 2D, no shape restriction, with the rounding
@@ -1200,7 +1211,7 @@ int batch_capture(ntg_batch *b) {
 
 struct TuneEntry {
     std::string key;
-    int strip = 32, threads = 128, tail = 4096, bc1 = 64, bc3 = 128, bc5 = 128;
+    int strip = 16, threads = 512, tail = 4096, bc1 = 64, bc3 = 128, bc5 = 128;
     double mip_ms = 0, encode_ms = 0;
 };
 
@@ -1246,8 +1257,8 @@ std::vector<TuneEntry> tune_cache_read() {
         if (k1 == std::string::npos) continue;
         TuneEntry e;
         e.key = obj.substr(k0 + 1, k1 - k0 - 1);
-        e.strip = (int)json_number(obj, "strip", 32);
-        e.threads = (int)json_number(obj, "threads", 128);
+        e.strip = (int)json_number(obj, "strip", 16);
+        e.threads = (int)json_number(obj, "threads", 512);
         e.tail = (int)json_number(obj, "tail", 4096);
         e.bc1 = (int)json_number(obj, "bc1", 64);
         e.bc3 = (int)json_number(obj, "bc3", 128);
@@ -1291,6 +1302,9 @@ void apply_entry(ntg_batch *b, const TuneEntry &e) {
 }
 
 // Device name and a hash of every texture's size and options.
+// Version of the tunable launch shapes (2:1 tile height and CTA size, tail size, encoder CTA sizes).
+constexpr long long kTuneShapeVersion = 2;
+
 std::string batch_key(const ntg_batch *b) {
     cudaDeviceProp prop;
     std::string dev = cudaGetDeviceProperties(&prop, b->ctx->device) == cudaSuccess ? prop.name : "device";
@@ -1300,6 +1314,7 @@ std::string batch_key(const ntg_batch *b) {
     auto mix = [&](long long v) {
         for (int i = 0; i < 8; i++) { h ^= (unsigned long long)((v >> (8 * i)) & 255); h *= 1099511628211ull; }
     };
+    mix(kTuneShapeVersion);  // entries written for another set of kernel shapes do not apply
     for (size_t t = 0; t < b->tex.size(); t++) {
         const ntg_chain_options &o = b->opts[t];
         mix(b->tex[t].w); mix(b->tex[t].h); mix(o.format); mix(o.quality); mix(o.filter); mix(o.alpha_mode);
@@ -1391,8 +1406,8 @@ int ntg_batch_autotune(ntg_batch *b, void *stream) {
     MipTuning best = keep;
     float best_ms = 1e30f;
     for (int tail : {1024, 4096})
-        for (int threads : {64, 128, 256})
-            for (int strip : {8, 16, 32, 64}) {
+        for (int threads : {256, 512})
+            for (int strip : {8, 16, 32}) {
                 b->tune.strip = strip;
                 b->tune.threads = threads;
                 b->tune.tail_texels = tail;

@@ -201,6 +201,28 @@ void build_srgb_steps(float steps[256]) {
     }
 }
 
+// Bucket table of the device's sRGB quantiser: over [2^-14, 2), bucket b covers the floats whose
+// bits >> 15 equal (bits of 2^-14 >> 15) + b; buckets[b] = steps at or below its smallest float.
+// Returns false unless every bucket holds at most one step beyond that and the first step lies
+// above 2^-14, the two facts the device's single correcting comparison relies on.
+bool build_srgb_buckets(const float steps[256], uint8_t buckets[kSrgbBuckets]) {
+    uint32_t first;
+    std::memcpy(&first, &steps[1], 4);
+    const uint32_t lo_bits = 113u << 23;  // 2^-14
+    if (first <= lo_bits) return false;
+    int k = 0;  // steps (1..255) at or below the current bound
+    for (int b = 0; b < kSrgbBuckets; b++) {
+        const uint32_t lo = lo_bits + ((uint32_t)b << 15), hi = lo + (1u << 15) - 1;
+        auto bits = [&](int i) { uint32_t u; std::memcpy(&u, &steps[i], 4); return u; };
+        while (k < 255 && bits(k + 1) <= lo) k++;
+        buckets[b] = (uint8_t)k;
+        int inside = 0;
+        for (int i = k + 1; i < 256 && bits(i) <= hi; i++) inside++;
+        if (inside > 1) return false;
+    }
+    return true;
+}
+
 // ---- polyphase kernels (src/nvimage/Filter.cpp) ----
 
 static const float kPi = (float)3.1415926535897932384626433833;

@@ -35,6 +35,8 @@ void build_input_lut(int xform, float gamma, const HostTables &t, float lut[256]
 void build_composed_lut(int in_xform, int out_xform, float gamma, const HostTables &t, float lut[256]);
 void build_composed_lut8(int in_xform, int out_xform, float gamma, const HostTables &t, uint8_t lut8[512]);
 void build_srgb_steps(float steps[256]);
+constexpr int kSrgbBuckets = 15 * 256;  // the device quantiser's buckets over [2^-14, 2)
+bool build_srgb_buckets(const float steps[256], uint8_t buckets[kSrgbBuckets]);
 
 // Polyphase filtering: 0 box, 1 triangle, 2 kaiser (params: alpha, stretch).
 float filter_evaluate(int filter, float width, float p0, float p1, float x);

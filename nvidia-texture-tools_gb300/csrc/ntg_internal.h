@@ -46,6 +46,8 @@ int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, 
 int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 int launch_bc5(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
 int launch_bc1a(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t s);
+// Counts the floats on which the fast sRGB quantiser and the step search disagree.
+int launch_check_srgb(const float *steps, unsigned long long *bad, cudaStream_t s);
 // Separable polyphase resize of a planar FP32 image (two launches through `tmp`, w * H * 16 bytes).
 int launch_resize(const float *src, int W, int H, float *tmp, int w, int h, const float *kx, const int *lx, int wsx,
                   const float *ky, const int *ly, int wsy, int wrap, float *dst, cudaStream_t s);
@@ -108,7 +110,7 @@ int launch_transform(float *rgba, size_t n, int kind, float p, cudaStream_t s);
 int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s);
 bool poly2x_supported(int ws);
 size_t poly_smem_bytes(int rx_max, int ry_max);
-size_t poly2x_smem_bytes(int ws, int threads);
+size_t poly2x_smem_bytes(int ws, int tile_h);  // dynamic shared memory of a 2:1 tile launch
 int poly_tile_w();
 int poly_tile_h();
 int poly_max_window();

@@ -60,6 +60,49 @@ __device__ __forceinline__ uint32_t quantize_bgra(float r, float g, float b, flo
            (quant_u8(a) << 24);
 }
 
+// The sRGB quantiser with a bucket table over [2^-14, 2): buckets[b] (b = float bits >> 15, from the
+// bucket of 2^-14) counts the steps at or below the smallest float of bucket b. The host checks,
+// when it builds the table, that no bucket holds more than one step and that the first step lies
+// above 2^-14; one comparison then finishes the count. Same code as quantize() for every float:
+// below 2^-14 (negatives and NaN included) nothing is passed, from 2 on everything is.
+constexpr int QB_LO = 113 << 8;   // (bits of 2^-14) >> 15; kSrgbBuckets buckets reach 2.0
+__device__ __forceinline__ uint32_t quantize_srgb(float x, const float *s_steps, const uint8_t *s_buckets) {
+    if (!(x >= 6.103515625e-05f)) return 0;
+    if (x >= 2.0f) return 255;
+    int c = s_buckets[(int)(__float_as_uint(x) >> 15) - QB_LO];
+    if (c < 255 && s_steps[c + 1] <= x) c++;
+    return (uint32_t)c;
+}
+
+__device__ __forceinline__ uint32_t quantize_srgb_bgra(float4 v, const float *s_steps, const uint8_t *s_buckets) {
+    return quantize_srgb(v.z, s_steps, s_buckets) | (quantize_srgb(v.y, s_steps, s_buckets) << 8) |
+           (quantize_srgb(v.x, s_steps, s_buckets) << 16) | (quant_u8(v.w) << 24);
+}
+
+// Self-check of quantize_srgb against the step search over every float bit pattern below 2^31
+// (all non-negative floats, infinities and NaNs included): counts the disagreements.
+__global__ void k_check_srgb(const float *__restrict__ steps, unsigned long long *__restrict__ bad) {
+    __shared__ float s_steps[256];
+    __shared__ uint8_t s_buckets[kSrgbBuckets];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_steps[i] = steps[i];
+    const uint8_t *b = reinterpret_cast<const uint8_t *>(steps + 256);
+    for (int i = threadIdx.x; i < kSrgbBuckets; i += blockDim.x) s_buckets[i] = b[i];
+    __syncthreads();
+    unsigned long long n = 0;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < 0x80000000u; u += gridDim.x * blockDim.x) {
+        const float x = __uint_as_float(u);
+        n += quantize(x, 2, s_steps) != quantize_srgb(x, s_steps, s_buckets);
+        n += quantize(-x, 2, s_steps) != quantize_srgb(-x, s_steps, s_buckets);
+    }
+    if (n) atomicAdd(bad, n);
+}
+
+int launch_check_srgb(const float *steps, unsigned long long *bad, cudaStream_t s) {
+    if (cudaMemsetAsync(bad, 0, sizeof *bad, s) != cudaSuccess) return launch_status();
+    k_check_srgb<<<152 * 8, 256, 0, s>>>(steps, bad);
+    return launch_status();
+}
+
 // Emits the quantised BGRA8 words of a planar FP32 level (used for level 0 of a chain).
 __global__ void k_quantize_level(const float *__restrict__ rgba, size_t n, Quant q, uint32_t *__restrict__ out) {
     __shared__ float s_steps[256];
@@ -286,169 +329,107 @@ __global__ void __launch_bounds__(PTHREADS) k_poly(const MipJob *__restrict__ jo
 }
 
 // Exact 2:1 kernel (both axes halve and every output has the same taps: power-of-two chains).
-// One warp per strip of 32 output columns x `strip` output rows sweeps the source rows top to
-// bottom, two rows per step. Each source row is staged once in shared memory (wrapped, even and
-// odd columns in separate halves so the stride-2 tap reads are conflict-free), its X taps are
-// computed per lane, and the result goes into the running Y sums of the outputs whose window
-// contains the row. Output t's window starts at row 2t, so at step p the NS open sums belong to
-// outputs p, p-1, ..., p-NS+1: row 2p gives sum d its tap 2d and row 2p+1 its tap 2d+1, the
-// oldest sum is then complete and written, and the window slides by one output. Every sum starts
-// at 0 and receives its taps in order, exactly like applyKernelY's loop.
+// One CTA per tile of 32 output columns x TH output rows (TH = the job's `strip`): the wrapped
+// source window (62 + WS columns x 2 TH - 2 + WS rows) is staged once in shared memory as float4,
+// even and odd columns in separate halves so the stride-2 tap reads of a warp are consecutive;
+// then every window row's X taps go to a (rows x 32) plane, then the Y taps. Every item of both
+// passes is independent, sums start at 0 and take their taps in order, as applyKernelX/Y do
+// (src/nvimage/FloatImage.cpp:1115-1176). The taps are the same for every output, so both
+// weight vectors live in registers.
 template <int WS>
-struct Poly2x {
+struct Tile2x {
     static_assert(WS % 2 == 1, "odd windows");
-    static constexpr int NS = (WS + 1) / 2;        // open output sums
-    static constexpr int SPAN = 62 + WS;           // source columns of 32 output columns
-    static constexpr int HALF = ((SPAN + 1) / 2 + 3) / 8 * 8 + 4;  // >= SPAN/2, = 4 mod 8: conflict-free stores
-    static constexpr int ROW = 2 * HALF;           // float4 per staged row
-    static constexpr int WARP_F4 = 2 * ROW + 8 + 128;          // per-warp shared memory in float4
-};
-
-// A source texel as loaded (BGRA8 word or four FP32 planes), converted to float4 when staged.
-template <bool SRC_U8> struct RawTexel;
-template <> struct RawTexel<true> { uint32_t v; };
-template <> struct RawTexel<false> { float4 v; };
-
-template <bool SRC_U8>
-__device__ __forceinline__ void fetch_raw(const MipJob &L, size_t s, size_t sn, RawTexel<SRC_U8> &r) {
-    if constexpr (SRC_U8) r.v = __ldg(L.bgra8 + s);
-    else r.v = make_float4(__ldg(L.src + s), __ldg(L.src + sn + s), __ldg(L.src + 2 * sn + s), __ldg(L.src + 3 * sn + s));
-}
-
-template <bool SRC_U8>
-__device__ __forceinline__ float4 convert_raw(const float *lut, const RawTexel<SRC_U8> &r) {
-    if constexpr (SRC_U8) {
-        const uint32_t p = r.v;
-        return make_float4(__ldg(lut + ((p >> 16) & 255)), __ldg(lut + ((p >> 8) & 255)), __ldg(lut + (p & 255)),
-                           (float)(p >> 24) / 255.0f);
-    } else {
-        return r.v;
-    }
-}
-
-// Loads two source rows of a strip (wrapped) into registers.
-struct RowFetch {
-    int r0, S, H, W, wrap, c0, span;
-    bool interior;
-    int lane;
-    size_t sn;
-    template <bool SRC_U8, int CPL>
-    __device__ __forceinline__ void pair(const MipJob &L, RawTexel<SRC_U8> (&pre)[2][CPL], int sa) const {
-#pragma unroll
-        for (int rr = 0; rr < 2; rr++) {
-            if (sa + rr < S) {
-                const int gy = r0 + sa + rr;
-                const size_t rowoff = (size_t)(gy >= 0 && gy < H ? gy : wrap_index(gy, H, wrap)) * W;
-#pragma unroll
-                for (int k = 0; k < CPL; k++) {
-                    const int c = lane + 32 * k;
-                    if (c < span) fetch_raw<SRC_U8>(L, rowoff + (interior ? c0 + c : wrap_index(c0 + c, W, wrap)), sn, pre[rr][k]);
-                }
-            }
-        }
+    static constexpr int TW = 32;
+    static constexpr int RW = 2 * (TW - 1) + WS;                       // source columns of a tile
+    static constexpr int HALF = ((RW + 1) / 2 + 3) / 8 * 8 + 4;         // >= RW/2, = 4 mod 8: conflict-free stores
+    static constexpr int ROW = 2 * HALF;                                // float4 per staged row
+    static __host__ __device__ constexpr int rows(int th) { return 2 * (th - 1) + WS; }
+    static __host__ __device__ constexpr size_t smem(int th) {
+        return ((size_t)rows(th) * ROW + (size_t)rows(th) * TW) * sizeof(float4);
     }
 };
 
 template <int WS, bool WEIGHTED, bool SRC_U8>
-__global__ void __launch_bounds__(256, 2) k_poly2x(const MipJob *__restrict__ jobs, int njobs, long long units) {
-    using P = Poly2x<WS>;
-    constexpr int NS = P::NS, HALF = P::HALF, ROW = P::ROW;
-    constexpr int CPL = (P::SPAN + 31) / 32;  // staged columns per lane
+__global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jobs, int njobs) {
+    using P = Tile2x<WS>;
+    constexpr int TW = P::TW, RW = P::RW, HALF = P::HALF, ROW = P::ROW;
     extern __shared__ float4 sm4[];
     __shared__ float s_steps[256];
-    load_steps(jobs, s_steps);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long u = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
-    if (u >= units) return;
-    const MipJob &L = jobs[find_mip_job(jobs, njobs, u)];
-    const long long lu = u - L.first_unit;
-    const int x0 = (int)(lu % L.tiles_x) * 32, y0 = (int)(lu / L.tiles_x) * L.strip;
-    const int W = L.W, H = L.H, w = L.w, wrap = L.wrap;
-    const int tv = min(L.strip, L.h - y0);
-    const int x = x0 + lane;
-    const bool xv = x < w;
-    // per-warp shared memory: two staged rows, the X and Y weights, then (8-bit source) the input
-    // table of RGB and alpha
-    float4 *buf = sm4 + warp * P::WARP_F4;
-    float *s_k = reinterpret_cast<float *>(buf + 2 * ROW);     // kx [16], ky [16]
-    float *s_lut = s_k + 32;
-    if (lane < WS) {
-        s_k[lane] = __ldg(L.kx + lane);
-        s_k[16 + lane] = __ldg(L.ky + lane);
+    __shared__ float s_lut[SRC_U8 ? 512 : 1];
+    __shared__ uint8_t s_buckets[kSrgbBuckets];
+    const MipJob &L = jobs[find_mip_job(jobs, njobs, blockIdx.x)];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const bool srgb = L.q_out && L.xform == 2;
+    if (L.q_out) {
+        for (int i = tid; i < 256; i += nt) s_steps[i] = __ldg(L.steps + i);
+        if (srgb) {
+            const uint32_t *b = reinterpret_cast<const uint32_t *>(L.steps + 256);
+            for (int i = tid; i < kSrgbBuckets / 4; i += nt) reinterpret_cast<uint32_t *>(s_buckets)[i] = __ldg(b + i);
+        }
     }
     if constexpr (SRC_U8)
-        for (int i = lane; i < 512; i += 32) s_lut[i] = __ldg(L.lut + i);
+        for (int i = tid; i < 512; i += nt) s_lut[i] = __ldg(L.lut + i);
+    float kx[WS], ky[WS];
+#pragma unroll
+    for (int j = 0; j < WS; j++) { kx[j] = __ldg(L.kx + j); ky[j] = __ldg(L.ky + j); }
+    const int th = L.strip;
+    const int rh = P::rows(th);
+    const long long lu = (long long)blockIdx.x - L.first_unit;
+    const int x0 = (int)(lu % L.tiles_x) * TW, y0 = (int)(lu / L.tiles_x) * th;
+    const int W = L.W, H = L.H, w = L.w, h = L.h, wrap = L.wrap;
     const int c0 = 2 * x0 + L.cx, r0 = 2 * y0 + L.cy;
-    const int span = 2 * (min(32, w - x0) - 1) + WS;
-    const bool interior = c0 >= 0 && c0 + span <= W;
-    const size_t sn = (size_t)W * H, dn = (size_t)w * L.h;
-    const int S = 2 * tv + WS - 2;   // source rows of the strip
-    const int steps = tv + NS - 1;   // row pairs
+    const bool cols_in = c0 >= 0 && c0 + RW <= W, rows_in = r0 >= 0 && r0 + rh <= H;
+    const size_t sn = (size_t)W * H, dn = (size_t)w * h;
+    float4 *region = sm4;                       // rh x ROW
+    float4 *tmp = sm4 + (size_t)rh * ROW;       // rh x TW
+    __syncthreads();
 
-    // source rows go through registers one pair ahead of the taps
-    RawTexel<SRC_U8> pre[2][CPL];
-    const RowFetch F{r0, S, H, W, wrap, c0, span, interior, lane, sn};
-
-    // open Y sums (norm: the alpha-weighted kernels' running weight)
-    float4 acc[NS];
-    float nrm[NS];
-#pragma unroll
-    for (int d = 0; d < NS; d++) { acc[d] = make_float4(0, 0, 0, 0); nrm[d] = 0; }
-
-    F.pair<SRC_U8, CPL>(L, pre, 0);
-#pragma unroll 1
-    for (int p = 0; p < steps; p++) {
-        const int sa = 2 * p;
-        __syncwarp();
-#pragma unroll
-        for (int rr = 0; rr < 2; rr++) {
-            if (sa + rr < S) {
-#pragma unroll
-                for (int k = 0; k < CPL; k++) {
-                    const int c = lane + 32 * k;
-                    if (c < span) {
-                        float4 v;
-                        if constexpr (SRC_U8) {
-                            const uint32_t q = pre[rr][k].v;
-                            v = make_float4(s_lut[(q >> 16) & 255], s_lut[(q >> 8) & 255], s_lut[q & 255], s_lut[256 + (q >> 24)]);
-                        } else {
-                            v = pre[rr][k].v;
-                        }
-                        buf[rr * ROW + (c & 1) * HALF + (c >> 1)] = v;
-                    }
-                }
-            }
+    // stage the wrapped source window (consecutive threads read consecutive columns)
+    for (int i = tid; i < rh * RW; i += nt) {
+        const int r = i / RW, c = i - r * RW;
+        const int gy = rows_in ? r0 + r : wrap_index(r0 + r, H, wrap);
+        const int gx = cols_in ? c0 + c : wrap_index(c0 + c, W, wrap);
+        const size_t s = (size_t)gy * W + gx;
+        float4 v;
+        if constexpr (SRC_U8) {
+            const uint32_t q = __ldg(L.bgra8 + s);
+            v = make_float4(s_lut[(q >> 16) & 255], s_lut[(q >> 8) & 255], s_lut[q & 255], s_lut[256 + (q >> 24)]);
+        } else {
+            v = make_float4(__ldg(L.src + s), __ldg(L.src + sn + s), __ldg(L.src + 2 * sn + s), __ldg(L.src + 3 * sn + s));
         }
-        __syncwarp();
-        if (sa + 2 < S) F.pair<SRC_U8, CPL>(L, pre, sa + 2);
+        region[r * ROW + (c & 1) * HALF + (c >> 1)] = v;
+    }
+    __syncthreads();
 
-        const int t = p - (NS - 1);  // the oldest sum completes with row 2p
-        const bool emit = t >= 0 && t < tv && xv;
-        const size_t o = (size_t)(y0 + t) * w + x;
-        float4 h[2];
+    // X taps of every window row: output column x reads source columns 2x .. 2x + WS - 1
+    for (int i = tid; i < rh * TW; i += nt) {
+        const int r = i >> 5, x = i & 31;
+        const float4 *row = region + r * ROW + x;
+        float4 sum = make_float4(0, 0, 0, 0);
+        float norm = 0;
 #pragma unroll
-        for (int rr = 0; rr < 2; rr++) {
-            const float4 *row = buf + rr * ROW + lane;
-            float4 sum = make_float4(0, 0, 0, 0);
-            float norm = 0;
+        for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, kx[j], row[(j & 1) * HALF + (j >> 1)]);
+        tmp[i] = finish<WEIGHTED>(sum, norm);
+    }
+    __syncthreads();
+
+    // Y taps: output row y reads window rows 2y .. 2y + WS - 1
+    for (int o = tid; o < th * TW; o += nt) {
+        const int y = o >> 5, x = o & 31;
+        if (y0 + y >= h || x0 + x >= w) continue;
+        const float4 *col = tmp + (2 * y) * TW + x;
+        float4 sum = make_float4(0, 0, 0, 0);
+        float norm = 0;
 #pragma unroll
-            for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, s_k[j], row[(j & 1) * HALF + (j >> 1)]);
-            h[rr] = finish<WEIGHTED>(sum, norm);
-        }
-        // row 2p: tap 2d of output p - d (the newest sum starts here)
-        acc[0] = make_float4(0, 0, 0, 0);
-        nrm[0] = 0;
-#pragma unroll
-        for (int d = 0; d < NS; d++) tap<WEIGHTED>(acc[d], nrm[d], s_k[16 + 2 * d], h[0]);
-        if (emit) store_texel(L, o, dn, finish<WEIGHTED>(acc[NS - 1], nrm[NS - 1]), s_steps);
-        // row 2p + 1: tap 2d + 1, then slide the window by one output
-#pragma unroll
-        for (int d = NS - 2; d >= 0; d--) {
-            tap<WEIGHTED>(acc[d], nrm[d], s_k[16 + 2 * d + 1], h[1]);
-            acc[d + 1] = acc[d];
-            nrm[d + 1] = nrm[d];
-        }
+        for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, ky[j], col[j * TW]);
+        const float4 v = finish<WEIGHTED>(sum, norm);
+        const size_t t = (size_t)(y0 + y) * w + x0 + x;
+        L.dst[t] = v.x;
+        L.dst[dn + t] = v.y;
+        L.dst[2 * dn + t] = v.z;
+        L.dst[3 * dn + t] = v.w;
+        if (L.q_out)
+            L.q_out[t] = srgb ? quantize_srgb_bgra(v, s_steps, s_buckets) : quantize_bgra(v.x, v.y, v.z, v.w, L.xform, s_steps);
     }
 }
 
@@ -655,17 +636,18 @@ static int launch_poly_t(const MipLaunch &m, const MipJob *jobs, cudaStream_t s)
 }
 
 template <int WS, bool W, bool U8>
-static int launch_poly2x_t(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
-    const int warps = m.threads / 32;
-    const long long grid = (m.units + warps - 1) / warps;
-    k_poly2x<WS, W, U8><<<(unsigned)grid, m.threads, m.smem, s>>>(jobs, m.njobs, m.units);
+static int launch_tile2x_t(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
+    static std::atomic<unsigned long long> configured{0};
+    if (first_use_on_device(configured))
+        cudaFuncSetAttribute(k_tile2x<WS, W, U8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    k_tile2x<WS, W, U8><<<(unsigned)m.units, m.threads, m.smem, s>>>(jobs, m.njobs);
     return launch_status();
 }
 
 template <int WS>
-static int launch_poly2x_ws(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
-    if (m.weighted) return m.u8 ? launch_poly2x_t<WS, true, true>(m, jobs, s) : launch_poly2x_t<WS, true, false>(m, jobs, s);
-    return m.u8 ? launch_poly2x_t<WS, false, true>(m, jobs, s) : launch_poly2x_t<WS, false, false>(m, jobs, s);
+static int launch_tile2x_ws(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
+    if (m.weighted) return m.u8 ? launch_tile2x_t<WS, true, true>(m, jobs, s) : launch_tile2x_t<WS, true, false>(m, jobs, s);
+    return m.u8 ? launch_tile2x_t<WS, false, true>(m, jobs, s) : launch_tile2x_t<WS, false, false>(m, jobs, s);
 }
 
 bool poly2x_supported(int ws) { return ws == 3 || ws == 5 || ws == 13; }
@@ -731,9 +713,8 @@ size_t poly_smem_bytes(int rx_max, int ry_max) {
            (size_t)(rx_max + ry_max) * sizeof(int);
 }
 
-size_t poly2x_smem_bytes(int ws, int threads) {
-    const int per_warp = ws == 3 ? Poly2x<3>::WARP_F4 : ws == 5 ? Poly2x<5>::WARP_F4 : Poly2x<13>::WARP_F4;
-    return (size_t)(threads / 32) * per_warp * sizeof(float4);
+size_t poly2x_smem_bytes(int ws, int tile_h) {
+    return ws == 3 ? Tile2x<3>::smem(tile_h) : ws == 5 ? Tile2x<5>::smem(tile_h) : Tile2x<13>::smem(tile_h);
 }
 
 int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s) {
@@ -760,10 +741,10 @@ int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s) {
             return launch_status();
         }
         case MIP_POLY2X:
-            if (m.threads < 32 || m.threads > 256 || m.threads % 32) return 1;
-            if (m.ws == 3) return launch_poly2x_ws<3>(m, jobs, s);
-            if (m.ws == 5) return launch_poly2x_ws<5>(m, jobs, s);
-            if (m.ws == 13) return launch_poly2x_ws<13>(m, jobs, s);
+            if (m.threads < 64 || m.threads > 512 || m.threads % 32 || m.smem > 200 * 1024) return 1;
+            if (m.ws == 3) return launch_tile2x_ws<3>(m, jobs, s);
+            if (m.ws == 5) return launch_tile2x_ws<5>(m, jobs, s);
+            if (m.ws == 13) return launch_tile2x_ws<13>(m, jobs, s);
             return 2;
         default:
             return 1;

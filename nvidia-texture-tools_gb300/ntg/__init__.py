@@ -84,6 +84,7 @@ def lib():
         "ntg_mip_level": (_i, [_vp, _vp, _i, _i, _vp, _i, _f, _vp, _i, _i, _i, _vp]),
         "ntg_resize": (_i, [_vp, _vp, _i, _i, _vp, _i, _i, _i, _f, _vp, _i, _i, _vp]),
         "ntg_target_extent": (_i, [_i, _i, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+        "ntg_selftest_srgb_quantizer": (_i, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "ntg_encode": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
         "ntg_encode_noalloc": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
         "ntg_chain_levels": (_i, [_i, _i, _i]),
@@ -208,6 +209,12 @@ class Context:
         _check(lib().ntg_mip_level(self.h, src.data_ptr(), w, h, out.data_ptr(), filter, width, ctypes.cast(p, _vp),
                                    wrap, alpha_mode, weighted, _stream_ptr(stream)))
         return out
+
+    def selftest_srgb_quantizer(self) -> int:
+        """Disagreements of the mip kernels' sRGB quantiser with the step search over all floats."""
+        n = ctypes.c_ulonglong()
+        _check(lib().ntg_selftest_srgb_quantizer(self.h, ctypes.byref(n)))
+        return n.value
 
     def resize(self, src, w, h, dw, dh, filter=FILTER_BOX, width=0.0, params=(0.0, 0.0), wrap=WRAP_MIRROR,
                alpha_mode=ALPHA_NONE, out=None, stream=None):

@@ -271,6 +271,12 @@ def test_chain_golden_fixture(ctx):
     assert np.array_equal(out, g["blocks"])
 
 
+def test_srgb_quantizer_bucket_table_is_exact(ctx):
+    """The mip kernels' sRGB quantiser (bucket table + one comparison) against the plain step search,
+    on all 2^32 float bit patterns."""
+    assert ctx.selftest_srgb_quantizer() == 0
+
+
 # ---------------------------------------------------------------------------------------------
 # resize (Surface::resize, the InputOptions resize step)
 
