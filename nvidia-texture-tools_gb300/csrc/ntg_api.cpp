@@ -359,9 +359,17 @@ void group_launches(const std::vector<std::pair<MipKey, MipJob>> &items, const M
         m.first_job = (int)all.size();
         m.njobs = (int)g.second.size();
         m.threads = tune.threads;
-        const int tile_h = std::min(32, std::max(4, tune.strip));
-        if (m.kernel == MIP_POLY2X)
+        int tile_h = std::min(32, std::max(4, tune.strip));
+        if (m.kernel == MIP_POLY2X) {
+            // lower tiles for small levels, so that the launch still spreads over the SMs
+            for (;;) {
+                long long n = 0;
+                for (const MipJob &J : g.second) n += (long long)J.tiles_x * ((J.h + tile_h - 1) / tile_h);
+                if (tile_h <= 4 || n >= 2 * 152) break;
+                tile_h /= 2;
+            }
             for (MipJob &J : g.second) J.strip = tile_h;
+        }
         long long units = 0;
         int rx = 0, ry = 0;
         for (MipJob J : g.second) {
@@ -380,8 +388,13 @@ void group_launches(const std::vector<std::pair<MipKey, MipJob>> &items, const M
 // First destination level of a chain that its tail launch computes (lv.size() = no tail).
 size_t tail_start(const ChainPlan &P, const MipTuning &tune) {
     const long long limit = std::min<long long>(tune.tail_texels, tail_max_texels());
-    for (size_t l = 1; l < P.lv.size(); l++)
-        if ((long long)P.lv[l - 1].w * P.lv[l - 1].h <= limit) return P.lv.size() - l >= 2 ? l : P.lv.size();
+    for (size_t l = 1; l < P.lv.size(); l++) {
+        const Level &S = P.lv[l - 1];
+        // the X pass plane (H x max(1, W/2)) must fit the tail's half-size buffer as well: a 1-wide
+        // level keeps its height there
+        if ((long long)S.w * S.h <= limit && (long long)S.h * std::max(1, S.w / 2) <= tail_max_texels() / 2)
+            return P.lv.size() - l >= 2 ? l : P.lv.size();
+    }
     return P.lv.size();
 }
 

@@ -384,20 +384,27 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
     float4 *tmp = sm4 + (size_t)rh * ROW;       // rh x TW
     __syncthreads();
 
-    // stage the wrapped source window (consecutive threads read consecutive columns)
-    for (int i = tid; i < rh * RW; i += nt) {
-        const int r = i / RW, c = i - r * RW;
-        const int gy = rows_in ? r0 + r : wrap_index(r0 + r, H, wrap);
-        const int gx = cols_in ? c0 + c : wrap_index(c0 + c, W, wrap);
-        const size_t s = (size_t)gy * W + gx;
-        float4 v;
-        if constexpr (SRC_U8) {
-            const uint32_t q = __ldg(L.bgra8 + s);
-            v = make_float4(s_lut[(q >> 16) & 255], s_lut[(q >> 8) & 255], s_lut[q & 255], s_lut[256 + (q >> 24)]);
-        } else {
-            v = make_float4(__ldg(L.src + s), __ldg(L.src + sn + s), __ldg(L.src + 2 * sn + s), __ldg(L.src + 3 * sn + s));
+    // stage the wrapped source window: a warp per row, lanes over consecutive columns
+    const int lane = tid & 31, nwarps = nt >> 5;
+    for (int r = tid >> 5; r < rh; r += nwarps) {
+        const size_t rowoff = (size_t)(rows_in ? r0 + r : wrap_index(r0 + r, H, wrap)) * W;
+        float4 *dst = region + r * ROW;
+#pragma unroll
+        for (int k = 0; k < (RW + 31) / 32; k++) {
+            const int c = lane + 32 * k;
+            if (c < RW) {
+                const size_t s = rowoff + (cols_in ? c0 + c : wrap_index(c0 + c, W, wrap));
+                float4 v;
+                if constexpr (SRC_U8) {
+                    const uint32_t q = __ldg(L.bgra8 + s);
+                    v = make_float4(s_lut[(q >> 16) & 255], s_lut[(q >> 8) & 255], s_lut[q & 255], s_lut[256 + (q >> 24)]);
+                } else {
+                    v = make_float4(__ldg(L.src + s), __ldg(L.src + sn + s), __ldg(L.src + 2 * sn + s),
+                                    __ldg(L.src + 3 * sn + s));
+                }
+                dst[(c & 1) * HALF + (c >> 1)] = v;
+            }
         }
-        region[r * ROW + (c & 1) * HALF + (c >> 1)] = v;
     }
     __syncthreads();
 
@@ -441,6 +448,7 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
 // are consecutive in the list: the first carries the number of levels in tiles_x, and all carry
 // the chain's index in first_unit.
 constexpr int TAIL_MAX = 4096;
+constexpr int TAIL_TAB = 12288;  // words of shared memory for the levels' weights and window starts
 
 __device__ __forceinline__ float fast_box_texel(const float *src, int W, int H, unsigned w, unsigned h, unsigned t) {
     const unsigned x = t % w, y = t / w;
@@ -484,32 +492,57 @@ __device__ __forceinline__ float fast_box_texel(const float *src, int W, int H, 
     return acc * scale;
 }
 
-size_t tail_smem_bytes() { return (size_t)4 * (TAIL_MAX + TAIL_MAX / 2 + TAIL_MAX / 2) * sizeof(float); }
+size_t tail_smem_bytes() {
+    return (size_t)4 * (TAIL_MAX + TAIL_MAX / 2 + TAIL_MAX / 2) * sizeof(float) + TAIL_TAB * sizeof(float);
+}
 
 template <bool WEIGHTED>
-__global__ void __launch_bounds__(256) k_mip_tail(const MipJob *__restrict__ jobs, int njobs) {
+__global__ void __launch_bounds__(1024) k_mip_tail(const MipJob *__restrict__ jobs, int njobs) {
     extern __shared__ float4 sm4[];
     __shared__ float s_steps[256];
-    float *s_a = reinterpret_cast<float *>(sm4);  // source level, 4 planes of up to TAIL_MAX
-    float *s_t = s_a + 4 * TAIL_MAX;              // X pass, 4 planes of up to TAIL_MAX / 2
-    float *s_b = s_t + 2 * TAIL_MAX;              // destination level, 4 planes of up to TAIL_MAX / 2
-    load_steps(jobs, s_steps);
+    __shared__ uint8_t s_buckets[kSrgbBuckets];
+    __shared__ int s_off[16][4];  // per level: offsets of kx, ky, lx, ly in s_tab, or -1 (read from global)
+    float *const lv0 = reinterpret_cast<float *>(sm4);  // levels alternate between two buffers: 4 planes of TAIL_MAX
+    float *const s_t = lv0 + 4 * TAIL_MAX;              // X pass, 4 planes of up to TAIL_MAX / 2
+    float *const lv1 = s_t + 2 * TAIL_MAX;              // 4 planes of up to TAIL_MAX / 2
+    float *const s_tab = lv1 + 2 * TAIL_MAX;            // every level's weights and window starts
+    const int tid = threadIdx.x, nt = blockDim.x;
     int j0 = 0, hi = njobs - 1;  // first job of chain blockIdx.x
     while (j0 < hi) {
         const int mid = (j0 + hi) >> 1;
         if (jobs[mid].first_unit < (long long)blockIdx.x) j0 = mid + 1;
         else hi = mid;
     }
-    const int count = jobs[j0].tiles_x;
+    const int count = min(jobs[j0].tiles_x, 16);
+    const bool quant = jobs[j0].q_out != nullptr, srgb = quant && jobs[j0].xform == 2;
+    if (tid == 0) {  // table layout: each level's tables where they fit, in level order
+        int off = 0;
+        for (int k = 0; k < count; k++) {
+            const MipJob &L = jobs[j0 + k];
+            const int need = L.kx ? L.w * L.wsx + L.h * L.wsy + L.w + L.h : 0;
+            const bool fit = L.kx && off + need <= TAIL_TAB;
+            s_off[k][0] = fit ? off : -1;
+            s_off[k][1] = fit ? off + L.w * L.wsx : -1;
+            s_off[k][2] = fit ? off + L.w * L.wsx + L.h * L.wsy : -1;
+            s_off[k][3] = fit ? off + L.w * L.wsx + L.h * L.wsy + L.w : -1;
+            if (fit) off += need;
+        }
+    }
+    if (quant)
+        for (int i = tid; i < 256; i += nt) s_steps[i] = __ldg(jobs[j0].steps + i);
+    if (srgb)
+        for (int i = tid; i < kSrgbBuckets / 4; i += nt)
+            reinterpret_cast<uint32_t *>(s_buckets)[i] = __ldg(reinterpret_cast<const uint32_t *>(jobs[j0].steps + 256) + i);
     {  // stage the chain's source level
         const MipJob &L = jobs[j0];
         const int n = L.W * L.H;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float *s_a = lv0;
+        for (int i = tid; i < n; i += nt) {
             if (L.src) {
 #pragma unroll
-                for (int c = 0; c < 4; c++) s_a[c * n + i] = L.src[(size_t)c * n + i];
+                for (int c = 0; c < 4; c++) s_a[c * n + i] = __ldg(L.src + (size_t)c * n + i);
             } else {
-                const uint32_t q = L.bgra8[i];
+                const uint32_t q = __ldg(L.bgra8 + i);
                 s_a[i] = __ldg(L.lut + ((q >> 16) & 255));
                 s_a[n + i] = __ldg(L.lut + ((q >> 8) & 255));
                 s_a[2 * n + i] = __ldg(L.lut + (q & 255));
@@ -518,50 +551,71 @@ __global__ void __launch_bounds__(256) k_mip_tail(const MipJob *__restrict__ job
         }
     }
     __syncthreads();
+    for (int k = 0; k < count; k++) {  // all levels' tables at once: one round of global latency
+        const MipJob &L = jobs[j0 + k];
+        if (s_off[k][0] < 0) continue;
+        for (int i = tid; i < L.w * L.wsx; i += nt) s_tab[s_off[k][0] + i] = __ldg(L.kx + i);
+        for (int i = tid; i < L.h * L.wsy; i += nt) s_tab[s_off[k][1] + i] = __ldg(L.ky + i);
+        for (int i = tid; i < L.w; i += nt) reinterpret_cast<int *>(s_tab)[s_off[k][2] + i] = __ldg(L.lx + i);
+        for (int i = tid; i < L.h; i += nt) reinterpret_cast<int *>(s_tab)[s_off[k][3] + i] = __ldg(L.ly + i);
+    }
+    __syncthreads();
     for (int k = 0; k < count; k++) {
         const MipJob &L = jobs[j0 + k];
-        const int W = L.W, H = L.H, w = L.w, h = L.h;
+        const float *src = (k & 1) ? lv1 : lv0;
+        float *dstb = (k & 1) ? lv0 : lv1;
+        const int W = L.W, H = L.H, w = L.w, h = L.h, wrap = L.wrap;
         const int sn = W * H, tn = H * w, dn = w * h;
-        if (L.kx == nullptr) {
-            for (int o = threadIdx.x; o < dn; o += blockDim.x)
-#pragma unroll
-                for (int c = 0; c < 4; c++) s_b[c * dn + o] = fast_box_texel(s_a + c * sn, W, H, w, h, o);
-        } else {
-            for (int i = threadIdx.x; i < tn; i += blockDim.x) {  // X taps of every source row
-                const int x = i % w, y = i / w;
-                const float *kx = L.kx + (size_t)x * L.wsx;
-                const int lx = L.lx[x];
+        const int wsx = L.wsx, wsy = L.wsy;
+        const bool staged = s_off[k][0] >= 0;
+        const float *kxs = staged ? s_tab + s_off[k][0] : L.kx;
+        const float *kys = staged ? s_tab + s_off[k][1] : L.ky;
+        const int *lxs = staged ? reinterpret_cast<const int *>(s_tab) + s_off[k][2] : L.lx;
+        const int *lys = staged ? reinterpret_cast<const int *>(s_tab) + s_off[k][3] : L.ly;
+        if (L.kx) {
+            for (int i = tid; i < tn; i += nt) {  // X taps of every source row
+                const int y = i / w, x = i - y * w;
+                const float *kx = kxs + x * wsx;
+                const int lx = lxs[x];
+                const bool inside = lx >= 0 && lx + wsx <= W;
+                const float *row = src + y * W;
                 float4 sum = make_float4(0, 0, 0, 0);
                 float norm = 0;
-                for (int j = 0; j < L.wsx; j++) {
-                    const int s = y * W + wrap_index(lx + j, W, L.wrap);
-                    tap<WEIGHTED>(sum, norm, kx[j], make_float4(s_a[s], s_a[sn + s], s_a[2 * sn + s], s_a[3 * sn + s]));
+                for (int j = 0; j < wsx; j++) {
+                    const int s = inside ? lx + j : wrap_index(lx + j, W, wrap);
+                    tap<WEIGHTED>(sum, norm, kx[j], make_float4(row[s], row[sn + s], row[2 * sn + s], row[3 * sn + s]));
                 }
                 sum = finish<WEIGHTED>(sum, norm);
                 s_t[i] = sum.x; s_t[tn + i] = sum.y; s_t[2 * tn + i] = sum.z; s_t[3 * tn + i] = sum.w;
             }
             __syncthreads();
-            for (int o = threadIdx.x; o < dn; o += blockDim.x) {  // Y taps
-                const int x = o % w, y = o / w;
-                const float *ky = L.ky + (size_t)y * L.wsy;
-                const int ly = L.ly[y];
+        }
+        for (int o = tid; o < dn; o += nt) {  // Y taps (or the box step), then out to the level
+            float4 v;
+            if (L.kx) {
+                const int y = o / w, x = o - y * w;
+                const float *ky = kys + y * wsy;
+                const int ly = lys[y];
+                const bool inside = ly >= 0 && ly + wsy <= H;
                 float4 sum = make_float4(0, 0, 0, 0);
                 float norm = 0;
-                for (int j = 0; j < L.wsy; j++) {
-                    const int s = wrap_index(ly + j, H, L.wrap) * w + x;
+                for (int j = 0; j < wsy; j++) {
+                    const int s = (inside ? ly + j : wrap_index(ly + j, H, wrap)) * w + x;
                     tap<WEIGHTED>(sum, norm, ky[j], make_float4(s_t[s], s_t[tn + s], s_t[2 * tn + s], s_t[3 * tn + s]));
                 }
-                sum = finish<WEIGHTED>(sum, norm);
-                s_b[o] = sum.x; s_b[dn + o] = sum.y; s_b[2 * dn + o] = sum.z; s_b[3 * dn + o] = sum.w;
+                v = finish<WEIGHTED>(sum, norm);
+            } else {
+                v = make_float4(fast_box_texel(src, W, H, w, h, o), fast_box_texel(src + sn, W, H, w, h, o),
+                                fast_box_texel(src + 2 * sn, W, H, w, h, o), fast_box_texel(src + 3 * sn, W, H, w, h, o));
             }
+            dstb[o] = v.x; dstb[dn + o] = v.y; dstb[2 * dn + o] = v.z; dstb[3 * dn + o] = v.w;
+            L.dst[o] = v.x;
+            L.dst[dn + o] = v.y;
+            L.dst[2 * dn + o] = v.z;
+            L.dst[3 * dn + o] = v.w;
+            if (L.q_out)
+                L.q_out[o] = srgb ? quantize_srgb_bgra(v, s_steps, s_buckets) : quantize_bgra(v.x, v.y, v.z, v.w, L.xform, s_steps);
         }
-        __syncthreads();
-        for (int o = threadIdx.x; o < dn; o += blockDim.x)
-            store_texel(L, (size_t)o, (size_t)dn, make_float4(s_b[o], s_b[dn + o], s_b[2 * dn + o], s_b[3 * dn + o]), s_steps);
-        // the destination becomes the next source (s_b is at most TAIL_MAX / 2 per plane)
-        for (int i = threadIdx.x; i < dn; i += blockDim.x)
-#pragma unroll
-            for (int c = 0; c < 4; c++) s_a[c * dn + i] = s_b[c * dn + i];
         __syncthreads();
     }
 }
@@ -736,8 +790,8 @@ int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s) {
                 cudaFuncSetAttribute(k_mip_tail<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem_bytes());
                 cudaFuncSetAttribute(k_mip_tail<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tail_smem_bytes());
             }
-            if (m.weighted) k_mip_tail<true><<<(unsigned)m.units, 256, tail_smem_bytes(), s>>>(jobs, m.njobs);
-            else k_mip_tail<false><<<(unsigned)m.units, 256, tail_smem_bytes(), s>>>(jobs, m.njobs);
+            if (m.weighted) k_mip_tail<true><<<(unsigned)m.units, 1024, tail_smem_bytes(), s>>>(jobs, m.njobs);
+            else k_mip_tail<false><<<(unsigned)m.units, 1024, tail_smem_bytes(), s>>>(jobs, m.njobs);
             return launch_status();
         }
         case MIP_POLY2X:

@@ -210,6 +210,8 @@ CHAINS = [
     (45, 27, 2, 2, 0, 0, 0, 0, 1),      # BC1a, box, odd sizes
     (64, 48, 6, 1, 1, 0, 0, 0, 2),      # BC4, triangle
     (37, 37, 6, 2, 2, 0, 1, 1, 0),      # BC4 Production, Kaiser, gamma
+    (1, 4096, 4, 1, 2, 0, 0, 0, 2),     # 1-wide and tall: the tail's X plane keeps the full height
+    (4096, 1, 1, 1, 2, 1, 2, 2, 1),     # 1-high and wide, sRGB
 ]
 
 
