@@ -167,6 +167,14 @@ size_t ntg_chain_bytes(int w, int h, const ntg_chain_options *opt);
  * blocks are written back to back, largest level first. */
 int ntg_compress_chain(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
                        void *d_blocks, void *stream);
+/* Many same-shaped images from host memory with the copies overlapped: while image k is encoded on
+ * `stream`, image k+1 is copied in and image k-1's blocks are copied out on two context-owned copy
+ * streams (double-buffered device slots). h_bgra[i]: w*h BGRA8 texels; h_blocks[i]: ntg_chain_bytes
+ * bytes; pinned host memory lets the copies run beside the kernels. Returns when every image's
+ * blocks are on the host. The same loop as n calls of ntg_compress_chain_host; no reference
+ * counterpart (the reference compresses one image per call). */
+int ntg_compress_chains_host(ntg_context *ctx, int n, const void *const *h_bgra, int w, int h,
+                             const ntg_chain_options *opt, void *const *h_blocks, void *stream);
 /* Same from host memory: copies the image in, encodes, copies the blocks out, drains the stream. */
 int ntg_compress_chain_host(ntg_context *ctx, const void *h_bgra, int w, int h, const ntg_chain_options *opt,
                             void *h_blocks, void *stream);

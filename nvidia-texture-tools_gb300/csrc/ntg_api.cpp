@@ -158,7 +158,45 @@ struct ntg_context {
         if (ws) cudaFree(ws);
         if (d_jobs) cudaFree(d_jobs);
         if (d_mipjobs) cudaFree(d_mipjobs);
+        if (slots) cudaFree(slots);
+        for (int i = 0; i < 2; i++) {
+            if (ev_in[i]) cudaEventDestroy(ev_in[i]);
+            if (ev_done[i]) cudaEventDestroy(ev_done[i]);
+            if (ev_out[i]) cudaEventDestroy(ev_out[i]);
+        }
+        if (up) cudaStreamDestroy(up);
+        if (down) cudaStreamDestroy(down);
     }
+
+    // copy streams and slots of ntg_compress_chains_host
+    cudaStream_t up = nullptr, down = nullptr;
+    cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
+    uint8_t *slots = nullptr;
+    size_t slot_in = 0, slot_out = 0;
+
+    int copy_streams() {
+        if (up) return NTG_OK;
+        NTG_CUDA(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking));
+        NTG_CUDA(cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; i++) {
+            NTG_CUDA(cudaEventCreateWithFlags(&ev_in[i], cudaEventDisableTiming));
+            NTG_CUDA(cudaEventCreateWithFlags(&ev_done[i], cudaEventDisableTiming));
+            NTG_CUDA(cudaEventCreateWithFlags(&ev_out[i], cudaEventDisableTiming));
+        }
+        return NTG_OK;
+    }
+
+    // Two input and two output slots of at least these sizes (synchronous growth, between calls).
+    int host_slots(size_t in_bytes, size_t out_bytes) {
+        in_bytes = align_up(in_bytes), out_bytes = align_up(out_bytes);
+        if (slots && in_bytes <= slot_in && out_bytes <= slot_out) return NTG_OK;
+        if (slots) { NTG_CUDA(cudaDeviceSynchronize()); cudaFree(slots); slots = nullptr; }
+        slot_in = std::max(in_bytes, slot_in);
+        slot_out = std::max(out_bytes, slot_out);
+        NTG_CUDA(cudaMalloc((void **)&slots, 2 * (slot_in + slot_out)));
+        return NTG_OK;
+    }
+    static size_t align_up(size_t b) { return (b + 255) / 256 * 256; }
 
     int alloc(void **p, size_t bytes) {
         NTG_CUDA(cudaMalloc(p, bytes));
@@ -940,6 +978,42 @@ int ntg_compress_chain_host(ntg_context *ctx, const void *h_bgra, int w, int h, 
     cudaError_t e = cudaStreamSynchronize(s);
     if (r == NTG_OK && e != cudaSuccess) r = cuda_fail(e, "stream");
     return r;
+}
+
+int ntg_compress_chains_host(ntg_context *ctx, int n, const void *const *h_bgra, int w, int h,
+                             const ntg_chain_options *opt, void *const *h_blocks, void *stream) {
+    g_error.clear();
+    if (!ctx || n < 0 || (n > 0 && (!h_bgra || !h_blocks)) || !opt || w <= 0 || h <= 0)
+        return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    for (int i = 0; i < n; i++)
+        if (!h_bgra[i] || !h_blocks[i]) return fail(NTG_ERROR_INVALID_INPUT, "null image or output");
+    NTG_TRY(check_opts(opt));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    NTG_TRY(ctx->copy_streams());
+    const size_t in_bytes = (size_t)w * h * 4, out_bytes = ntg_chain_bytes(w, h, opt);
+    NTG_TRY(ctx->host_slots(in_bytes, out_bytes));
+    cudaStream_t s = S(stream);
+    uint8_t *in[2] = {ctx->slots, ctx->slots + ctx->slot_in};
+    uint8_t *out[2] = {ctx->slots + 2 * ctx->slot_in, ctx->slots + 2 * ctx->slot_in + ctx->slot_out};
+    // the slots' previous users (an earlier call) are done: they all ended with this call's streams drained
+    for (int i = 0; i < n; i++) {
+        const int k = i & 1;
+        if (i >= 2) NTG_CUDA(cudaStreamWaitEvent(ctx->up, ctx->ev_done[k], 0));      // chain i-2 read in[k]
+        NTG_CUDA(cudaMemcpyAsync(in[k], h_bgra[i], in_bytes, cudaMemcpyHostToDevice, ctx->up));
+        NTG_CUDA(cudaEventRecord(ctx->ev_in[k], ctx->up));
+        NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_in[k], 0));
+        if (i >= 2) NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_out[k], 0));             // blocks of i-2 copied out
+        NTG_TRY(chain_common(ctx, in[k], w, h, opt, out[k], nullptr, s));
+        NTG_CUDA(cudaEventRecord(ctx->ev_done[k], s));
+        NTG_CUDA(cudaStreamWaitEvent(ctx->down, ctx->ev_done[k], 0));
+        NTG_CUDA(cudaMemcpyAsync(h_blocks[i], out[k], out_bytes, cudaMemcpyDeviceToHost, ctx->down));
+        NTG_CUDA(cudaEventRecord(ctx->ev_out[k], ctx->down));
+    }
+    NTG_CUDA(cudaStreamSynchronize(ctx->up));
+    NTG_CUDA(cudaStreamSynchronize(s));
+    NTG_CUDA(cudaStreamSynchronize(ctx->down));
+    return NTG_OK;
 }
 
 int ntg_host_polyphase(int filter, float width, const float *params, int src_len, int dst_len, float *weights,

@@ -91,6 +91,8 @@ def lib():
         "ntg_chain_bytes": (_sz, [_i, _i, ctypes.POINTER(ChainOptions)]),
         "ntg_compress_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
         "ntg_compress_chain_host": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
+        "ntg_compress_chains_host": (_i, [_vp, _i, ctypes.POINTER(_vp), _i, _i, ctypes.POINTER(ChainOptions),
+                                          ctypes.POINTER(_vp), _vp]),
         "ntg_mip_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
         "ntg_decode": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
         "ntg_profile_enable": (_i, [_vp, _i]),
@@ -240,6 +242,18 @@ class Context:
         out = out if out is not None else torch.empty(chain_bytes(w, h, opt), dtype=torch.uint8, device=bgra.device)
         _check(lib().ntg_compress_chain(self.h, bgra.data_ptr(), w, h, ctypes.byref(opt), out.data_ptr(), _stream_ptr(stream)))
         return out
+
+    def compress_chains_host(self, images, w, h, opt: ChainOptions, outs=None, stream=None):
+        """Same-shaped host images through the chain with overlapped copies (ntg_compress_chains_host);
+        returns the list of output arrays."""
+        n = len(images)
+        ins = [np.ascontiguousarray(im) for im in images]
+        if outs is None:
+            outs = [np.empty(chain_bytes(w, h, opt), np.uint8) for _ in range(n)]
+        a = (_vp * max(n, 1))(*[im.ctypes.data for im in ins])
+        b = (_vp * max(n, 1))(*[o.ctypes.data for o in outs])
+        _check(lib().ntg_compress_chains_host(self.h, n, a, w, h, ctypes.byref(opt), b, _stream_ptr(stream)))
+        return outs
 
     def compress_chain_host(self, bgra: np.ndarray, w, h, opt: ChainOptions, out: np.ndarray | None = None, stream=None):
         out = out if out is not None else np.empty(chain_bytes(w, h, opt), np.uint8)

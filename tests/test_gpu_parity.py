@@ -263,6 +263,18 @@ def test_chain_host_variant_matches_device_variant(ctx):
     assert np.array_equal(a, b)
 
 
+def test_chains_host_pipeline_matches_single_calls(ctx):
+    """ntg_compress_chains_host (copies overlapped with the chains, double-buffered slots) gives each
+    image exactly what its own ntg_compress_chain_host call gives."""
+    w, h = 160, 96
+    opt = ntg.ChainOptions.make(format=4, quality=1, filter=2, alpha_mode=1, in_xform=2, out_xform=2)
+    imgs = [synth.colour_texture(w, h, 30 + i, alpha=synth.alpha_field(w, h, 30 + i)) for i in range(5)]
+    outs = ctx.compress_chains_host(imgs, w, h, opt)
+    for img, out in zip(imgs, outs):
+        assert np.array_equal(out, ctx.compress_chain_host(img, w, h, opt))
+    assert ctx.compress_chains_host([], w, h, opt) == []
+
+
 def test_chain_golden_fixture(ctx):
     """The GPU chain against the reference's own bytes (tests/golden/chain_c0.npz)."""
     import os
