@@ -408,35 +408,35 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
     }
     __syncthreads();
 
-    // X taps of every window row: output column x reads source columns 2x .. 2x + WS - 1
-    for (int i = tid; i < rh * TW; i += nt) {
-        const int r = i >> 5, x = i & 31;
-        const float4 *row = region + r * ROW + x;
+    // X taps of every window row: output column x (= lane) reads source columns 2x .. 2x + WS - 1
+    for (int r = tid >> 5; r < rh; r += nwarps) {
+        const float4 *row = region + r * ROW + lane;
         float4 sum = make_float4(0, 0, 0, 0);
         float norm = 0;
 #pragma unroll
         for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, kx[j], row[(j & 1) * HALF + (j >> 1)]);
-        tmp[i] = finish<WEIGHTED>(sum, norm);
+        tmp[r * TW + lane] = finish<WEIGHTED>(sum, norm);
     }
     __syncthreads();
 
     // Y taps: output row y reads window rows 2y .. 2y + WS - 1
-    for (int o = tid; o < th * TW; o += nt) {
-        const int y = o >> 5, x = o & 31;
-        if (y0 + y >= h || x0 + x >= w) continue;
-        const float4 *col = tmp + (2 * y) * TW + x;
+    if (x0 + lane >= w) return;
+    const int ty = min(th, h - y0);
+    float *const dst = L.dst + (size_t)y0 * w + x0 + lane;
+    uint32_t *const qd = L.q_out ? L.q_out + (size_t)y0 * w + x0 + lane : nullptr;
+    for (int y = tid >> 5; y < ty; y += nwarps) {
+        const float4 *col = tmp + (2 * y) * TW + lane;
         float4 sum = make_float4(0, 0, 0, 0);
         float norm = 0;
 #pragma unroll
         for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, ky[j], col[j * TW]);
         const float4 v = finish<WEIGHTED>(sum, norm);
-        const size_t t = (size_t)(y0 + y) * w + x0 + x;
-        L.dst[t] = v.x;
-        L.dst[dn + t] = v.y;
-        L.dst[2 * dn + t] = v.z;
-        L.dst[3 * dn + t] = v.w;
-        if (L.q_out)
-            L.q_out[t] = srgb ? quantize_srgb_bgra(v, s_steps, s_buckets) : quantize_bgra(v.x, v.y, v.z, v.w, L.xform, s_steps);
+        float *const d = dst + (size_t)y * w;
+        d[0] = v.x;
+        d[dn] = v.y;
+        d[2 * dn] = v.z;
+        d[3 * dn] = v.w;
+        if (qd) qd[(size_t)y * w] = srgb ? quantize_srgb_bgra(v, s_steps, s_buckets) : quantize_bgra(v.x, v.y, v.z, v.w, L.xform, s_steps);
     }
 }
 
