@@ -479,10 +479,13 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     }
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
+    // Two float4 arrays and the weights per thread: the reduced colours overwrite the gathered
+    // texels in place (reduce_colors only writes slots it has already read), and the texels are
+    // gathered again for the output stage once the cluster fits are done with the colours.
     Lane<float4> in{smem + t, T};
-    Lane<float4> col{smem + 16 * T + t, T};
-    Lane<float4> sat{smem + 32 * T + t, T};
-    Lane<float> wi{reinterpret_cast<float *>(smem + 48 * T) + t, T};
+    Lane<float4> col = in;
+    Lane<float4> sat{smem + 16 * T + t, T};
+    Lane<float> wi{reinterpret_cast<float *>(smem + 32 * T) + t, T};
     const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
     uint8_t *const out = J.out + 8 * (size_t)blk;
 
@@ -550,13 +553,12 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
         return;
     }
 
-    // compress_dxt1_cluster_fit (src/nvtt/icbc.h:3292-3325)
+    // compress_dxt1_cluster_fit (src/nvtt/icbc.h:3292-3325); both fits first, then the output stage
+    // (pure functions of the texels and the endpoints, so their order does not matter)
     const f3 metric = cw * cw;
     int sn = compute_sat(col, cnt, sat);
-    f3 s0, s1;
+    f3 s0, s1, t0, t1;
     cluster_fit_four(sat, sn, metric, s0, s1);
-    Block1 cf;
-    float cerr = output_block4(in, wi, cw, s0, s1, cf);
     bool run3 = true;
     if (any_black) {
         // skip_blacks in place: compact the non-black colours to the front of `col`
@@ -569,10 +571,13 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
         if (m == 0) run3 = false;
         else sn = compute_sat(col, m, sat);
     }
+    if (run3) cluster_fit_three(sat, sn, metric, t0, t1);
+    gather_block(J, blk, in, wi);
+    Block1 cf;
+    float cerr = output_block4(in, wi, cw, s0, s1, cf);
     if (run3) {
-        cluster_fit_three(sat, sn, metric, s0, s1);
         Block1 c3;
-        float e3 = output_block3(in, wi, cw, true, s0, s1, c3);
+        float e3 = output_block3(in, wi, cw, true, t0, t1, c3);
         if (e3 < cerr) { cerr = e3; cf = c3; }
     }
     // taken only when its error compares below FLT_MAX: a NaN error leaves the block as the
@@ -923,10 +928,13 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
     }
 }
 
+// Shared memory of k_bc1: per thread the texels (then the reduced colours), the SAT and the weights.
+static size_t bc1_fit_smem(int T) { return (size_t)T * (32 * sizeof(float4) + 16 * sizeof(float)); }
+
 int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
     const int T = threads == 32 ? 32 : 64;  // blocks per CTA (one thread per 4x4 block)
-    const size_t sm = (size_t)T * (48 * sizeof(float4) + 16 * sizeof(float));
+    const size_t sm = bc1_fit_smem(T);
     const unsigned grid = (unsigned)((nblocks + T - 1) / T);
     static std::atomic<unsigned long long> configured{0};
     if (first_use_on_device(configured)) {  // the per-thread arrays exceed the 48 KB default
@@ -983,8 +991,8 @@ int launch_bc1_list(const EncJob *d_jobs, int njobs, const long long *list, cons
     if (max_count == 0) return 0;
     const int T = 64;
     static std::atomic<unsigned long long> configured{0};
-    allow_smem(k_bc1<7>, bc1_smem(T), configured);
-    k_bc1<7><<<(unsigned)((max_count + T - 1) / T), T, bc1_smem(T), s>>>(d_jobs, njobs, max_count, list, d_count);
+    allow_smem(k_bc1<7>, bc1_fit_smem(T), configured);
+    k_bc1<7><<<(unsigned)((max_count + T - 1) / T), T, bc1_fit_smem(T), s>>>(d_jobs, njobs, max_count, list, d_count);
     return launch_status();
 }
 
