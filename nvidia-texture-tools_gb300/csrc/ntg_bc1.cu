@@ -861,13 +861,16 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
     if (gblk >= nblocks) return;
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
+    // the layout of k_bc1: colours reduced over the texels in place, texels gathered again for the
+    // output stage
     Lane<float4> in{smem + t, T};
-    Lane<float4> col{smem + 16 * T + t, T};
-    Lane<float4> sat{smem + 32 * T + t, T};
-    Lane<float> wi{reinterpret_cast<float *>(smem + 48 * T) + t, T};
+    Lane<float4> col = in;
+    Lane<float4> sat{smem + 16 * T + t, T};
+    Lane<float> wi{reinterpret_cast<float *>(smem + 32 * T) + t, T};
     const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
     uint8_t *const out = J.out + 8 * (size_t)blk;
     gather_block(J, blk, in, wi);
+    const Frame f = block_frame(in, wi, cw);
     bool any_black = false;
     const int cnt = reduce_colors(in, wi, col, any_black);
     bool take = false;
@@ -876,7 +879,6 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
         store_block(out, cnt == 0 ? Block1{0, 0, 0} : single_colour(col[0]));
     } else {
         const float *yp = y + gblk * 16;
-        const Frame f = block_frame(in, wi, cw);
         const float full_pred = (f.var + 1.0f) * expf(yp[5]) - 1.0f;
         const f3 metric = cw * cw;
         uint64_t order;
@@ -885,11 +887,10 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
         if (axis_reversed(col, sn, order, f.v)) { const float a = q0; q0 = 1 - q2; q1 = 1 - q1; q2 = 1 - a; }
         const int e0 = frac_end(sat, sn, q0), e1 = max(e0, frac_end(sat, sn, q1));
         const int e2 = max(max(e1, 0), frac_end(sat, sn, q2));
-        f3 s0, s1;
+        f3 s0, s1, t0, t1;
         evaluated += pruned_four(sat, sn, metric, e0, e1, e2, radius, s0, s1);
         Block1 o{0, 0, 0}, cf;
         float err = FLT_MAX;
-        float cerr = output_block4(in, wi, cw, s0, s1, cf);
         bool run3 = true;
         if (any_black) {
             int m = 0;
@@ -905,9 +906,13 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
             float r0 = yp[3], r1 = yp[4];
             if (axis_reversed(col, sn, order, f.v)) { const float a = r0; r0 = 1 - r1; r1 = 1 - a; }
             const int f0 = frac_end(sat, sn, r0), f1 = max(max(f0, 0), frac_end(sat, sn, r1));
-            evaluated += pruned_three(sat, sn, metric, f0, f1, radius, s0, s1);
+            evaluated += pruned_three(sat, sn, metric, f0, f1, radius, t0, t1);
+        }
+        gather_block(J, blk, in, wi);
+        float cerr = output_block4(in, wi, cw, s0, s1, cf);
+        if (run3) {
             Block1 b3;
-            float e3 = output_block3(in, wi, cw, true, s0, s1, b3);
+            float e3 = output_block3(in, wi, cw, true, t0, t1, b3);
             if (e3 < cerr) { cerr = e3; cf = b3; }
         }
         if (cerr < err) { o = cf; err = cerr; }
@@ -978,8 +983,8 @@ int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const
     if (nblocks == 0) return 0;
     const int T = 64;
     static std::atomic<unsigned long long> configured{0};
-    allow_smem(k_bc1_learned, bc1_smem(T), configured);
-    k_bc1_learned<<<(unsigned)((nblocks + T - 1) / T), T, bc1_smem(T), s>>>(d_jobs, njobs, nblocks, y, radius, margin,
+    allow_smem(k_bc1_learned, bc1_fit_smem(T), configured);
+    k_bc1_learned<<<(unsigned)((nblocks + T - 1) / T), T, bc1_fit_smem(T), s>>>(d_jobs, njobs, nblocks, y, radius, margin,
                                                                             fallback, stats);
     return launch_status();
 }
