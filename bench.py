@@ -764,7 +764,7 @@ def run_gpu_learned(args):
             "config": {"workload": f"learned endpoint proposal, BC1 Normal: {size}x{size} separate-seed RGBA8 texture "
                                    "(sRGB, alpha field, Kaiser mips, transparency), whole chain",
                        "texels_per_step": texels, "blocks_per_step": nb, "l2": "flushed (256 MiB write) between steps",
-                       "network": "MLP 48-256-256-8, GELU, BF16 weights/activations, FP32 accumulation (tcgen05)",
+                       "network": "MLP 48-256-256-8, GELU (tanh form), BF16 weights/activations, FP32 accumulation (tcgen05)",
                        "training": f"Adam lr {cfg['lr']}, batch {cfg['batch']}, {steps} steps on {cfg['train_blocks']} "
                                    f"seeded blocks of both generators; data {data_s:.1f} s, training {train_s:.1f} s, "
                                    f"loss {float(losses[0]):.4f} -> {float(losses[-64:].mean()):.4f}",

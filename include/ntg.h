@@ -229,7 +229,7 @@ int ntg_batch_proposal_stats(ntg_batch *batch, unsigned long long stats[3]);
 int ntg_batch_destroy(ntg_batch *batch);
 
 /* ---- the learned endpoint proposal's network ----
- * No counterpart in the reference. An MLP 48 -> 256 -> 256 -> 8 (GELU; BF16 weights and
+ * No counterpart in the reference. An MLP 48 -> 256 -> 256 -> 8 (GELU, tanh form; BF16 weights and
  * activations, FP32 accumulation) on the tcgen05 tensor cores: inputs are a 4x4 block's 16 texels
  * in the block's principal frame (centred on its weighted mean colour, divided by its RMS deviation
  * + 1/255, rotated onto the principal axis of its colours and two axes orthogonal to it, sorted

@@ -2,7 +2,8 @@
 
 Compiles in-tree into nvidia-texture-tools_gb300/_build/ with nvcc (kernels) and g++ (host code),
 translation units in parallel, one -gencode. Kernels use --fmad=false and host code
--ffp-contract=off: results must match the reference's CPU arithmetic bit for bit.
+-ffp-contract=off: results must match the reference's CPU arithmetic bit for bit (the learned
+proposal's network, ntg_mlp.cu, has no reference arithmetic and contracts multiply-adds).
 
     python nvidia-texture-tools_gb300/build.py          # incremental
     python nvidia-texture-tools_gb300/build.py --force  # rebuild everything
@@ -30,6 +31,15 @@ HEADERS = ["ntg_device.cuh", "ntg_internal.h", "ntg_host_tables.h"]
 
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+# The learned proposal's network has no reference arithmetic to reproduce (its oracle compares within
+# a tolerance), so its kernels may contract multiply-adds.
+FMAD_ON = {"ntg_mlp.cu"}
+
+
+def nvcc_flags(src: str):
+    return [("--fmad=true" if f == "--fmad=false" and src in FMAD_ON else f) for f in NVCC_FLAGS]
+
+
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + os.path.join(CUDA, "include")]
 
@@ -57,7 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         src, obj = os.path.join(CSRC, s), os.path.join(OUT, s + ".o")
         objs.append(obj)
         if force or _newer([src] + headers, obj):
-            jobs.append([NVCC] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([NVCC] + nvcc_flags(s) + ["-c", src, "-o", obj])
     cxx = shutil.which("g++") or "g++"
     for s in CPP_SOURCES:
         src, obj = os.path.join(CSRC, s), os.path.join(OUT, s + ".o")

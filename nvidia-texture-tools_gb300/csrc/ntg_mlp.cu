@@ -1,5 +1,6 @@
 // The learned endpoint proposal's network on the 5th-generation tensor cores: an MLP
-// 48 -> 256 -> 256 -> 8 (GELU, BF16 weights and activations, FP32 accumulation) trained with Adam.
+// 48 -> 256 -> 256 -> 8 (GELU, tanh form; BF16 weights and activations, FP32 accumulation) trained
+// with Adam.
 // Inputs are a block's 16 texels x RGB; outputs 0-5 are the two endpoints of the block's cluster
 // fit, output 6 the fit's log-error (used to decide when the pruned search falls back to the full
 // one), output 7 is unused. No counterpart in the reference.
@@ -131,9 +132,26 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks & Gimpel, "Gaussian Error Linear Units", 2016):
+// gelu(z) = z / 2 (1 + tanh(sqrt(2 / pi) (z + 0.044715 z^3))), with the hardware tanh
+// (tanh.approx.f32, about 2^-11 relative error, below the BF16 rounding of the activations), and its
+// derivative for training. The network is defined with this activation, in training, inference and
+// the oracle alike.
+__device__ __forceinline__ float tanh_hw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float GELU_S = 0.7978845608028654f;  // sqrt(2 / pi)
+constexpr float GELU_C = 0.044715f;
+__device__ __forceinline__ float gelu(float z) {
+    const float t = tanh_hw(GELU_S * (z + GELU_C * (z * z * z)));
+    return 0.5f * z * (1.0f + t);
+}
 __device__ __forceinline__ float gelu_grad(float z) {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+    const float z2 = z * z;
+    const float t = tanh_hw(GELU_S * (z + GELU_C * (z2 * z)));
+    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * GELU_S * (1.0f + 3.0f * GELU_C * z2);
 }
 
 // Copies rows [r0, r0 + rows) x K-chunk [k0, k0 + BK) of a K-major matrix into the canonical
@@ -406,11 +424,11 @@ __device__ void load_operand(uint8_t *dst, const __nv_bfloat16 *src, int rows, i
     }
 }
 
-// Bias + GELU of this thread's half (128 columns from c_begin) of its row's accumulator, into its
+// Bias + GELU of this thread's quarter (64 columns from c_begin) of its row's accumulator, into its
 // row of the activation operand.
 __device__ __forceinline__ void hidden_epilogue(uint32_t lane_addr, const float *bias, uint8_t *act, int row, int c_begin) {
 #pragma unroll 1
-    for (int c0 = c_begin; c0 < c_begin + HID / 2; c0 += 16) {
+    for (int c0 = c_begin; c0 < c_begin + HID / 4; c0 += 16) {
         float v[16];
         tmem_ld16(lane_addr + c0, v);
         uint32_t p[8];
@@ -421,7 +439,7 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t lane_addr, const float 
     }
 }
 
-__global__ void __launch_bounds__(256, 1) k_mlp_infer(const __nv_bfloat16 *__restrict__ w1, const __nv_bfloat16 *__restrict__ w2,
+__global__ void __launch_bounds__(512, 1) k_mlp_infer(const __nv_bfloat16 *__restrict__ w1, const __nv_bfloat16 *__restrict__ w2,
                                                        const __nv_bfloat16 *__restrict__ w3, const float *__restrict__ b1,
                                                        const float *__restrict__ b2, const float *__restrict__ b3,
                                                        const float *__restrict__ x, long long rows, float *__restrict__ y,
@@ -431,8 +449,9 @@ __global__ void __launch_bounds__(256, 1) k_mlp_infer(const __nv_bfloat16 *__res
     __shared__ uint32_t tmem_base;
     uint8_t *sw1 = smem + F_W1, *sw2 = smem + F_W2, *sw3 = smem + F_W3, *act = smem + F_ACT;
     float *sb = reinterpret_cast<float *>(smem + F_BIAS);
-    // 8 warps: thread t owns row t % 128 (TMEM lane) and half t / 128 of its columns
-    const int warp = threadIdx.x >> 5, row = threadIdx.x & 127, half = threadIdx.x >> 7;
+    // 16 warps: thread t owns row t % 128 (TMEM lane: warp t / 32 reads lane quarter (t / 32) % 4) and
+    // quarter t / 128 of its columns
+    const int warp = threadIdx.x >> 5, row = threadIdx.x & 127, quarter = threadIdx.x >> 7;
     if (warp == 0) tmem_alloc(&tmem_base, 512);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
@@ -453,9 +472,9 @@ __global__ void __launch_bounds__(256, 1) k_mlp_infer(const __nv_bfloat16 *__res
     const long long tiles = (rows + BM - 1) / BM;
     for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         const long long r = tile * BM + row;
-        // X: this thread's half of its row as bf16 (rows past the end are zero)
+        // X: this thread's half of its row as bf16 (rows past the end are zero; quarters 0 and 1)
 #pragma unroll
-        for (int kc = half * (IN / 16); kc < (half + 1) * (IN / 16); kc++) {
+        for (int kc = quarter * (IN / 16); kc < (quarter + 1) * (IN / 16) && quarter < 2; kc++) {
             float4 a = make_float4(0, 0, 0, 0), b = a;
             if (r < rows) {
                 a = *reinterpret_cast<const float4 *>(x + r * IN + kc * 8);
@@ -493,8 +512,8 @@ __global__ void __launch_bounds__(256, 1) k_mlp_infer(const __nv_bfloat16 *__res
             tc_fence_after();
             if (!ok) break;
             if (layer < 2) {
-                hidden_epilogue(lane_addr + (layer == 0 ? 0u : (uint32_t)HID), sb + layer * HID, act, row, half * (HID / 2));
-            } else if (half == 0) {
+                hidden_epilogue(lane_addr + (layer == 0 ? 0u : (uint32_t)HID), sb + layer * HID, act, row, quarter * (HID / 4));
+            } else if (quarter == 0) {
                 float v[16];
                 tmem_ld16(lane_addr, v);
                 if (r < rows) {
@@ -683,7 +702,7 @@ int mlp_forward_device(ntg_mlp *m, const float *d_x, long long rows, float *d_y,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
     const long long tiles = (rows + BM - 1) / BM;
     const int grid = (int)std::min<long long>(tiles, std::max(1, sms));
-    k_mlp_infer<<<grid, 256, F_BYTES, s>>>(m->w1, m->w2, m->w3, m->p + OFF_B1, m->p + OFF_B2, m->b3p, d_x, rows, d_y,
+    k_mlp_infer<<<grid, 512, F_BYTES, s>>>(m->w1, m->w2, m->w3, m->p + OFF_B1, m->p + OFF_B2, m->b3p, d_x, rows, d_y,
                                            m->status);
     MLP_LAUNCH(launch_status());
     return NTG_OK;

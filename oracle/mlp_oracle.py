@@ -38,16 +38,18 @@ def unpack(p):
     return parts
 
 
-def _erf(x):
-    return np.vectorize(math.erf)(x)
+# GELU in its tanh form (Hendrycks & Gimpel 2016), the network's activation, in float64.
+GELU_S = math.sqrt(2.0 / math.pi)
+GELU_C = 0.044715
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(GELU_S * (z + GELU_C * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(GELU_S * (z + GELU_C * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_S * (1.0 + 3.0 * GELU_C * z * z)
 
 
 def forward(p, x):
