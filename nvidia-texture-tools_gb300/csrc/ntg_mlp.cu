@@ -470,17 +470,32 @@ __global__ void __launch_bounds__(512, 1) k_mlp_infer(const __nv_bfloat16 *__res
     uint32_t phase = 0;
     bool ok = true;
     const long long tiles = (rows + BM - 1) / BM;
+    // X of the next tile is loaded into registers while the current tile is in the tensor cores and
+    // the epilogues (quarters 0 and 1: half a row each, rows past the end are zero)
+    constexpr int XC = IN / 16;  // 8-element chunks per half row
+    float4 xr[2 * XC];
+    auto load_x = [&](long long tile) {
+        const long long r = tile * BM + row;
+#pragma unroll
+        for (int k = 0; k < XC; k++) {
+            const int kc = quarter * XC + k;
+            xr[2 * k] = xr[2 * k + 1] = make_float4(0, 0, 0, 0);
+            if (quarter < 2 && tile < tiles && r < rows) {
+                xr[2 * k] = *reinterpret_cast<const float4 *>(x + r * IN + kc * 8);
+                xr[2 * k + 1] = *reinterpret_cast<const float4 *>(x + r * IN + kc * 8 + 4);
+            }
+        }
+    };
+    load_x(blockIdx.x);
     for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         const long long r = tile * BM + row;
-        // X: this thread's half of its row as bf16 (rows past the end are zero; quarters 0 and 1)
+        if (quarter < 2) {
 #pragma unroll
-        for (int kc = quarter * (IN / 16); kc < (quarter + 1) * (IN / 16) && quarter < 2; kc++) {
-            float4 a = make_float4(0, 0, 0, 0), b = a;
-            if (r < rows) {
-                a = *reinterpret_cast<const float4 *>(x + r * IN + kc * 8);
-                b = *reinterpret_cast<const float4 *>(x + r * IN + kc * 8 + 4);
+            for (int k = 0; k < XC; k++) {
+                const float4 a = xr[2 * k], b = xr[2 * k + 1];
+                put8(act, SBO_IN, row, quarter * XC + k,
+                     make_uint4(pack_bf16(a.x, a.y), pack_bf16(a.z, a.w), pack_bf16(b.x, b.y), pack_bf16(b.z, b.w)));
             }
-            put8(act, SBO_IN, row, kc, make_uint4(pack_bf16(a.x, a.y), pack_bf16(a.z, a.w), pack_bf16(b.x, b.y), pack_bf16(b.z, b.w)));
         }
 #pragma unroll 1
         for (int layer = 0; layer < 3 && ok; layer++) {
@@ -511,6 +526,7 @@ __global__ void __launch_bounds__(512, 1) k_mlp_infer(const __nv_bfloat16 *__res
             phase++;
             tc_fence_after();
             if (!ok) break;
+            if (layer == 0) load_x(tile + gridDim.x);  // layer 1 has read this tile's X
             if (layer < 2) {
                 hidden_epilogue(lane_addr + (layer == 0 ? 0u : (uint32_t)HID), sb + layer * HID, act, row, quarter * (HID / 4));
             } else if (quarter == 0) {
