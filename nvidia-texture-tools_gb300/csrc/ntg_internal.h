@@ -69,7 +69,7 @@ namespace ntg {
 int mlp_forward_device(ntg_mlp *m, const float *d_x, long long rows, float *d_y, cudaStream_t s);
 
 // One buildNextMipmap step (source level -> destination level) of one texture. A mip launch walks a
-// list of these: its units (destination texels, tiles or strips, depending on the kernel) are
+// list of these: its units (destination texels or tiles, depending on the kernel) are
 // numbered across the jobs (`first_unit`), so one launch covers the same step of many textures.
 struct MipJob {
     const float *src;        // planar FP32 source level, or null to read bgra8 through lut
@@ -86,7 +86,7 @@ struct MipJob {
     int xform;               // output transform folded into the quantiser (0 none, 1 gamma 2.2, 2 sRGB)
     const float *steps;      // sRGB quantiser steps (xform 2)
     int tiles_x;             // units along x (tail launches: levels in the chain, on its first job)
-    int strip;               // 2:1 kernel: output rows per unit
+    int strip;               // 2:1 kernel: output rows per tile
     int rx_max, ry_max;      // general kernel: widest source window of a tile (host side, for shared memory)
     long long first_unit;    // running unit count of the launch (tail launches: the chain's index)
 };
@@ -101,7 +101,7 @@ struct MipLaunch {
     int first_job, njobs;
     long long units;
     size_t smem;             // dynamic shared memory
-    int threads;             // 2:1 kernel: threads per CTA (one strip per warp)
+    int threads;             // 2:1 kernel: threads per CTA (one tile per CTA)
 };
 
 int launch_set_image(const uint32_t *bgra, size_t n, const float *lut, float *out, cudaStream_t s);
