@@ -208,6 +208,13 @@ typedef struct ntg_batch_texture {
 int ntg_batch_build(ntg_context *ctx, const ntg_batch_texture *textures, int count, ntg_batch **out);
 /* Replays the graph on `stream` (enqueue only). */
 int ntg_batch_launch(ntg_batch *batch, void *stream);
+/* Double buffering: binds a second set of inputs and outputs (d_bgra[i], d_blocks[i] for texture i,
+ * same sizes and options) to the batch, with its own job lists and graph; ntg_batch_launch_alternate
+ * replays that graph. While one binding's graph runs, the other's inputs can be copied in and its
+ * outputs copied out. Both graphs use the batch's workspace: launch them on one stream (or order
+ * them), never concurrently. Autotuning and ntg_batch_set_proposal recapture both. */
+int ntg_batch_bind_alternate(ntg_batch *batch, const void *const *d_bgra, void *const *d_blocks);
+int ntg_batch_launch_alternate(ntg_batch *batch, void *stream);
 /* Times candidate launch shapes on this batch (rows per strip and threads per CTA of the 2:1 mip
  * kernel, the tail threshold, blocks per CTA of each encoder), keeps the fastest, recaptures the
  * graph and stores the choice in the tuning cache. Synchronises `stream`. */

@@ -1123,10 +1123,29 @@ struct ntg_batch {
     int radius = 1;
     float margin = 0.5f;
     uint8_t *d_learn = nullptr;           // network inputs, outputs, full-fit list, statistics
+    // The alternate binding: the same plan over a second set of inputs and outputs, with its own job
+    // lists and graph (double-buffered host copies). Both graphs use the one workspace, so they run
+    // one after the other. `which` selects the binding the planning and launching helpers work on.
+    std::vector<ntg_batch_texture> alt;   // empty: none bound
+    MipJob *d_mip_alt = nullptr;
+    EncJob *d_enc_alt = nullptr;
+    cudaGraph_t graph_alt = nullptr;
+    cudaGraphExec_t exec_alt = nullptr;
+    int which = 0;
+
+    const std::vector<ntg_batch_texture> &io() const { return which ? alt : tex; }
+    MipJob *&dmip() { return which ? d_mip_alt : d_mip; }
+    EncJob *&denc() { return which ? d_enc_alt : d_enc; }
+    cudaGraph_t &gr() { return which ? graph_alt : graph; }
+    cudaGraphExec_t &ex() { return which ? exec_alt : exec; }
 
     ~ntg_batch() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        if (exec_alt) cudaGraphExecDestroy(exec_alt);
+        if (graph_alt) cudaGraphDestroy(graph_alt);
+        if (d_mip_alt) cudaFree(d_mip_alt);
+        if (d_enc_alt) cudaFree(d_enc_alt);
         if (d_ws) cudaFree(d_ws);
         if (d_mip) cudaFree(d_mip);
         if (d_enc) cudaFree(d_enc);
@@ -1180,7 +1199,7 @@ int batch_plan(ntg_batch *b) {
             const ChainPlan &P = b->plans[t];
             if (l >= P.lv.size() || l >= tails[t]) continue;
             items.emplace_back();
-            NTG_TRY(chain_step(ctx, P, l, (const uint32_t *)b->tex[t].d_bgra, b->opts[t], b->xts[t], b->d_ws + b->base[t],
+            NTG_TRY(chain_step(ctx, P, l, (const uint32_t *)b->io()[t].d_bgra, b->opts[t], b->xts[t], b->d_ws + b->base[t],
                                items.back().second, items.back().first));
         }
         std::vector<MipLaunch> stage;
@@ -1194,7 +1213,7 @@ int batch_plan(ntg_batch *b) {
             long long chains = 0;
             for (size_t t = 0; t < n; t++) {
                 if (tails[t] != l || (b->opts[t].weighted != 0) != (weighted != 0)) continue;
-                NTG_TRY(chain_tail(ctx, b->plans[t], l, (const uint32_t *)b->tex[t].d_bgra, b->opts[t], b->xts[t],
+                NTG_TRY(chain_tail(ctx, b->plans[t], l, (const uint32_t *)b->io()[t].d_bgra, b->opts[t], b->xts[t],
                                    b->d_ws + b->base[t], chains++, all));
             }
             if (chains) {
@@ -1213,22 +1232,24 @@ int batch_plan(ntg_batch *b) {
         ntg_batch::Enc e{g.first.first, g.first.second, (int)ejobs.size(), 0, 0};
         long long nb = 0;
         for (size_t t : g.second)
-            chain_jobs(b->plans[t], (const uint32_t *)b->tex[t].d_bgra, b->opts[t], b->xts[t], b->d_ws + b->base[t],
-                       (uint8_t *)b->tex[t].d_blocks, ejobs, nb);
+            chain_jobs(b->plans[t], (const uint32_t *)b->io()[t].d_bgra, b->opts[t], b->xts[t], b->d_ws + b->base[t],
+                       (uint8_t *)b->io()[t].d_blocks, ejobs, nb);
         e.njobs = (int)ejobs.size() - e.first;
         e.nblocks = nb;
         b->encodes.push_back(e);
     }
-    if (b->d_mip) cudaFree(b->d_mip);
-    if (b->d_enc) cudaFree(b->d_enc);
-    b->d_mip = nullptr;
-    b->d_enc = nullptr;
+    MipJob *&dm = b->dmip();
+    EncJob *&de = b->denc();
+    if (dm) cudaFree(dm);
+    if (de) cudaFree(de);
+    dm = nullptr;
+    de = nullptr;
     if (!all.empty()) {
-        NTG_CUDA(cudaMalloc((void **)&b->d_mip, all.size() * sizeof(MipJob)));
-        NTG_CUDA(cudaMemcpy(b->d_mip, all.data(), all.size() * sizeof(MipJob), cudaMemcpyHostToDevice));
+        NTG_CUDA(cudaMalloc((void **)&dm, all.size() * sizeof(MipJob)));
+        NTG_CUDA(cudaMemcpy(dm, all.data(), all.size() * sizeof(MipJob), cudaMemcpyHostToDevice));
     }
-    NTG_CUDA(cudaMalloc((void **)&b->d_enc, ejobs.size() * sizeof(EncJob)));
-    NTG_CUDA(cudaMemcpy(b->d_enc, ejobs.data(), ejobs.size() * sizeof(EncJob), cudaMemcpyHostToDevice));
+    NTG_CUDA(cudaMalloc((void **)&de, ejobs.size() * sizeof(EncJob)));
+    NTG_CUDA(cudaMemcpy(de, ejobs.data(), ejobs.size() * sizeof(EncJob), cudaMemcpyHostToDevice));
     b->launches = (int)b->set_images.size() + (int)b->encodes.size();
     for (const auto &e : b->encodes)
         if (learned_group(b, e)) b->launches += 3;  // features, network, pruned fit, full-fit list
@@ -1239,10 +1260,10 @@ int batch_plan(ntg_batch *b) {
 int batch_mips(ntg_batch *b, cudaStream_t s) {
     for (int t : b->set_images) {
         const ChainPlan &P = b->plans[t];
-        NTG_TRY(launched(launch_set_image((const uint32_t *)b->tex[t].d_bgra, (size_t)P.lv[0].w * P.lv[0].h, b->xts[t]->d_in,
+        NTG_TRY(launched(launch_set_image((const uint32_t *)b->io()[t].d_bgra, (size_t)P.lv[0].w * P.lv[0].h, b->xts[t]->d_in,
                                           (float *)(b->d_ws + b->base[t] + P.f_off[0]), s), "set image"));
     }
-    return run_stages(b->stages, b->d_mip, s);
+    return run_stages(b->stages, b->dmip(), s);
 }
 
 int batch_encodes(ntg_batch *b, cudaStream_t s, int only_slot = -1) {
@@ -1253,7 +1274,7 @@ int batch_encodes(ntg_batch *b, cudaStream_t s, int only_slot = -1) {
             float *x = (float *)(b->d_learn + L.x), *y = (float *)(b->d_learn + L.y);
             long long *list = (long long *)(b->d_learn + L.list);
             unsigned long long *stats = (unsigned long long *)(b->d_learn + L.stats);
-            const EncJob *jobs = b->d_enc + e.first;
+            const EncJob *jobs = b->denc() + e.first;
             NTG_TRY(launched(launch_bc1_features(jobs, e.njobs, e.nblocks, x, s), "block features"));
             const int r = mlp_forward_device(b->mlp, x, e.nblocks, y, s);
             if (r) return fail(r, std::string("proposal network: ") + ntg_last_error_string());
@@ -1263,7 +1284,7 @@ int batch_encodes(ntg_batch *b, cudaStream_t s, int only_slot = -1) {
             NTG_TRY(launched(launch_bc1_list(jobs, e.njobs, list, stats + 1, e.nblocks, s), "full fit of the listed blocks"));
             continue;
         }
-        NTG_TRY(launch_encode(e.format, b->d_enc + e.first, e.njobs, e.nblocks, e.quality, s, b->enc_threads[enc_slot(e.format)]));
+        NTG_TRY(launch_encode(e.format, b->denc() + e.first, e.njobs, e.nblocks, e.quality, s, b->enc_threads[enc_slot(e.format)]));
     }
     return NTG_OK;
 }
@@ -1271,8 +1292,8 @@ int batch_encodes(ntg_batch *b, cudaStream_t s, int only_slot = -1) {
 // Runs the sequence once on a private stream (first-use attributes, and the outputs), then
 // captures it into a graph.
 int batch_capture(ntg_batch *b) {
-    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
-    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    if (b->ex()) { cudaGraphExecDestroy(b->ex()); b->ex() = nullptr; }
+    if (b->gr()) { cudaGraphDestroy(b->gr()); b->gr() = nullptr; }
     cudaStream_t cs;
     NTG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     int r = batch_mips(b, cs);
@@ -1285,16 +1306,30 @@ int batch_capture(ntg_batch *b) {
         else {
             r = batch_mips(b, cs);
             if (r == NTG_OK) r = batch_encodes(b, cs);
-            e = cudaStreamEndCapture(cs, &b->graph);
+            e = cudaStreamEndCapture(cs, &b->gr());
             if (r == NTG_OK && e != cudaSuccess) r = cuda_fail(e, "end capture");
         }
     }
     if (r == NTG_OK) {
-        e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        e = cudaGraphInstantiate(&b->ex(), b->gr(), 0);
         if (e != cudaSuccess) r = cuda_fail(e, "graph instantiate");
     }
     cudaStreamDestroy(cs);
     return r;
+}
+
+// Plans and captures both bindings for the current launch shapes (the alternate one if bound),
+// leaving the primary selected.
+int batch_replan(ntg_batch *b) {
+    if (!b->alt.empty()) {
+        b->which = 1;
+        int r = batch_plan(b);
+        if (r == NTG_OK) r = batch_capture(b);
+        b->which = 0;
+        NTG_TRY(r);
+    }
+    NTG_TRY(batch_plan(b));
+    return batch_capture(b);
 }
 
 // ---- tuning cache: a small JSON file of {"key", launch shape, timings} entries
@@ -1484,6 +1519,34 @@ int ntg_batch_launch(ntg_batch *b, void *stream) {
     return NTG_OK;
 }
 
+int ntg_batch_bind_alternate(ntg_batch *b, const void *const *d_bgra, void *const *d_blocks) {
+    g_error.clear();
+    if (!b || !d_bgra || !d_blocks) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    for (size_t t = 0; t < b->tex.size(); t++)
+        if (!d_bgra[t] || !d_blocks[t]) return fail(NTG_ERROR_INVALID_INPUT, "null input or output");
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    NTG_TRY(ensure_device(b->ctx));
+    b->alt = b->tex;
+    for (size_t t = 0; t < b->alt.size(); t++) {
+        b->alt[t].d_bgra = d_bgra[t];
+        b->alt[t].d_blocks = d_blocks[t];
+    }
+    // the plan (stages, encode groups) is the same for both bindings; only the job lists differ
+    b->which = 1;
+    int r = batch_plan(b);
+    if (r == NTG_OK) r = batch_capture(b);
+    b->which = 0;
+    return r;
+}
+
+int ntg_batch_launch_alternate(ntg_batch *b, void *stream) {
+    g_error.clear();
+    if (!b || !b->exec_alt) return fail(NTG_ERROR_INVALID_INPUT, "no alternate binding");
+    NTG_TRY(ensure_device(b->ctx));
+    NTG_CUDA(cudaGraphLaunch(b->exec_alt, S(stream)));
+    return NTG_OK;
+}
+
 int ntg_batch_autotune(ntg_batch *b, void *stream) {
     g_error.clear();
     if (!b) return fail(NTG_ERROR_INVALID_INPUT, "null batch");
@@ -1526,7 +1589,7 @@ int ntg_batch_autotune(ntg_batch *b, void *stream) {
         b->enc_threads[slot] = best_t;
         enc_total += best_e;
     }
-    NTG_TRY(batch_capture(b));
+    NTG_TRY(batch_replan(b));
     std::vector<TuneEntry> cache = tune_cache_read();
     TuneEntry e;
     e.key = b->key;
@@ -1593,8 +1656,7 @@ int ntg_batch_set_proposal(ntg_batch *b, ntg_mlp *mlp, int radius, float margin)
         if (learned_group(b, e)) nb = std::max(nb, e.nblocks);
     if (b->d_learn) { cudaFree(b->d_learn); b->d_learn = nullptr; }
     if (mlp && nb > 0) NTG_CUDA(cudaMalloc((void **)&b->d_learn, LearnLayout(nb).bytes));
-    NTG_TRY(batch_plan(b));
-    return batch_capture(b);
+    return batch_replan(b);
 }
 
 int ntg_batch_proposal_stats(ntg_batch *b, unsigned long long stats[3]) {

@@ -91,6 +91,8 @@ def lib():
         "ntg_chain_bytes": (_sz, [_i, _i, ctypes.POINTER(ChainOptions)]),
         "ntg_compress_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
         "ntg_compress_chain_host": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
+        "ntg_batch_bind_alternate": (_i, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+        "ntg_batch_launch_alternate": (_i, [_vp, _vp]),
         "ntg_compress_chains_host": (_i, [_vp, _i, ctypes.POINTER(_vp), _i, _i, ctypes.POINTER(ChainOptions),
                                           ctypes.POINTER(_vp), _vp]),
         "ntg_mip_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
@@ -376,8 +378,19 @@ class Batch:
         self.h = ctypes.c_void_p()
         _check(lib().ntg_batch_build(ctx.h, arr, len(textures), ctypes.byref(self.h)))
 
-    def launch(self, stream=None):
-        _check(lib().ntg_batch_launch(self.h, _stream_ptr(stream)))
+    def launch(self, stream=None, alternate=False):
+        fn = lib().ntg_batch_launch_alternate if alternate else lib().ntg_batch_launch
+        _check(fn(self.h, _stream_ptr(stream)))
+
+    def bind_alternate(self, inputs, outputs):
+        """A second set of device inputs and outputs (one per texture, same sizes) with its own graph,
+        replayed by launch(alternate=True); the tensors must outlive the batch."""
+        n = len(self._keep)
+        assert len(inputs) == n and len(outputs) == n
+        self._keep_alt = list(zip(inputs, outputs))
+        a = (_vp * n)(*[x.data_ptr() for x in inputs])
+        b = (_vp * n)(*[y.data_ptr() for y in outputs])
+        _check(lib().ntg_batch_bind_alternate(self.h, a, b))
 
     def autotune(self, stream=None):
         _check(lib().ntg_batch_autotune(self.h, _stream_ptr(stream)))

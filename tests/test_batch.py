@@ -113,6 +113,47 @@ def test_batch_new_inputs_in_same_buffers(ctx, tmp_path, monkeypatch):
         b.close()
 
 
+def test_alternate_binding(ctx, tmp_path, monkeypatch):
+    """A second set of inputs and outputs with its own graph: each binding encodes its own images,
+    replays of either leave the other's outputs alone, and autotuning recaptures both."""
+    import torch
+    monkeypatch.setenv("NTG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    cases = MIXED[:8]
+    _, textures, refs = make_batch(ctx, cases, 400)
+    b = ntg.Batch(ctx, textures)
+    try:
+        alt_in, alt_out, alt_refs = [], [], []
+        for i, (c, t) in enumerate(zip(cases, textures)):
+            img = image(c, 1400 + i)
+            alt_in.append(dev(img.reshape(-1).view(np.uint32)))
+            alt_out.append(torch.zeros_like(t[4]))
+            alt_refs.append(host(ctx.compress_chain(alt_in[-1], c[0], c[1], t[3])))
+        b.bind_alternate(alt_in, alt_out)
+        for y in alt_out:
+            y.zero_()
+        for t in textures:
+            t[4].zero_()
+        b.launch(alternate=True)
+        for y, r in zip(alt_out, alt_refs):
+            assert np.array_equal(host(y), r)
+        for t in textures:
+            assert not host(t[4]).any()
+        b.launch()
+        for t, r in zip(textures, refs):
+            assert np.array_equal(host(t[4]), r)
+        b.autotune()
+        for y in alt_out:
+            y.zero_()
+        b.launch(alternate=True)
+        b.launch()
+        for y, r in zip(alt_out, alt_refs):
+            assert np.array_equal(host(y), r)
+        for t, r in zip(textures, refs):
+            assert np.array_equal(host(t[4]), r)
+    finally:
+        b.close()
+
+
 def test_autotune_keeps_results_and_caches_shape(ctx, tmp_path, monkeypatch):
     cache = tmp_path / "tune.json"
     monkeypatch.setenv("NTG_TUNE_CACHE", str(cache))
