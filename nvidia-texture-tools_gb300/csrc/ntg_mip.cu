@@ -349,6 +349,17 @@ struct Tile2x {
     }
 };
 
+// A source texel as loaded (BGRA8 word or four FP32 planes), converted to float4 when staged.
+template <bool SRC_U8> struct RawTexel;
+template <> struct RawTexel<true> { uint32_t v; };
+template <> struct RawTexel<false> { float4 v; };
+
+template <bool SRC_U8>
+__device__ __forceinline__ void fetch_raw(const MipJob &L, size_t s, size_t sn, RawTexel<SRC_U8> &r) {
+    if constexpr (SRC_U8) r.v = __ldg(L.bgra8 + s);
+    else r.v = make_float4(__ldg(L.src + s), __ldg(L.src + sn + s), __ldg(L.src + 2 * sn + s), __ldg(L.src + 3 * sn + s));
+}
+
 template <int WS, bool WEIGHTED, bool SRC_U8>
 __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jobs, int njobs) {
     using P = Tile2x<WS>;
@@ -384,27 +395,40 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
     float4 *tmp = sm4 + (size_t)rh * ROW;       // rh x TW
     __syncthreads();
 
-    // stage the wrapped source window: a warp per row, lanes over consecutive columns
+    // stage the wrapped source window: a warp per row, lanes over consecutive columns; the next
+    // row's loads are in flight while this row is converted and stored
     const int lane = tid & 31, nwarps = nt >> 5;
-    for (int r = tid >> 5; r < rh; r += nwarps) {
+    constexpr int CPL = (RW + 31) / 32;  // columns per lane
+    auto fetch = [&](int r, RawTexel<SRC_U8> (&raw)[CPL]) {
         const size_t rowoff = (size_t)(rows_in ? r0 + r : wrap_index(r0 + r, H, wrap)) * W;
+#pragma unroll
+        for (int k = 0; k < CPL; k++) {
+            const int c = lane + 32 * k;
+            if (c < RW) fetch_raw<SRC_U8>(L, rowoff + (cols_in ? c0 + c : wrap_index(c0 + c, W, wrap)), sn, raw[k]);
+        }
+    };
+    RawTexel<SRC_U8> cur[CPL], nxt[CPL];
+    int r = tid >> 5;
+    if (r < rh) fetch(r, cur);
+    for (; r < rh; r += nwarps) {
+        if (r + nwarps < rh) fetch(r + nwarps, nxt);
         float4 *dst = region + r * ROW;
 #pragma unroll
-        for (int k = 0; k < (RW + 31) / 32; k++) {
+        for (int k = 0; k < CPL; k++) {
             const int c = lane + 32 * k;
             if (c < RW) {
-                const size_t s = rowoff + (cols_in ? c0 + c : wrap_index(c0 + c, W, wrap));
                 float4 v;
                 if constexpr (SRC_U8) {
-                    const uint32_t q = __ldg(L.bgra8 + s);
+                    const uint32_t q = cur[k].v;
                     v = make_float4(s_lut[(q >> 16) & 255], s_lut[(q >> 8) & 255], s_lut[q & 255], s_lut[256 + (q >> 24)]);
                 } else {
-                    v = make_float4(__ldg(L.src + s), __ldg(L.src + sn + s), __ldg(L.src + 2 * sn + s),
-                                    __ldg(L.src + 3 * sn + s));
+                    v = cur[k].v;
                 }
                 dst[(c & 1) * HALF + (c >> 1)] = v;
             }
         }
+#pragma unroll
+        for (int k = 0; k < CPL; k++) cur[k] = nxt[k];
     }
     __syncthreads();
 
