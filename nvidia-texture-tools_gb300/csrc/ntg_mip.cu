@@ -380,9 +380,6 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
     }
     if constexpr (SRC_U8)
         for (int i = tid; i < 512; i += nt) s_lut[i] = __ldg(L.lut + i);
-    float kx[WS], ky[WS];
-#pragma unroll
-    for (int j = 0; j < WS; j++) { kx[j] = __ldg(L.kx + j); ky[j] = __ldg(L.ky + j); }
     const int th = L.strip;
     const int rh = P::rows(th);
     const long long lu = (long long)blockIdx.x - L.first_unit;
@@ -407,11 +404,18 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
             if (c < RW) fetch_raw<SRC_U8>(L, rowoff + (cols_in ? c0 + c : wrap_index(c0 + c, W, wrap)), sn, raw[k]);
         }
     };
-    RawTexel<SRC_U8> cur[CPL], nxt[CPL];
+    // rows in flight ahead of the one being stored: two for BGRA8 words, one for FP32 texels
+    constexpr int AHEAD = SRC_U8 ? 2 : 1;
+    RawTexel<SRC_U8> cur[CPL], nxt[CPL], nxt2[CPL];
     int r = tid >> 5;
     if (r < rh) fetch(r, cur);
+    if (AHEAD > 1 && r + nwarps < rh) fetch(r + nwarps, nxt);
     for (; r < rh; r += nwarps) {
-        if (r + nwarps < rh) fetch(r + nwarps, nxt);
+        if (AHEAD > 1) {
+            if (r + 2 * nwarps < rh) fetch(r + 2 * nwarps, nxt2);
+        } else if (r + nwarps < rh) {
+            fetch(r + nwarps, nxt);
+        }
         float4 *dst = region + r * ROW;
 #pragma unroll
         for (int k = 0; k < CPL; k++) {
@@ -428,9 +432,17 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
             }
         }
 #pragma unroll
-        for (int k = 0; k < CPL; k++) cur[k] = nxt[k];
+        for (int k = 0; k < CPL; k++) {
+            cur[k] = nxt[k];
+            if (AHEAD > 1) nxt[k] = nxt2[k];
+        }
     }
     __syncthreads();
+
+    // the taps (the same for every output), loaded after the staging to keep its registers free
+    float kx[WS], ky[WS];
+#pragma unroll
+    for (int j = 0; j < WS; j++) { kx[j] = __ldg(L.kx + j); ky[j] = __ldg(L.ky + j); }
 
     // X taps of every window row: output column x (= lane) reads source columns 2x .. 2x + WS - 1
     for (int r = tid >> 5; r < rh; r += nwarps) {
