@@ -549,12 +549,22 @@ __global__ void __launch_bounds__(1024) k_mip_tail(const MipJob *__restrict__ jo
         if (jobs[mid].first_unit < (long long)blockIdx.x) j0 = mid + 1;
         else hi = mid;
     }
+    // the chain's job records, copied to shared memory once (every thread reads them every level)
+    __shared__ MipJob s_jobs[16];
     const int count = min(jobs[j0].tiles_x, 16);
-    const bool quant = jobs[j0].q_out != nullptr, srgb = quant && jobs[j0].xform == 2;
+    {
+        static_assert(sizeof(MipJob) % 8 == 0, "job records copy as 8-byte words");
+        const unsigned long long *src = reinterpret_cast<const unsigned long long *>(jobs + j0);
+        unsigned long long *dst = reinterpret_cast<unsigned long long *>(s_jobs);
+        const int words = count * (int)(sizeof(MipJob) / 8);
+        for (int i = tid; i < words; i += nt) dst[i] = __ldg(src + i);
+    }
+    __syncthreads();
+    const bool quant = s_jobs[0].q_out != nullptr, srgb = quant && s_jobs[0].xform == 2;
     if (tid == 0) {  // table layout: each level's tables where they fit, in level order
         int off = 0;
         for (int k = 0; k < count; k++) {
-            const MipJob &L = jobs[j0 + k];
+            const MipJob &L = s_jobs[k];
             const int need = L.kx ? L.w * L.wsx + L.h * L.wsy + L.w + L.h : 0;
             const bool fit = L.kx && off + need <= TAIL_TAB;
             s_off[k][0] = fit ? off : -1;
@@ -565,12 +575,12 @@ __global__ void __launch_bounds__(1024) k_mip_tail(const MipJob *__restrict__ jo
         }
     }
     if (quant)
-        for (int i = tid; i < 256; i += nt) s_steps[i] = __ldg(jobs[j0].steps + i);
+        for (int i = tid; i < 256; i += nt) s_steps[i] = __ldg(s_jobs[0].steps + i);
     if (srgb)
         for (int i = tid; i < kSrgbBuckets / 4; i += nt)
-            reinterpret_cast<uint32_t *>(s_buckets)[i] = __ldg(reinterpret_cast<const uint32_t *>(jobs[j0].steps + 256) + i);
+            reinterpret_cast<uint32_t *>(s_buckets)[i] = __ldg(reinterpret_cast<const uint32_t *>(s_jobs[0].steps + 256) + i);
     {  // stage the chain's source level
-        const MipJob &L = jobs[j0];
+        const MipJob &L = s_jobs[0];
         const int n = L.W * L.H;
         float *s_a = lv0;
         for (int i = tid; i < n; i += nt) {
@@ -588,7 +598,7 @@ __global__ void __launch_bounds__(1024) k_mip_tail(const MipJob *__restrict__ jo
     }
     __syncthreads();
     for (int k = 0; k < count; k++) {  // all levels' tables at once: one round of global latency
-        const MipJob &L = jobs[j0 + k];
+        const MipJob &L = s_jobs[k];
         if (s_off[k][0] < 0) continue;
         for (int i = tid; i < L.w * L.wsx; i += nt) s_tab[s_off[k][0] + i] = __ldg(L.kx + i);
         for (int i = tid; i < L.h * L.wsy; i += nt) s_tab[s_off[k][1] + i] = __ldg(L.ky + i);
@@ -597,7 +607,7 @@ __global__ void __launch_bounds__(1024) k_mip_tail(const MipJob *__restrict__ jo
     }
     __syncthreads();
     for (int k = 0; k < count; k++) {
-        const MipJob &L = jobs[j0 + k];
+        const MipJob &L = s_jobs[k];
         const float *src = (k & 1) ? lv1 : lv0;
         float *dstb = (k & 1) ? lv0 : lv1;
         const int W = L.W, H = L.H, w = L.w, h = L.h, wrap = L.wrap;
