@@ -120,7 +120,7 @@ struct AxisTable {
 struct MipTuning {
     int strip = 16;
     int threads = 512;
-    long long tail_texels = 4096;  // a chain's remaining levels go to one tail CTA from a source this small
+    long long tail_texels = 1024;  // a chain's remaining levels go to one tail CTA from a source this small
 };
 
 // Device copy of one 256-entry table set for an (in, out, gamma) transform combination.
@@ -1336,7 +1336,7 @@ int batch_replan(ntg_batch *b) {
 
 struct TuneEntry {
     std::string key;
-    int strip = 16, threads = 512, tail = 4096, bc1 = 64, bc3 = 128, bc5 = 128;
+    int strip = 16, threads = 512, tail = 1024, bc1 = 64, bc3 = 128, bc5 = 128;
     double mip_ms = 0, encode_ms = 0;
 };
 
@@ -1384,7 +1384,7 @@ std::vector<TuneEntry> tune_cache_read() {
         e.key = obj.substr(k0 + 1, k1 - k0 - 1);
         e.strip = (int)json_number(obj, "strip", 16);
         e.threads = (int)json_number(obj, "threads", 512);
-        e.tail = (int)json_number(obj, "tail", 4096);
+        e.tail = (int)json_number(obj, "tail", 1024);
         e.bc1 = (int)json_number(obj, "bc1", 64);
         e.bc3 = (int)json_number(obj, "bc3", 128);
         e.bc5 = (int)json_number(obj, "bc5", 128);
