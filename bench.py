@@ -397,7 +397,7 @@ def run_gpu(args):
         fp32_peak = 152 * 128 * sm_mhz_m * 1e6
         roof_hbm = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
                     "traffic": None, "kernel": "mip launches of the chain (k_tile2x for the 2:1 steps, k_mip_tail for the "
-                                              "levels below 64x64)",
+                                              "levels from 32x32 down)",
                     "algorithmic_bytes": mip_bytes, "ms": mips_ms, "peak_source": peak_src,
                     "fp32_ops": mip_ops, "fp32_frac": mip_ops / (mips_ms / 1000.0) / fp32_peak,
                     "note": "the Kaiser filter is FP32-bound before it is HBM-bound: 312 FP32 instructions per output "
