@@ -114,6 +114,7 @@ struct AxisTable {
     std::vector<int> left;
     bool half = false;  // exact 2:1 with every output on the same taps (left[i] = left0 + 2i, equal rows)
     int left0 = 0;
+    std::vector<float> row0;  // taps of output 0
 };
 
 // Launch shape of the 2:1 mip kernel (output rows per tile, threads per CTA).
@@ -227,6 +228,7 @@ struct ntg_context {
         t.left.resize(dst);
         build_polyphase(filter, width, p0, p1, src, dst, w.data(), t.left.data());
         t.left0 = t.left[0];
+        t.row0.assign(w.begin(), w.begin() + t.ws);
         t.half = src == 2 * dst;
         for (int i = 1; i < dst && t.half; i++) {
             t.half = t.left[i] == t.left0 + 2 * i &&
@@ -338,8 +340,12 @@ ChainPlan plan_chain(int w, int h, const ntg_chain_options &o, bool keep_level0_
 
 struct MipKey {
     int kernel, ws, weighted, u8;
+    // the BGRA8 tile kernel loads these once per launch: its jobs must share them
+    const float *lut = nullptr, *steps = nullptr;
+    std::vector<float> taps;
     bool operator<(const MipKey &o) const {
-        return std::tie(kernel, ws, weighted, u8) < std::tie(o.kernel, o.ws, o.weighted, o.u8);
+        return std::tie(kernel, ws, weighted, u8, lut, steps, taps) <
+               std::tie(o.kernel, o.ws, o.weighted, o.u8, o.lut, o.steps, o.taps);
     }
 };
 
@@ -363,6 +369,14 @@ int plan_step(ntg_context *ctx, const ntg_chain_options &o, float width, const f
     if (!ax || !ay) return fail(NTG_ERROR_CUDA, "polyphase table upload failed");
     J.wsx = ax->ws; J.wsy = ay->ws; J.kx = ax->d_w; J.ky = ay->d_w; J.lx = ax->d_left; J.ly = ay->d_left;
     const int weighted = o.weighted != 0, u8 = src == nullptr;
+    if (u8 && ax->half && ay->half && ax->ws == ay->ws && ((ax->left0 % 4) + 4) % 4 == tile_u8_phase(ax->ws)) {
+        J.cx = ax->left0; J.cy = ay->left0;
+        J.tiles_x = (D.w + tile_u8_w() - 1) / tile_u8_w();
+        J.strip = tile_u8_h();
+        key = {MIP_TILE_U8, ax->ws, weighted, u8, lut, steps, ax->row0};
+        key.taps.insert(key.taps.end(), ay->row0.begin(), ay->row0.end());
+        return NTG_OK;
+    }
     if (ax->half && ay->half && ax->ws == ay->ws && poly2x_supported(ax->ws)) {
         J.cx = ax->left0; J.cy = ay->left0;
         J.tiles_x = (D.w + 31) / 32;
@@ -381,7 +395,7 @@ int plan_step(ntg_context *ctx, const ntg_chain_options &o, float width, const f
 
 long long mip_units(const MipKey &k, const MipJob &J) {
     if (k.kernel == MIP_FAST_BOX) return (long long)J.w * J.h;
-    if (k.kernel == MIP_POLY2X) return (long long)J.tiles_x * ((J.h + J.strip - 1) / J.strip);
+    if (k.kernel == MIP_POLY2X || k.kernel == MIP_TILE_U8) return (long long)J.tiles_x * ((J.h + J.strip - 1) / J.strip);
     return (long long)J.tiles_x * ((J.h + poly_tile_h() - 1) / poly_tile_h());
 }
 
@@ -419,6 +433,7 @@ void group_launches(const std::vector<std::pair<MipKey, MipJob>> &items, const M
         }
         m.units = units;
         m.smem = m.kernel == MIP_POLY ? poly_smem_bytes(rx, ry) : m.kernel == MIP_POLY2X ? poly2x_smem_bytes(m.ws, tile_h) : 0;
+        if (m.kernel == MIP_TILE_U8) m.threads = 1024;  // shared memory sized inside the launcher
         out.push_back(m);
     }
 }

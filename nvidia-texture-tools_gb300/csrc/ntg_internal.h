@@ -91,7 +91,7 @@ struct MipJob {
     long long first_unit;    // running unit count of the launch (tail launches: the chain's index)
 };
 
-enum MipKernel { MIP_FAST_BOX = 0, MIP_POLY = 1, MIP_POLY2X = 2, MIP_TAIL = 3 };
+enum MipKernel { MIP_FAST_BOX = 0, MIP_POLY = 1, MIP_POLY2X = 2, MIP_TAIL = 3, MIP_TILE_U8 = 4 };
 
 // One launch over jobs [first_job, first_job + njobs) of a device job array.
 struct MipLaunch {
@@ -109,6 +109,11 @@ int launch_quantize(const float *rgba, size_t n, int xform, const float *steps, 
 int launch_transform(float *rgba, size_t n, int kind, float p, cudaStream_t s);
 int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s);
 bool poly2x_supported(int ws);
+// 2:1 steps from the BGRA8 input (persistent, cp.async-pipelined 64 x 16 tiles): the window start of
+// output column 0 mod 4 that the kernel for `ws` taps is built for (-1: none), and the tile size.
+int tile_u8_phase(int ws);
+int tile_u8_w();
+int tile_u8_h();
 size_t poly_smem_bytes(int rx_max, int ry_max);
 size_t poly2x_smem_bytes(int ws, int tile_h);  // dynamic shared memory of a 2:1 tile launch
 int poly_tile_w();

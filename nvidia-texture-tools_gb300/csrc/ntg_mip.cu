@@ -8,6 +8,8 @@
 // Exactness: kernels are built with --fmad=false; polyphase weights and window offsets come from
 // the host (computed with the reference's own float/double steps), and every output is the
 // sequential tap-order sum the reference computes, so levels are bit-identical to the CPU path.
+#include <algorithm>
+
 #include "ntg_device.cuh"
 #include "ntg_internal.h"
 
@@ -151,8 +153,8 @@ __global__ void k_fast_down(const MipJob *__restrict__ jobs, int njobs, long lon
         const float *src0 = L.src;
         const unsigned w = W / 2 > 1 ? (unsigned)W / 2 : 1u, h = H / 2 > 1 ? (unsigned)H / 2 : 1u;
         const size_t sn = (size_t)W * H, dn = (size_t)w * h;
-        const size_t t = (size_t)(u - L.first_unit);
-        const unsigned x = (unsigned)(t % w), y = (unsigned)(t / w);
+        const unsigned t = (unsigned)(u - L.first_unit);  // levels hold < 2^32 texels: 32-bit division
+        const unsigned x = t % w, y = t / w;
         float v[4];
 #pragma unroll
         for (int c = 0; c < 4; c++) {
@@ -382,8 +384,8 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
         for (int i = tid; i < 512; i += nt) s_lut[i] = __ldg(L.lut + i);
     const int th = L.strip;
     const int rh = P::rows(th);
-    const long long lu = (long long)blockIdx.x - L.first_unit;
-    const int x0 = (int)(lu % L.tiles_x) * TW, y0 = (int)(lu / L.tiles_x) * th;
+    const unsigned lu = (unsigned)((long long)blockIdx.x - L.first_unit), tx = (unsigned)L.tiles_x;
+    const int x0 = (int)(lu % tx) * TW, y0 = (int)(lu / tx) * th;
     const int W = L.W, H = L.H, w = L.w, h = L.h, wrap = L.wrap;
     const int c0 = 2 * x0 + L.cx, r0 = 2 * y0 + L.cy;
     const bool cols_in = c0 >= 0 && c0 + RW <= W, rows_in = r0 >= 0 && r0 + rh <= H;
@@ -473,6 +475,188 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
         d[2 * dn] = v.z;
         d[3 * dn] = v.w;
         if (qd) qd[(size_t)y * w] = srgb ? quantize_srgb_bgra(v, s_steps, s_buckets) : quantize_bgra(v.x, v.y, v.z, v.w, L.xform, s_steps);
+    }
+}
+
+// 2:1 steps that read the BGRA8 input (the first step of a chain): a persistent kernel, one
+// 1024-thread CTA per SM walking 64 x 16 output tiles with one barrier per tile. A tile's source
+// window of BGRA8 words is copied into shared memory with cp.async while the previous tile is
+// filtered. Each warp then takes whole source rows: it converts the row's words through the input
+// table into its own scratch row, as float4 columns split by column mod 4 (a lane that computes two
+// adjacent outputs then reads consecutive float4 at every tap, and each texel it loads serves both
+// outputs), and writes the row's X taps to the tile's X plane. In the same phase the other warps run
+// the Y taps of the previous tile from the other X plane, two output rows of one column per thread.
+// Every sum starts at 0 and takes its taps in window order, as in applyKernelX/Y
+// (src/nvimage/FloatImage.cpp:1115-1176), so the levels equal k_tile2x's. The input table, the
+// quantiser tables and the taps are the same for every job of a launch (the host groups by them).
+template <int WS>
+struct TileU8 {
+    static constexpr int TW = 64, TH = 16, WARPS = 32;
+    static constexpr int D = WS == 3 ? 0 : 3;            // window start of output column 0, mod 4 (-5, -1, 0)
+    static constexpr int RW = 2 * (TW - 1) + WS;          // source columns of a tile
+    static constexpr int NC = (D + RW + 3) / 4 * 4;       // staged columns, from a multiple of 4
+    static constexpr int QP = (NC / 4 + 1) / 8 * 8 + 6;   // float4 per column class of a scratch row,
+                                                          // = 6 mod 8: conflict-free class-split stores
+    static constexpr int ROWS = 2 * (TH - 1) + WS;        // source rows of a tile
+    static constexpr size_t RAW_WORDS = (size_t)ROWS * NC;
+    static constexpr size_t XPLANE = (size_t)ROWS * TW;   // float4
+    static constexpr size_t smem() { return (2 * XPLANE + (size_t)WARPS * 4 * QP) * 16 + 2 * RAW_WORDS * 4; }
+};
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+struct TilePos {
+    const MipJob *L;
+    int x0, y0;   // first output column / row
+    int a0, r0;   // first staged source column (a multiple of 4) / row, before wrapping
+    bool inner;   // window inside the level, rows 16-byte aligned: whole-vector copies
+};
+
+template <int WS>
+__device__ __forceinline__ TilePos tile_u8_pos(const MipJob *__restrict__ jobs, int njobs, long long u) {
+    using P = TileU8<WS>;
+    const MipJob &L = jobs[find_mip_job(jobs, njobs, u)];
+    const unsigned lu = (unsigned)(u - L.first_unit), tx = (unsigned)L.tiles_x;  // 32-bit division
+    TilePos p;
+    p.L = &L;
+    p.x0 = (int)(lu % tx) * P::TW;
+    p.y0 = (int)(lu / tx) * P::TH;
+    p.a0 = 2 * p.x0 + L.cx - P::D;
+    p.r0 = 2 * p.y0 + L.cy;
+    p.inner = p.a0 >= 0 && p.a0 + P::NC <= L.W && p.r0 >= 0 && p.r0 + P::ROWS <= L.H && (L.W & 3) == 0 &&
+              ((uintptr_t)L.bgra8 & 15) == 0;
+    return p;
+}
+
+// Issues the copies of a tile's source window (ROWS x NC words, wrapped at the level's edges).
+template <int WS>
+__device__ __forceinline__ void tile_u8_fetch(const TilePos &p, uint32_t *raw) {
+    using P = TileU8<WS>;
+    const MipJob &L = *p.L;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (p.inner) {
+        constexpr int CH = P::NC / 4;
+        for (int i = tid; i < P::ROWS * CH; i += nt) {
+            const int r = i / CH, k = i - r * CH;
+            cp_async16(raw + r * P::NC + 4 * k, L.bgra8 + (size_t)(p.r0 + r) * L.W + p.a0 + 4 * k);
+        }
+    } else {
+        for (int i = tid; i < P::ROWS * P::NC; i += nt) {
+            const int r = i / P::NC, c = i - r * P::NC;
+            const int sy = wrap_index(p.r0 + r, L.H, L.wrap), sx = wrap_index(p.a0 + c, L.W, L.wrap);
+            cp_async4(raw + i, L.bgra8 + (size_t)sy * L.W + sx);
+        }
+    }
+    cp_async_commit();
+}
+
+template <int WS, bool WEIGHTED>
+__global__ void __launch_bounds__(1024, 1) k_tile2x_u8(const MipJob *__restrict__ jobs, int njobs, long long units) {
+    using P = TileU8<WS>;
+    constexpr int TW = P::TW, TH = P::TH, D = P::D, NC = P::NC, QP = P::QP, ROWS = P::ROWS;
+    extern __shared__ float4 sm4[];
+    __shared__ float s_steps[256];
+    __shared__ float s_lut[512];
+    __shared__ uint8_t s_buckets[kSrgbBuckets];
+    __shared__ float s_ky[WS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float4 *const xplane0 = sm4;                                   // 2 x ROWS x TW
+    float4 *const scratch = sm4 + 2 * P::XPLANE + warp * 4 * QP;   // this warp's converted row
+    uint32_t *const raw0 = reinterpret_cast<uint32_t *>(sm4 + 2 * P::XPLANE + P::WARPS * 4 * QP);  // 2 x ROWS x NC
+    const long long g = gridDim.x;
+    if (blockDim.x != 32 * P::WARPS || (long long)blockIdx.x >= units) return;
+
+    // tables and taps, shared by every job of the launch
+    const MipJob &J0 = jobs[0];
+    for (int i = tid; i < 512; i += blockDim.x) s_lut[i] = __ldg(J0.lut + i);
+    if (tid < WS) s_ky[tid] = __ldg(J0.ky + tid);
+    if (J0.steps) {
+        for (int i = tid; i < 256; i += blockDim.x) s_steps[i] = __ldg(J0.steps + i);
+        const uint32_t *b = reinterpret_cast<const uint32_t *>(J0.steps + 256);
+        for (int i = tid; i < kSrgbBuckets / 4; i += blockDim.x) reinterpret_cast<uint32_t *>(s_buckets)[i] = __ldg(b + i);
+    }
+    float kx[WS];
+#pragma unroll
+    for (int j = 0; j < WS; j++) kx[j] = __ldg(J0.kx + j);
+
+    // iteration i converts and X-filters tile blockIdx + i g and Y-filters tile blockIdx + (i - 1) g
+    const long long n = (units - blockIdx.x + g - 1) / g;
+    tile_u8_fetch<WS>(tile_u8_pos<WS>(jobs, njobs, blockIdx.x), raw0);
+    for (long long i = 0; i <= n; i++) {
+        cp_async_wait<0>();
+        __syncthreads();  // tile i's words are in; iteration i - 1 is done with raw[(i + 1) % 2] and the X planes
+        if (i + 1 < n) tile_u8_fetch<WS>(tile_u8_pos<WS>(jobs, njobs, blockIdx.x + (i + 1) * g), raw0 + ((i + 1) & 1) * P::RAW_WORDS);
+        const uint32_t *const raw = raw0 + (i & 1) * P::RAW_WORDS;
+        float4 *const xp = xplane0 + (i & 1) * P::XPLANE;
+        const float4 *const yp = xplane0 + ((i + 1) & 1) * P::XPLANE;
+        const int nx = i < n ? ROWS : 0, ny = i > 0 ? TH : 0;
+        for (int item = warp; item < nx + ny; item += P::WARPS) {
+            if (item < nx) {
+                // convert source row `item`: staged column c -> class c % 4, slot c / 4
+                const int r = item;
+                __syncwarp();  // the warp's previous row has been read
+#pragma unroll
+                for (int c = lane; c < NC; c += 32) {
+                    const uint32_t q = raw[r * NC + c];
+                    scratch[(c & 3) * QP + (c >> 2)] =
+                        make_float4(s_lut[(q >> 16) & 255], s_lut[(q >> 8) & 255], s_lut[q & 255], s_lut[256 + (q >> 24)]);
+                }
+                __syncwarp();
+                // X taps: lane -> output columns 2 lane, 2 lane + 1 = staged columns D + 4 lane + t,
+                // t in [0, WS) and [2, WS + 2)
+                float4 s0 = make_float4(0, 0, 0, 0), s1 = s0;
+                float n0 = 0, n1 = 0;
+#pragma unroll
+                for (int t = 0; t < WS + 2; t++) {
+                    const float4 v = scratch[((D + t) & 3) * QP + ((D + t) >> 2) + lane];
+                    if (t < WS) tap<WEIGHTED>(s0, n0, kx[t], v);
+                    if (t >= 2) tap<WEIGHTED>(s1, n1, kx[t - 2], v);
+                }
+                xp[r * TW + 2 * lane] = finish<WEIGHTED>(s0, n0);
+                xp[r * TW + 2 * lane + 1] = finish<WEIGHTED>(s1, n1);
+            } else {
+                // Y taps of tile i - 1: output rows 2 p, 2 p + 1 (p = k / 2) of column 32 (k % 2) + lane
+                // read X rows 4 p + t, t in [0, WS) and [2, WS + 2)
+                const int k = item - nx, p = k >> 1, x = 32 * (k & 1) + lane;
+                const float4 *const col = yp + (4 * p) * TW + x;
+                float4 s0 = make_float4(0, 0, 0, 0), s1 = s0;
+                float n0 = 0, n1 = 0;
+#pragma unroll
+                for (int t = 0; t < WS + 2; t++) {
+                    const float4 v = col[t * TW];
+                    if (t < WS) tap<WEIGHTED>(s0, n0, s_ky[t], v);
+                    if (t >= 2) tap<WEIGHTED>(s1, n1, s_ky[t - 2], v);
+                }
+                const TilePos pos = tile_u8_pos<WS>(jobs, njobs, blockIdx.x + (i - 1) * g);
+                const MipJob &L = *pos.L;
+                const int w = L.w, h = L.h, gx = pos.x0 + x, gy = pos.y0 + 2 * p;
+                if (gx >= w) continue;
+                const size_t dn = (size_t)w * h;
+                const bool srgb = L.q_out && L.xform == 2;
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    if (gy + e >= h) break;
+                    const float4 v = e == 0 ? finish<WEIGHTED>(s0, n0) : finish<WEIGHTED>(s1, n1);
+                    const size_t o = (size_t)(gy + e) * w + gx;
+                    L.dst[o] = v.x;
+                    L.dst[dn + o] = v.y;
+                    L.dst[2 * dn + o] = v.z;
+                    L.dst[3 * dn + o] = v.w;
+                    if (L.q_out)
+                        L.q_out[o] = srgb ? quantize_srgb_bgra(v, s_steps, s_buckets) : quantize_bgra(v.x, v.y, v.z, v.w, L.xform, s_steps);
+                }
+            }
+        }
     }
 }
 
@@ -752,6 +936,35 @@ static int launch_tile2x_ws(const MipLaunch &m, const MipJob *jobs, cudaStream_t
 
 bool poly2x_supported(int ws) { return ws == 3 || ws == 5 || ws == 13; }
 
+template <int WS, bool W>
+static int launch_tile2x_u8_t(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
+    static std::atomic<unsigned long long> configured{0};
+    static int sms = 0;
+    if (first_use_on_device(configured)) {
+        cudaFuncSetAttribute(k_tile2x_u8<WS, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TileU8<WS>::smem());
+        int d = 0;
+        cudaGetDevice(&d);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+    }
+    const long long grid = std::min<long long>(m.units, sms > 0 ? sms : 152);
+    k_tile2x_u8<WS, W><<<(unsigned)grid, 1024, TileU8<WS>::smem(), s>>>(jobs, m.njobs, m.units);
+    return launch_status();
+}
+
+template <int WS>
+static int launch_tile2x_u8_ws(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
+    return m.weighted ? launch_tile2x_u8_t<WS, true>(m, jobs, s) : launch_tile2x_u8_t<WS, false>(m, jobs, s);
+}
+
+int tile_u8_phase(int ws) {
+    if (ws == 3) return TileU8<3>::D;
+    if (ws == 5) return TileU8<5>::D;
+    if (ws == 13) return TileU8<13>::D;
+    return -1;
+}
+int tile_u8_w() { return TileU8<13>::TW; }
+int tile_u8_h() { return TileU8<13>::TH; }
+
 // ---------------------------------------------------------------------------------------------
 // Surface::resize (src/nvtt/Surface.cpp:1152-1230) -> FloatImage::resize (src/nvimage/FloatImage.cpp:
 // 761-808, and the alpha-first variant :877-925, which computes every channel the same way): the X
@@ -764,7 +977,7 @@ __global__ void k_resize_x(const float *__restrict__ src, int W, int H, const fl
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = (long long)w * H;
     if (i >= n) return;
-    const int x = (int)(i % w), y = (int)(i / w);
+    const int x = (int)((unsigned)i % (unsigned)w), y = (int)((unsigned)i / (unsigned)w);
     const size_t sn = (size_t)W * H;
     const float *k = kx + (size_t)x * ws;
     const int left = lx[x];
@@ -783,7 +996,7 @@ __global__ void k_resize_y(const float *__restrict__ tmp, int w, int H, const fl
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = (long long)w * h;
     if (o >= n) return;
-    const int x = (int)(o % w), y = (int)(o / w);
+    const int x = (int)((unsigned)o % (unsigned)w), y = (int)((unsigned)o / (unsigned)w);
     const size_t tn = (size_t)w * H;
     const float *k = ky + (size_t)y * ws;
     const int left = ly[y];
@@ -840,6 +1053,11 @@ int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s) {
             else k_mip_tail<false><<<(unsigned)m.units, 1024, tail_smem_bytes(), s>>>(jobs, m.njobs);
             return launch_status();
         }
+        case MIP_TILE_U8:
+            if (m.ws == 3) return launch_tile2x_u8_ws<3>(m, jobs, s);
+            if (m.ws == 5) return launch_tile2x_u8_ws<5>(m, jobs, s);
+            if (m.ws == 13) return launch_tile2x_u8_ws<13>(m, jobs, s);
+            return 2;
         case MIP_POLY2X:
             if (m.threads < 64 || m.threads > 512 || m.threads % 32 || m.smem > 200 * 1024) return 1;
             if (m.ws == 3) return launch_tile2x_ws<3>(m, jobs, s);
