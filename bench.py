@@ -396,7 +396,7 @@ def run_gpu(args):
         sm_mhz_m = clocks["sm_mhz"] or 2070.0
         fp32_peak = 152 * 128 * sm_mhz_m * 1e6
         roof_hbm = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
-                    "traffic": None, "kernel": "mip launches of the chain (k_tile2x for the 2:1 steps, k_mip_tail for the "
+                    "traffic": None, "kernel": "mip launches of the chain (k_tile2x_u8 / k_tile2x for the 2:1 steps, k_mip_tail for the "
                                               "levels from 32x32 down)",
                     "algorithmic_bytes": mip_bytes, "ms": mips_ms, "peak_source": peak_src,
                     "fp32_ops": mip_ops, "fp32_frac": mip_ops / (mips_ms / 1000.0) / fp32_peak,
@@ -609,7 +609,7 @@ def run_gpu_batch(args):
         mip_gbs = mip_bytes / (phases["mips"] / 1000.0) / 1e9
         dominant = max(("bc1", "bc3", "bc5", "mips"), key=lambda k: phases[k])
         roof_mips = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
-                     "traffic": None, "kernel": "mip launches of the batch (k_tile2x, k_poly, k_mip_tail, k_fast_down)",
+                     "traffic": None, "kernel": "mip launches of the batch (k_tile2x_u8, k_tile2x, k_poly, k_mip_tail, k_fast_down)",
                      "algorithmic_bytes": mip_bytes, "ms": phases["mips"], "peak_source": peak_src}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
