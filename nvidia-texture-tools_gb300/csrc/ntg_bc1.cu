@@ -42,7 +42,11 @@ __device__ __forceinline__ unsigned to565(f3 v) {
 
 __device__ __forceinline__ float round5(float x) { return (float)(int)(x * 31.0f + 0.5f) * (1.0f / 31.0f); }
 __device__ __forceinline__ float round6(float x) { return (float)(int)(x * 63.0f + 0.5f) * (1.0f / 63.0f); }
-__device__ __forceinline__ f3 round_ept(f3 v) { return mk3(round5(snap_clamp(v.x)), round6(snap_clamp(v.y)), round5(snap_clamp(v.z))); }
+// vround_ept(n * f) (src/nvtt/icbc.h:1572-1578): saturate, then the 5:6:5 grid; the product and the
+// clamp are one saturating multiply, equal to saturate(n * f) for every input as far as the snap sees.
+__device__ __forceinline__ f3 round_ept(f3 n, float f) {
+    return mk3(round5(mul_sat(n.x, f)), round6(mul_sat(n.y, f)), round5(mul_sat(n.z, f)));
+}
 __device__ __forceinline__ bool is_black(f3 c) { return c.x < 1.0f / 8 && c.y < 1.0f / 8 && c.z < 1.0f / 8; }
 __device__ __forceinline__ f3 xyz(float4 v) { return mk3(v.x, v.y, v.z); }
 
@@ -234,10 +238,8 @@ __device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &s
 __device__ __forceinline__ float cf_eval(f3 ax, f3 sum, float a2, float b2, float ab, f3 metric, f3 &pa, f3 &pb) {
     float factor = 1.0f / (a2 * b2 - ab * ab);
     f3 bx = sum - ax;
-    f3 a = ((ax * b2) - (bx * ab)) * factor;
-    f3 b = ((bx * a2) - (ax * ab)) * factor;
-    a = round_ept(a);
-    b = round_ept(b);
+    const f3 a = round_ept((ax * b2) - (bx * ab), factor);
+    const f3 b = round_ept((bx * a2) - (ax * ab), factor);
     f3 e2 = ((a * ((b * ab) - ax)) - (b * bx)) * 2.0f;
     f3 e1 = ((a * a) * a2) + (((b * b) * b2) + e2);
     pa = a; pb = b;

@@ -192,11 +192,12 @@ __device__ __forceinline__ int float_to_int(float a, int limit) {
 // split loops, which index points by running counts. In DXT1 mode (BC1a) a texel with alpha 0
 // is never live and never matched, and takes index 3 at the end.
 
-// Min(one, Max(zero, v)) then Floor(grid * v + half) * gridrcp
-// (src/nvtt/squish/weightedclusterfit.cpp:516-519) per channel, grid (31, 63, 31); the clamp is
-// snap_clamp, which gives the same snapped value as squish's Max/Min for every input.
-__device__ __forceinline__ f3 snap565(f3 v) {
-    const float x = snap_clamp(v.x), y = snap_clamp(v.y), z = snap_clamp(v.z);
+// v = n * f, Min(one, Max(zero, v)), then Floor(grid * v + half) * gridrcp
+// (src/nvtt/squish/weightedclusterfit.cpp:513-519) per channel, grid (31, 63, 31); the product and
+// the clamp are one saturating multiply, which gives the same snapped value as squish's Max/Min
+// for every input.
+__device__ __forceinline__ f3 snap565(f3 n, float f) {
+    const float x = mul_sat(n.x, f), y = mul_sat(n.y, f), z = mul_sat(n.z, f);
     return mk3(floorf(31.0f * x + 0.5f) * (1.0f / 31.0f), floorf(63.0f * y + 0.5f) * (1.0f / 63.0f),
                floorf(31.0f * z + 0.5f) * (1.0f / 31.0f));
 }
@@ -345,8 +346,8 @@ __device__ __forceinline__ float squish_search4(const SquishSet &S, f3 msq, Arr 
                 const float f = 1.0f / (a2 * b2s - ab * ab);
                 const f3 ax = axp + (x2 * (1.0f / 3.0f));
                 const f3 bx = xsum - ax;
-                const f3 a = snap565(((ax * b2s) - (bx * ab)) * f);
-                const f3 b = snap565(((bx * a2) - (ax * ab)) * f);
+                const f3 a = snap565((ax * b2s) - (bx * ab), f);
+                const f3 b = snap565((bx * a2) - (ax * ab), f);
                 const f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
                 const f3 e1 = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
                 // x * 1.0f is x exactly: the default unit metric drops the three multiplies
@@ -388,8 +389,8 @@ __device__ __forceinline__ float squish_search3(const SquishSet &S, f3 msq, Arr 
             const float f = 1.0f / (a2 * b2s - ab * ab);
             const f3 ax = x0 + x1 * 0.5f;
             const f3 bx = S.xsum - ax;
-            const f3 a = snap565(((ax * b2s) - (bx * ab)) * f);
-            const f3 b = snap565(((bx * a2) - (ax * ab)) * f);
+            const f3 a = snap565((ax * b2s) - (bx * ab), f);
+            const f3 b = snap565((bx * a2) - (ax * ab), f);
             const f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
             const f3 e1 = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
             const float err = UNIT_METRIC ? (e1.x + e1.y) + e1.z : dot(e1, msq);
@@ -457,8 +458,8 @@ __device__ __forceinline__ uint2 squish_block4(const SquishSet &S, f3 msq, Arr w
     const float f = 1.0f / (a2 * b2s - ab * ab);
     const f3 ax = (x0 + (x1 * (2.0f / 3.0f))) + (x2 * (1.0f / 3.0f));
     const f3 bx = S.xsum - ax;
-    const f3 bs = snap565(((ax * b2s) - (bx * ab)) * f);
-    const f3 be = snap565(((bx * a2) - (ax * ab)) * f);
+    const f3 bs = snap565((ax * b2s) - (bx * ab), f);
+    const f3 be = snap565((bx * a2) - (ax * ab), f);
     uint32_t idx = texel_indices<false>(S, b0, b1, b2);
     int ea = squish_565(bs), eb = squish_565(be);
     if (ea < eb) { int t = ea; ea = eb; eb = t; idx ^= 0x55555555u; }
@@ -482,8 +483,8 @@ __device__ __forceinline__ uint2 squish_block3(const SquishSet &S, f3 msq, Arr w
     const float f = 1.0f / (a2 * b2s - ab * ab);
     const f3 ax = x0 + x1 * 0.5f;
     const f3 bx = S.xsum - ax;
-    const f3 bs = snap565(((ax * b2s) - (bx * ab)) * f);
-    const f3 be = snap565(((bx * a2) - (ax * ab)) * f);
+    const f3 bs = snap565((ax * b2s) - (bx * ab), f);
+    const f3 be = snap565((bx * a2) - (ax * ab), f);
     uint32_t idx = texel_indices<true>(S, b0, b1, 0);
     int ea = squish_565(bs), eb = squish_565(be);
     // WriteColourBlock3: endpoints ascending; swapping exchanges indices 0 and 1

@@ -27,6 +27,13 @@ __device__ __forceinline__ float sq_min(float a, float b) { return (b < a) ? b :
 // fminf(fmaxf(x, 0), 1) everywhere else except in the sign of a zero result, which the snap
 // loses (k * -0 + 0.5 = 0.5). Only valid where the clamped value feeds such a snap.
 __device__ __forceinline__ float snap_clamp(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+// snap_clamp(x * y) as one instruction: the product rounded to nearest, then clamped to [0, 1] by
+// the multiply's saturation, which also turns a NaN into +0 (PTX mul.sat).
+__device__ __forceinline__ float mul_sat(float x, float y) {
+    float r;
+    asm("mul.rn.sat.f32 %0, %1, %2;" : "=f"(r) : "f"(x), "f"(y));
+    return r;
+}
 
 struct f3 { float x, y, z; };
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
