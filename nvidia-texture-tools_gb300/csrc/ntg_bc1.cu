@@ -247,13 +247,14 @@ __device__ __forceinline__ float cf_eval(f3 ax, f3 sum, float a2, float b2, floa
 }
 
 // One ordering of cluster_fit_four (src/nvtt/icbc.h:2250-2549): cumulative cluster ends from the
-// SAT, solve, snap, residual.
+// SAT, solve, snap, residual. The last end is never 0 (the ordering tables leave out the empty
+// split, src/nvtt/icbc.h:1913-1914), so its SAT entry needs no check.
 __device__ __forceinline__ float four_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
                                            f3 &b) {
     const int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1, c2 = (int)((o >> 16) & 255) - 1;
     const float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
     const float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
-    const float4 v2 = c2 >= 0 ? sat[c2] : make_float4(0, 0, 0, 0);
+    const float4 v2 = sat[c2];
     float w0 = v0.w, w1 = v1.w, w2 = v2.w;
     const float w3 = wsum - w2;
     const f3 x0 = xyz(v0), x1 = xyz(v1) - x0, x2 = xyz(v2) - xyz(v1);
@@ -300,12 +301,13 @@ __device__ uint32_t best_order_four(const Lane<float4> &sat, int n, f3 metric) {
     return bo;
 }
 
-// One ordering of cluster_fit_three (src/nvtt/icbc.h:2016-2247).
+// One ordering of cluster_fit_three (src/nvtt/icbc.h:2016-2247); its last end is never 0 either
+// (src/nvtt/icbc.h:1948-1949).
 __device__ __forceinline__ float three_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
                                             f3 &b) {
     const int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1;
     const float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
-    const float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
+    const float4 v1 = sat[c1];
     float w0 = v0.w, w1 = v1.w;
     const float w2 = wsum - w1;
     const f3 x0 = xyz(v0), x1 = xyz(v1) - x0;
