@@ -233,6 +233,86 @@ __device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &s
     return n;
 }
 
+// compute_sat over `col` in place: the same axis, order and prefix sums, with the colours first
+// moved into axis order (each cycle of the permutation followed once) and then summed where they
+// lie, so the table needs no storage of its own. Returns n.
+__device__ int compute_sat_inplace(const Lane<float4> &col, int n) {
+    // computeCentroid / computeCovariance / firstEigenVector_PowerMethod as in compute_sat
+    f3 c = mk3(0, 0, 0);
+    float total = 0.0f;
+    for (int i = 0; i < n; i++) { float4 p = col[i]; total += p.w; c = c + xyz(p) * p.w; }
+    c = c * (1.0f / total);
+    float m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0;
+    for (int i = 0; i < n; i++) {
+        float4 p = col[i];
+        f3 a = xyz(p) - c;
+        f3 b = a * p.w;
+        m0 += a.x * b.x; m1 += a.x * b.y; m2 += a.x * b.z;
+        m3 += a.y * b.y; m4 += a.y * b.z; m5 += a.z * b.z;
+    }
+    f3 v;
+    if (m0 == 0 && m3 == 0 && m5 == 0) {
+        v = mk3(0, 0, 0);
+    } else {
+        f3 r0 = mk3(m0, m1, m2), r1 = mk3(m1, m3, m4), r2 = mk3(m2, m4, m5);
+        float l0 = dot(r0, r0), l1 = dot(r1, r1), l2 = dot(r2, r2);
+        v = (l0 > l1 && l0 > l2) ? r0 : (l1 > l2 ? r1 : r2);
+#pragma unroll
+        for (int it = 0; it < 8; it++) {
+            float x = v.x * m0 + v.y * m1 + v.z * m2;
+            float y = v.x * m1 + v.y * m3 + v.z * m4;
+            float z = v.x * m2 + v.y * m4 + v.z * m5;
+            float norm = ic_max(ic_max(x, y), z);
+            v = mk3(x, y, z) * (1.0f / norm);
+        }
+    }
+    float dps[16];
+    uint64_t order = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        dps[i] = i < n ? dot(xyz(col[i]), v) : 0.0f;
+        order |= (uint64_t)i << (4 * i);
+    }
+#pragma unroll
+    for (int i = 1; i < 16; i++) {
+        bool moving = i < n;
+#pragma unroll
+        for (int j = i; j > 0; --j) {
+            moving = moving && (dps[j] < dps[j - 1]);
+            if (moving) {
+                float t = dps[j]; dps[j] = dps[j - 1]; dps[j - 1] = t;
+                uint64_t a = (order >> (4 * j)) & 15, b = (order >> (4 * (j - 1))) & 15;
+                order &= ~((uint64_t)0xFF << (4 * (j - 1)));
+                order |= (a << (4 * (j - 1))) | (b << (4 * j));
+            }
+        }
+    }
+    // col[i] <- col[order_i] for i < n (the order is a permutation of [0, n))
+    uint32_t done = 0;
+    for (int s = 0; s < n; s++) {
+        if (done & (1u << s)) continue;
+        const float4 first = col[s];
+        int i = s;
+        for (int step = 0; step < 16; step++) {
+            done |= 1u << i;
+            const int p = (int)((order >> (4 * i)) & 15);
+            if (p == s) break;
+            col[i] = col[p];
+            i = p;
+        }
+        col[i] = first;
+    }
+    float4 acc = col[0];
+    acc = make_float4(acc.x * acc.w, acc.y * acc.w, acc.z * acc.w, acc.w);
+    col[0] = acc;
+    for (int i = 1; i < n; i++) {
+        float4 p = col[i];
+        acc = make_float4(acc.x + p.x * p.w, acc.y + p.y * p.w, acc.z + p.z * p.w, acc.w + p.w);
+        col[i] = acc;
+    }
+    return n;
+}
+
 // Shared solve / snap / residual of cluster_fit_three and cluster_fit_four
 // (src/nvtt/icbc.h:2200-2240, 2501-2540).
 __device__ __forceinline__ float cf_eval(f3 ax, f3 sum, float a2, float b2, float ab, f3 metric, f3 &pa, f3 &pb) {
@@ -483,13 +563,14 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     }
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
-    // Two float4 arrays and the weights per thread: the reduced colours overwrite the gathered
-    // texels in place (reduce_colors only writes slots it has already read), and the texels are
-    // gathered again for the output stage once the cluster fits are done with the colours.
+    // One float4 array and the weights per thread: the reduced colours overwrite the gathered
+    // texels in place (reduce_colors only writes slots it has already read), the summed-area table
+    // overwrites the colours in place, and the texels are gathered again for the output stage once
+    // the cluster fits are done.
     Lane<float4> in{smem + t, T};
     Lane<float4> col = in;
-    Lane<float4> sat{smem + 16 * T + t, T};
-    Lane<float> wi{reinterpret_cast<float *>(smem + 32 * T) + t, T};
+    Lane<float4> sat = in;
+    Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
     const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
     uint8_t *const out = J.out + 8 * (size_t)blk;
 
@@ -560,12 +641,16 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     // compress_dxt1_cluster_fit (src/nvtt/icbc.h:3292-3325); both fits first, then the output stage
     // (pure functions of the texels and the endpoints, so their order does not matter)
     const f3 metric = cw * cw;
-    int sn = compute_sat(col, cnt, sat);
+    int sn = compute_sat_inplace(col, cnt);
     f3 s0, s1, t0, t1;
     cluster_fit_four(sat, sn, metric, s0, s1);
     bool run3 = true;
     if (any_black) {
-        // skip_blacks in place: compact the non-black colours to the front of `col`
+        // the table has replaced the colours: reduce them again (the same colours), then
+        // skip_blacks in place, compacting the non-black ones to the front of `col`
+        gather_block(J, blk, in, wi);
+        bool again = false;
+        reduce_colors(in, wi, col, again);
         int m = 0;
         for (int i = 0; i < cnt; i++) {
             float4 q = col[i];
@@ -573,7 +658,7 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
             col[m++] = q;
         }
         if (m == 0) run3 = false;
-        else sn = compute_sat(col, m, sat);
+        else sn = compute_sat_inplace(col, m);
     }
     if (run3) cluster_fit_three(sat, sn, metric, t0, t1);
     gather_block(J, blk, in, wi);
@@ -865,8 +950,8 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
     if (gblk >= nblocks) return;
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
-    // the layout of k_bc1: colours reduced over the texels in place, texels gathered again for the
-    // output stage
+    // colours reduced over the texels in place, the SAT beside them (the proposal's ends are read
+    // against both), texels gathered again for the output stage
     Lane<float4> in{smem + t, T};
     Lane<float4> col = in;
     Lane<float4> sat{smem + 16 * T + t, T};
@@ -937,8 +1022,11 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
     }
 }
 
-// Shared memory of k_bc1: per thread the texels (then the reduced colours), the SAT and the weights.
-static size_t bc1_fit_smem(int T) { return (size_t)T * (32 * sizeof(float4) + 16 * sizeof(float)); }
+// Shared memory of k_bc1: per thread the texels (then the reduced colours, then the SAT) and the
+// weights.
+static size_t bc1_fit_smem(int T) { return (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float)); }
+// k_bc1_learned keeps the colours beside the SAT (its orderings are read back against them).
+static size_t bc1_learned_smem(int T) { return (size_t)T * (32 * sizeof(float4) + 16 * sizeof(float)); }
 
 int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
@@ -987,8 +1075,8 @@ int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const
     if (nblocks == 0) return 0;
     const int T = 64;
     static std::atomic<unsigned long long> configured{0};
-    allow_smem(k_bc1_learned, bc1_fit_smem(T), configured);
-    k_bc1_learned<<<(unsigned)((nblocks + T - 1) / T), T, bc1_fit_smem(T), s>>>(d_jobs, njobs, nblocks, y, radius, margin,
+    allow_smem(k_bc1_learned, bc1_learned_smem(T), configured);
+    k_bc1_learned<<<(unsigned)((nblocks + T - 1) / T), T, bc1_learned_smem(T), s>>>(d_jobs, njobs, nblocks, y, radius, margin,
                                                                             fallback, stats);
     return launch_status();
 }
