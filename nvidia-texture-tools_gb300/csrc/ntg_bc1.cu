@@ -235,8 +235,9 @@ __device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &s
 
 // compute_sat over `col` in place: the same axis, order and prefix sums, with the colours first
 // moved into axis order (each cycle of the permutation followed once) and then summed where they
-// lie, so the table needs no storage of its own. Returns n.
-__device__ int compute_sat_inplace(const Lane<float4> &col, int n) {
+// lie, so the table needs no storage of its own. Returns n. With `frame_v`, *reversed tells
+// whether the first colour in axis order projects above the last on frame_v (axis_reversed).
+__device__ int compute_sat_inplace(const Lane<float4> &col, int n, const f3 *frame_v = nullptr, bool *reversed = nullptr) {
     // computeCentroid / computeCovariance / firstEigenVector_PowerMethod as in compute_sat
     f3 c = mk3(0, 0, 0);
     float total = 0.0f;
@@ -302,6 +303,7 @@ __device__ int compute_sat_inplace(const Lane<float4> &col, int n) {
         }
         col[i] = first;
     }
+    if (frame_v) *reversed = dot(xyz(col[0]), *frame_v) > dot(xyz(col[n - 1]), *frame_v);
     float4 acc = col[0];
     acc = make_float4(acc.x * acc.w, acc.y * acc.w, acc.z * acc.w, acc.w);
     col[0] = acc;
@@ -950,12 +952,12 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
     if (gblk >= nblocks) return;
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
-    // colours reduced over the texels in place, the SAT beside them (the proposal's ends are read
-    // against both), texels gathered again for the output stage
+    // the layout of k_bc1: colours reduced over the texels in place, the SAT built over the colours
+    // in place, texels gathered again for the output stage
     Lane<float4> in{smem + t, T};
     Lane<float4> col = in;
-    Lane<float4> sat{smem + 16 * T + t, T};
-    Lane<float> wi{reinterpret_cast<float *>(smem + 32 * T) + t, T};
+    Lane<float4> sat = in;
+    Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
     const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
     uint8_t *const out = J.out + 8 * (size_t)blk;
     gather_block(J, blk, in, wi);
@@ -970,10 +972,10 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
         const float *yp = y + gblk * 16;
         const float full_pred = (f.var + 1.0f) * expf(yp[5]) - 1.0f;
         const f3 metric = cw * cw;
-        uint64_t order;
-        int sn = compute_sat(col, cnt, sat, &order);
+        bool rev = false;
+        int sn = compute_sat_inplace(col, cnt, &f.v, &rev);
         float q0 = yp[0], q1 = yp[1], q2 = yp[2];
-        if (axis_reversed(col, sn, order, f.v)) { const float a = q0; q0 = 1 - q2; q1 = 1 - q1; q2 = 1 - a; }
+        if (rev) { const float a = q0; q0 = 1 - q2; q1 = 1 - q1; q2 = 1 - a; }
         const int e0 = frac_end(sat, sn, q0), e1 = max(e0, frac_end(sat, sn, q1));
         const int e2 = max(max(e1, 0), frac_end(sat, sn, q2));
         f3 s0, s1, t0, t1;
@@ -982,6 +984,10 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
         float err = FLT_MAX;
         bool run3 = true;
         if (any_black) {
+            // the table has replaced the colours: reduce them again, then skip the black ones
+            gather_block(J, blk, in, wi);
+            bool again = false;
+            reduce_colors(in, wi, col, again);
             int m = 0;
             for (int i = 0; i < cnt; i++) {
                 float4 q = col[i];
@@ -989,11 +995,11 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
                 col[m++] = q;
             }
             if (m == 0) run3 = false;
-            else sn = compute_sat(col, m, sat, &order);
+            else sn = compute_sat_inplace(col, m, &f.v, &rev);
         }
         if (run3) {
             float r0 = yp[3], r1 = yp[4];
-            if (axis_reversed(col, sn, order, f.v)) { const float a = r0; r0 = 1 - r1; r1 = 1 - a; }
+            if (rev) { const float a = r0; r0 = 1 - r1; r1 = 1 - a; }
             const int f0 = frac_end(sat, sn, r0), f1 = max(max(f0, 0), frac_end(sat, sn, r1));
             evaluated += pruned_three(sat, sn, metric, f0, f1, radius, t0, t1);
         }
@@ -1025,8 +1031,6 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
 // Shared memory of k_bc1: per thread the texels (then the reduced colours, then the SAT) and the
 // weights.
 static size_t bc1_fit_smem(int T) { return (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float)); }
-// k_bc1_learned keeps the colours beside the SAT (its orderings are read back against them).
-static size_t bc1_learned_smem(int T) { return (size_t)T * (32 * sizeof(float4) + 16 * sizeof(float)); }
 
 int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
@@ -1075,8 +1079,8 @@ int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const
     if (nblocks == 0) return 0;
     const int T = 64;
     static std::atomic<unsigned long long> configured{0};
-    allow_smem(k_bc1_learned, bc1_learned_smem(T), configured);
-    k_bc1_learned<<<(unsigned)((nblocks + T - 1) / T), T, bc1_learned_smem(T), s>>>(d_jobs, njobs, nblocks, y, radius, margin,
+    allow_smem(k_bc1_learned, bc1_fit_smem(T), configured);
+    k_bc1_learned<<<(unsigned)((nblocks + T - 1) / T), T, bc1_fit_smem(T), s>>>(d_jobs, njobs, nblocks, y, radius, margin,
                                                                             fallback, stats);
     return launch_status();
 }
