@@ -118,8 +118,9 @@ __global__ void k_quantize_level(const float *__restrict__ rgba, size_t n, Quant
 // ---------------------------------------------------------------------------------------------
 // Job lists. Every mip kernel takes an array of MipJob (one level step of one texture) and a
 // running unit count per job, so one launch covers a level of any number of textures; a unit is a
-// destination texel (box), a PTW x PTH tile (general polyphase) or a 32-column x `strip`-row tile
-// (2:1 polyphase). A unit finds its job by binary search over `first_unit`.
+// destination texel (box), a PTW x PTH tile (general polyphase), a 32-column x `strip`-row tile
+// (2:1 polyphase from FP32) or a 64 x 16 tile (2:1 polyphase from BGRA8). A unit finds its job by
+// binary search over `first_unit`.
 __device__ __forceinline__ int find_mip_job(const MipJob *__restrict__ jobs, int njobs, long long u) {
     int lo = 0, hi = njobs - 1;
     while (lo < hi) {
