@@ -212,6 +212,10 @@ CHAINS = [
     (37, 37, 6, 2, 2, 0, 1, 1, 0),      # BC4 Production, Kaiser, gamma
     (1, 4096, 4, 1, 2, 0, 0, 0, 2),     # 1-wide and tall: the tail's X plane keeps the full height
     (4096, 1, 1, 1, 2, 1, 2, 2, 1),     # 1-high and wide, sRGB
+    # level 1 from the BGRA8 input: tiles whose window lies inside the level take whole-vector copies
+    (384, 128, 4, 1, 2, 1, 2, 2, 2),    # Kaiser / sRGB / BC3, interior tiles at (64, 16) and (64, 32)
+    (320, 96, 1, 1, 1, 0, 0, 0, 1),     # triangle, repeat, BC1, interior tiles
+    (50, 18, 4, 1, 2, 1, 2, 2, 2),      # rows of 50 words (not 16-byte multiples): wrapped copies only
 ]
 
 
