@@ -61,6 +61,14 @@ LEARNED_BATCHES = {"c4"}
 # proposal needs a tighter fallback than on the sRGB workload)
 BATCH_PROPOSAL = {"radius": 2, "margin": 0.1}
 
+# FP32 operations of one ordering of icbc's cluster fits (src/nvtt/icbc.h:2501-2540 and 2200-2240 in
+# the scalar build), each multiply/add/min/max/round/reciprocal counted once: cluster_fit_four w3 1,
+# cluster differences 8, alpha2 4, beta2 4, alphabeta 2, alphax 12 = 31, cluster_fit_three 14, then
+# the shared solve/snap/residual: factor 4, betax 3, a 12, b 12, saturate + 5:6:5 rounding 36, e2 18,
+# e1 18, metric 5, compare 1 = 109.
+OPS_PER_ORDERING4 = 140
+OPS_PER_ORDERING3 = 123
+
 # FP32 operations of one cluster-split evaluation of squish's WeightedClusterFit::Compress4
 # (src/nvtt/squish/weightedclusterfit.cpp:505-545), each multiply/add/min/max/floor/divide counted
 # once: w3 3, alpha2 4, beta2 4, alphabeta 2, factor 4, alphax 12, betax 3, a 12, b 12, clamp 12,
@@ -611,6 +619,20 @@ def run_gpu_batch(args):
         roof_mips = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
                      "traffic": None, "kernel": "mip launches of the batch (k_tile2x_u8, k_tile2x, k_poly, k_mip_tail, k_fast_down)",
                      "algorithmic_bytes": mip_bytes, "ms": phases["mips"], "peak_source": peak_src}
+        roof = None
+        if dominant == "bc1" and phases["bc1"] > 0:
+            # the BC1 Level8 fit against the FP32 issue peak: orderings counted on the device by the
+            # same gather / reduce_colors the encoder runs, times the operations of one ordering
+            n4, n3 = batch.count_work()
+            sm_mhz_b = clocks["sm_mhz"] or 2070.0
+            peak_b = 152 * 128 * sm_mhz_b * 1e6
+            ops = n4 * OPS_PER_ORDERING4 + n3 * OPS_PER_ORDERING3
+            ach = ops / (phases["bc1"] / 1000.0)
+            roof = {"bound": "fp32", "achieved": ach / 1e12, "peak": peak_b / 1e12, "unit": "TFLOP/s",
+                    "frac": ach / peak_b, "traffic": None, "kernel": "k_bc1<7> (icbc Level8 cluster fit)",
+                    "note": f"peak = 152 SMs x 128 FP32 lanes x median SM clock {sm_mhz_b:.0f} MHz; {n4} four-cluster x "
+                            f"{OPS_PER_ORDERING4} + {n3} three-cluster x {OPS_PER_ORDERING3} ops over the BC1 phase "
+                            f"({phases['bc1']:.3f} ms, one run outside the graph, CUDA events)"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -623,7 +645,7 @@ def run_gpu_batch(args):
                         "matches_device_path": same,
                         "api": "ntg_batch_launch / ntg_batch_launch_alternate (two bindings), copies on two streams"},
                 "gpu_launches": info["launches"] * args.steps,
-                "clocks": clocks, "roofline": None, "roofline_mips": roof_mips,
+                "clocks": clocks, "roofline": roof, "roofline_mips": roof_mips,
                 "phase_ms": phases, "phase_blocks": blocks, "dominant_phase": dominant, "learned": learned_info,
                 "wall_s_timed": wall, "cpu_baseline": None}
         if not args.no_cpu and world == 1:

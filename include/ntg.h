@@ -227,6 +227,11 @@ int ntg_batch_info(const ntg_batch *batch, long long *texels, long long *blocks,
  * ms[0] = every mip launch, ms[1..3] = the BC1, BC3, BC5 encoder launches (0 when absent), and
  * blocks[0..2] = the 4x4 blocks of each format. Synchronises `stream`. */
 int ntg_batch_time_phases(ntg_batch *batch, void *stream, float ms[4], long long blocks[3]);
+/* Measurement only: the cluster orderings the BC1 Level8 fit evaluates over the batch's BC1 blocks
+ * (Normal and Production quality), four-cluster in bc1_orderings[0] and three-cluster in [1]
+ * (icbc::compress_dxt1_cluster_fit, src/nvtt/icbc.h:3292-3325: four_total / three_total of each
+ * block's reduced colour counts). Synchronises `stream`. */
+int ntg_batch_count_work(ntg_batch *batch, void *stream, unsigned long long bc1_orderings[2]);
 /* Encodes the batch's BC1 Normal-quality blocks through the learned endpoint proposal (see
  * ntg_compress_chain_learned; mlp NULL restores the full fit) and recaptures the graph; the network
  * must outlive the batch. ntg_batch_proposal_stats reads the last run's {kept, full fit, orderings}

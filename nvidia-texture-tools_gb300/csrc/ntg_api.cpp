@@ -1658,6 +1658,25 @@ int ntg_batch_time_phases(ntg_batch *b, void *stream, float ms[4], long long blo
     return NTG_OK;
 }
 
+int ntg_batch_count_work(ntg_batch *b, void *stream, unsigned long long bc1_orderings[2]) {
+    g_error.clear();
+    if (!b || !bc1_orderings) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    NTG_TRY(ensure_device(b->ctx));
+    cudaStream_t s = S(stream);
+    unsigned long long *d = nullptr;
+    NTG_CUDA(cudaMallocAsync((void **)&d, 2 * sizeof(unsigned long long), s));
+    int status = cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s) == cudaSuccess ? NTG_OK : NTG_ERROR_CUDA;
+    for (const auto &e : b->encodes)
+        if (status == NTG_OK && e.format == NTG_FORMAT_BC1 && e.quality != NTG_QUALITY_FASTEST)
+            status = launched(launch_bc1_work(b->denc() + e.first, e.njobs, e.nblocks, d, s), "fit work count");
+    if (status == NTG_OK && cudaMemcpyAsync(bc1_orderings, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        status = NTG_ERROR_CUDA;
+    cudaFreeAsync(d, s);
+    if (status == NTG_OK && cudaStreamSynchronize(s) != cudaSuccess) status = NTG_ERROR_CUDA;
+    return status == NTG_OK ? NTG_OK : fail(status, "fit work count failed");
+}
+
 int ntg_batch_set_proposal(ntg_batch *b, ntg_mlp *mlp, int radius, float margin) {
     g_error.clear();
     if (!b || radius < 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");

@@ -1028,6 +1028,42 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
     }
 }
 
+// Work of the Level8 fit (measurement only, outside the encoder): per block the orderings that
+// cluster_fit_four and cluster_fit_three evaluate (over the non-black colours when the block has
+// black ones), from the same gather and reduce_colors as k_bc1; summed into work[0] and work[1].
+__global__ void __launch_bounds__(64) k_bc1_work(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
+                                                 unsigned long long *__restrict__ work) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    unsigned long long n4 = 0, n3 = 0;
+    if (gblk < nblocks) {
+        const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+        Lane<float4> in{smem + t, T};
+        Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
+        gather_block(J, (int)(gblk - J.first_block), in, wi);
+        bool any_black = false;
+        const int cnt = reduce_colors(in, wi, in, any_black);
+        if (cnt >= 2) {
+            n4 = c_tab.four_total[cnt - 1];
+            int m = cnt;
+            if (any_black) {
+                m = 0;
+                for (int i = 0; i < cnt; i++) m += !is_black(xyz(in[i]));
+            }
+            if (m > 0) n3 = c_tab.three_total[m - 1];
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        n4 += __shfl_down_sync(0xffffffffu, n4, off);
+        n3 += __shfl_down_sync(0xffffffffu, n3, off);
+    }
+    if ((t & 31) == 0 && (n4 | n3)) {
+        atomicAdd(&work[0], n4);
+        atomicAdd(&work[1], n3);
+    }
+}
+
 // Shared memory of k_bc1: per thread the texels (then the reduced colours, then the SAT) and the
 // weights.
 static size_t bc1_fit_smem(int T) { return (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float)); }
@@ -1082,6 +1118,13 @@ int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const
     allow_smem(k_bc1_learned, bc1_fit_smem(T), configured);
     k_bc1_learned<<<(unsigned)((nblocks + T - 1) / T), T, bc1_fit_smem(T), s>>>(d_jobs, njobs, nblocks, y, radius, margin,
                                                                             fallback, stats);
+    return launch_status();
+}
+
+int launch_bc1_work(const EncJob *d_jobs, int njobs, long long nblocks, unsigned long long *work, cudaStream_t s) {
+    if (nblocks == 0) return 0;
+    const int T = 64;
+    k_bc1_work<<<(unsigned)((nblocks + T - 1) / T), T, bc1_fit_smem(T), s>>>(d_jobs, njobs, nblocks, work);
     return launch_status();
 }
 

@@ -60,6 +60,9 @@ int launch_bc1_features(const EncJob *d_jobs, int njobs, long long nblocks, floa
 int launch_bc1_targets(const EncJob *d_jobs, int njobs, long long nblocks, float *tg, cudaStream_t s);
 int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const float *y, int radius, float margin,
                        long long *fallback, unsigned long long *stats, cudaStream_t s);
+// Orderings the Level8 fit evaluates over the jobs' blocks (four-cluster, three-cluster), added to
+// work[0], work[1] (measurement only).
+int launch_bc1_work(const EncJob *d_jobs, int njobs, long long nblocks, unsigned long long *work, cudaStream_t s);
 // The full fit over the first *d_count entries of `list` (at most max_count; no host round trip).
 int launch_bc1_list(const EncJob *d_jobs, int njobs, const long long *list, const unsigned long long *d_count,
                     long long max_count, cudaStream_t s);

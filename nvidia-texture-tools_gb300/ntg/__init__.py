@@ -110,6 +110,7 @@ def lib():
                                 ctypes.POINTER(_i), ctypes.POINTER(_i)]),
         "ntg_batch_destroy": (_i, [_vp]),
         "ntg_batch_time_phases": (_i, [_vp, _vp, ctypes.POINTER(_f), ctypes.POINTER(ctypes.c_longlong)]),
+        "ntg_batch_count_work": (_i, [_vp, _vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "ntg_batch_set_proposal": (_i, [_vp, _vp, _i, _f]),
         "ntg_batch_proposal_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "ntg_mlp_create": (_i, [_i, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
@@ -419,6 +420,12 @@ class Batch:
         _check(lib().ntg_batch_time_phases(self.h, _stream_ptr(stream), ms, blocks))
         return ({"mips": ms[0], "bc1": ms[1], "bc3": ms[2], "bc5": ms[3]},
                 {"bc1": blocks[0], "bc3": blocks[1], "bc5": blocks[2]})
+
+    def count_work(self, stream=None):
+        """(four-cluster, three-cluster) orderings the BC1 Level8 fit evaluates over the batch."""
+        n = (ctypes.c_ulonglong * 2)()
+        _check(lib().ntg_batch_count_work(self.h, _stream_ptr(stream), n))
+        return int(n[0]), int(n[1])
 
     def close(self):
         if self.h:

@@ -232,3 +232,27 @@ def test_batch_learned_proposal_wide_radius_is_exact(ctx, tmp_path, monkeypatch)
     finally:
         b.close()
         net.close()
+
+
+@pytest.mark.gpu
+def test_count_work_orderings(ctx, tmp_path, monkeypatch):
+    """ntg_batch_count_work: a block of 16 distinct bright colours evaluates every ordering (968 four-
+    cluster, 152 three-cluster); with eight black colours among its 16, the three-cluster fit runs over
+    the other eight (44 orderings); a solid block runs no fit."""
+    monkeypatch.setenv("NTG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    w, h = 12, 4  # three blocks, level 0 only
+    img = np.zeros((h, w, 4), np.uint8)  # B, G, R, A
+    img[..., 3] = 255
+    for k in range(16):
+        y, x = k // 4, k % 4
+        img[y, x] = (100, 200, 64 + 8 * k, 255)                  # block 0: bright, distinct
+        img[y, 4 + x] = (0, 0, 3 * k, 255) if k < 8 else (100, 200, 64 + 8 * k, 255)  # block 1: 8 black
+        img[y, 8 + x] = (30, 60, 90, 255)                        # block 2: one colour
+    opt = ntg.ChainOptions.make(format=ntg.FORMAT_BC1, quality=ntg.QUALITY_NORMAL, max_levels=1)
+    d_in = dev(img.reshape(-1).view(np.uint32))
+    out = dev(np.zeros(ntg.chain_bytes(w, h, opt), np.uint8))
+    b = ntg.Batch(ctx, [(d_in, w, h, opt, out)])
+    try:
+        assert b.count_work() == (968 + 968, 152 + 44)
+    finally:
+        b.close()
