@@ -20,6 +20,14 @@ struct Lane {  // one thread's view of a [k][thread] shared-memory array
     __device__ __forceinline__ T &operator[](int k) const { return base[k * stride]; }
 };
 
+// One thread's 16 weights packed in four float4 slots of a [slot][thread] array (k -> slot k / 4,
+// component k % 4), so that every slot holds this thread's data only.
+struct LaneW {
+    float *base;  // component 0 of this thread's first slot
+    int stride;   // floats between consecutive slots of one thread
+    __device__ __forceinline__ float &operator[](int k) const { return base[(k >> 2) * stride + (k & 3)]; }
+};
+
 __device__ __forceinline__ float to_srgb(float f) {
     // toSrgb (src/nvtt/Surface.cpp:1512-1519)
     if (isnan(f)) return 0.0f;
@@ -125,7 +133,8 @@ __device__ uint32_t indices_any(const Lane<float4> &in, f3 cw, const Pal3 &pal) 
 }
 
 // evaluate_mse over the input texels (src/nvtt/icbc.h:2733-2756)
-__device__ float block_mse(const Lane<float4> &in, const Lane<float> &wi, f3 cw, const Pal3 &pal, uint32_t idx) {
+template <typename W>
+__device__ float block_mse(const Lane<float4> &in, const W &wi, f3 cw, const Pal3 &pal, uint32_t idx) {
     float err = 0.0f;
 #pragma unroll 4
     for (int i = 0; i < 16; i++) {
@@ -139,7 +148,8 @@ __device__ float block_mse(const Lane<float4> &in, const Lane<float> &wi, f3 cw,
 
 struct Block1 { unsigned c0, c1; uint32_t idx; };
 
-__device__ float output_block4(const Lane<float4> &in, const Lane<float> &wi, f3 cw, f3 v0, f3 v1, Block1 &o) {
+template <typename W>
+__device__ float output_block4(const Lane<float4> &in, const W &wi, f3 cw, f3 v0, f3 v1, Block1 &o) {
     unsigned c0 = to565(v0), c1 = to565(v1);
     if (c0 < c1) { unsigned t = c0; c0 = c1; c1 = t; }
     Pal3 pal;
@@ -149,7 +159,8 @@ __device__ float output_block4(const Lane<float4> &in, const Lane<float> &wi, f3
     return block_mse(in, wi, cw, pal, o.idx);
 }
 
-__device__ float output_block3(const Lane<float4> &in, const Lane<float> &wi, f3 cw, bool allow_black, f3 v0, f3 v1, Block1 &o) {
+template <typename W>
+__device__ float output_block3(const Lane<float4> &in, const W &wi, f3 cw, bool allow_black, f3 v0, f3 v1, Block1 &o) {
     unsigned c0 = to565(v0), c1 = to565(v1);
     if (c0 > c1) { unsigned t = c0; c0 = c1; c1 = t; }
     Pal3 pal;
@@ -159,7 +170,8 @@ __device__ float output_block3(const Lane<float4> &in, const Lane<float> &wi, f3
     return block_mse(in, wi, cw, pal, o.idx);
 }
 
-__device__ __forceinline__ float mse_of(const Lane<float4> &in, const Lane<float> &wi, f3 cw, const Block1 &o) {
+template <typename W>
+__device__ __forceinline__ float mse_of(const Lane<float4> &in, const W &wi, f3 cw, const Block1 &o) {
     Pal3 pal;
     palette_f(o.c0, o.c1, pal);
     return block_mse(in, wi, cw, pal, o.idx);
@@ -237,6 +249,9 @@ __device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &s
 // moved into axis order (each cycle of the permutation followed once) and then summed where they
 // lie, so the table needs no storage of its own. Returns n. With `frame_v`, *reversed tells
 // whether the first colour in axis order projects above the last on frame_v (axis_reversed).
+// ZERO: entry k holds the sum of the first k colours (entry 0 zero, n + 1 entries), so that a
+// cumulative cluster end indexes it directly; else entry k holds the first k + 1 (n entries).
+template <bool ZERO = false>
 __device__ int compute_sat_inplace(const Lane<float4> &col, int n, const f3 *frame_v = nullptr, bool *reversed = nullptr) {
     // computeCentroid / computeCovariance / firstEigenVector_PowerMethod as in compute_sat
     f3 c = mk3(0, 0, 0);
@@ -306,6 +321,16 @@ __device__ int compute_sat_inplace(const Lane<float4> &col, int n, const f3 *fra
     if (frame_v) *reversed = dot(xyz(col[0]), *frame_v) > dot(xyz(col[n - 1]), *frame_v);
     float4 acc = col[0];
     acc = make_float4(acc.x * acc.w, acc.y * acc.w, acc.z * acc.w, acc.w);
+    if (ZERO) {
+        col[0] = make_float4(0, 0, 0, 0);
+        for (int i = 1; i < n; i++) {
+            float4 p = col[i];  // read colour i before its slot takes the sum of the first i
+            col[i] = acc;
+            acc = make_float4(acc.x + p.x * p.w, acc.y + p.y * p.w, acc.z + p.z * p.w, acc.w + p.w);
+        }
+        col[n] = acc;
+        return n;
+    }
     col[0] = acc;
     for (int i = 1; i < n; i++) {
         float4 p = col[i];
@@ -330,12 +355,15 @@ __device__ __forceinline__ float cf_eval(f3 ax, f3 sum, float a2, float b2, floa
 
 // One ordering of cluster_fit_four (src/nvtt/icbc.h:2250-2549): cumulative cluster ends from the
 // SAT, solve, snap, residual. The last end is never 0 (the ordering tables leave out the empty
-// split, src/nvtt/icbc.h:1913-1914), so its SAT entry needs no check.
+// split, src/nvtt/icbc.h:1913-1914), so its SAT entry needs no check; with a ZERO table (entry 0
+// zero) no end does.
+template <bool ZERO = false>
 __device__ __forceinline__ float four_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
                                            f3 &b) {
-    const int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1, c2 = (int)((o >> 16) & 255) - 1;
-    const float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
-    const float4 v1 = c1 >= 0 ? sat[c1] : make_float4(0, 0, 0, 0);
+    const int d = ZERO ? 0 : 1;
+    const int c0 = (int)(o & 255) - d, c1 = (int)((o >> 8) & 255) - d, c2 = (int)((o >> 16) & 255) - d;
+    const float4 v0 = (ZERO || c0 >= 0) ? sat[c0] : make_float4(0, 0, 0, 0);
+    const float4 v1 = (ZERO || c1 >= 0) ? sat[c1] : make_float4(0, 0, 0, 0);
     const float4 v2 = sat[c2];
     float w0 = v0.w, w1 = v1.w, w2 = v2.w;
     const float w3 = wsum - w2;
@@ -351,8 +379,9 @@ __device__ __forceinline__ float four_eval(const Lane<float4> &sat, uint32_t o, 
 
 // The first strict minimum over all orderings wins, as in the scalar build. The search keeps the
 // index of the best ordering; its endpoints are recomputed once at the end.
+template <bool ZERO = false>
 __device__ void cluster_fit_four(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
-    const float4 s = sat[n - 1];
+    const float4 s = sat[ZERO ? n : n - 1];
     const f3 sum = xyz(s);
     const float wsum = s.w;
     float best = FLT_MAX;
@@ -360,12 +389,12 @@ __device__ void cluster_fit_four(const Lane<float4> &sat, int n, f3 metric, f3 &
     const int total = c_tab.four_total[n - 1];
     for (int i = 0; i < total; i++) {
         f3 a, b;
-        const float e = four_eval(sat, c_tab.four[i], sum, wsum, metric, a, b);
+        const float e = four_eval<ZERO>(sat, c_tab.four[i], sum, wsum, metric, a, b);
         if (e < best) { best = e; bi = i; }
     }
     start = mk3(0, 0, 0);
     end = mk3(0, 0, 0);
-    if (bi >= 0) four_eval(sat, c_tab.four[bi], sum, wsum, metric, start, end);
+    if (bi >= 0) four_eval<ZERO>(sat, c_tab.four[bi], sum, wsum, metric, start, end);
 }
 
 // The full search's best ordering code (0 when none), for training targets.
@@ -385,10 +414,12 @@ __device__ uint32_t best_order_four(const Lane<float4> &sat, int n, f3 metric) {
 
 // One ordering of cluster_fit_three (src/nvtt/icbc.h:2016-2247); its last end is never 0 either
 // (src/nvtt/icbc.h:1948-1949).
+template <bool ZERO = false>
 __device__ __forceinline__ float three_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
                                             f3 &b) {
-    const int c0 = (int)(o & 255) - 1, c1 = (int)((o >> 8) & 255) - 1;
-    const float4 v0 = c0 >= 0 ? sat[c0] : make_float4(0, 0, 0, 0);
+    const int d = ZERO ? 0 : 1;
+    const int c0 = (int)(o & 255) - d, c1 = (int)((o >> 8) & 255) - d;
+    const float4 v0 = (ZERO || c0 >= 0) ? sat[c0] : make_float4(0, 0, 0, 0);
     const float4 v1 = sat[c1];
     float w0 = v0.w, w1 = v1.w;
     const float w2 = wsum - w1;
@@ -415,8 +446,9 @@ __device__ uint32_t best_order_three(const Lane<float4> &sat, int n, f3 metric) 
     return bo;
 }
 
+template <bool ZERO = false>
 __device__ void cluster_fit_three(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
-    const float4 s = sat[n - 1];
+    const float4 s = sat[ZERO ? n : n - 1];
     const f3 sum = xyz(s);
     const float wsum = s.w;
     float best = FLT_MAX;
@@ -424,17 +456,18 @@ __device__ void cluster_fit_three(const Lane<float4> &sat, int n, f3 metric, f3 
     const int total = c_tab.three_total[n - 1];
     for (int i = 0; i < total; i++) {
         f3 a, b;
-        const float e = three_eval(sat, c_tab.three[i], sum, wsum, metric, a, b);
+        const float e = three_eval<ZERO>(sat, c_tab.three[i], sum, wsum, metric, a, b);
         if (e < best) { best = e; bi = i; }
     }
     start = mk3(0, 0, 0);
     end = mk3(0, 0, 0);
-    if (bi >= 0) three_eval(sat, c_tab.three[bi], sum, wsum, metric, start, end);
+    if (bi >= 0) three_eval<ZERO>(sat, c_tab.three[bi], sum, wsum, metric, start, end);
 }
 
 // refine_endpoints (src/nvtt/icbc.h:3329-3406), including the reference's use of the current
 // output's palette (not the candidate's) for index selection.
-__device__ float refine_endpoints(const Lane<float4> &in, const Lane<float> &wi, f3 cw, float err, Block1 &o) {
+template <typename W>
+__device__ float refine_endpoints(const Lane<float4> &in, const W &wi, f3 cw, float err, Block1 &o) {
     const int8_t deltas[16][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1},
                                   {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {-1, -1, 0}, {-1, 0, -1}, {0, -1, -1},
                                   {-1, 1, 0}, {1, -1, 0}, {0, -1, 1}, {0, 1, -1}};
@@ -479,7 +512,8 @@ __device__ __forceinline__ int find_job(const EncJob *jobs, int njobs, long long
 // FloatColorCompressorTask gather (src/nvtt/BlockCompressor.cpp:116-166): the block's 16 texels
 // after the output transform, weight saturate(alpha) under AlphaMode_Transparency, texels outside
 // the image at weight 0.
-__device__ __forceinline__ void gather_block(const EncJob &J, int blk, const Lane<float4> &in, const Lane<float> &wi) {
+template <typename W>
+__device__ __forceinline__ void gather_block(const EncJob &J, int blk, const Lane<float4> &in, const W &wi) {
     const int bx = blk % J.bw, by = blk / J.bw;
     const size_t n = (size_t)J.w * J.h;
     const int vw = min(J.w - bx * 4, 4), vh = min(J.h - by * 4, 4);
@@ -512,7 +546,8 @@ __device__ __forceinline__ void gather_block(const EncJob &J, int blk, const Lan
 
 // reduce_colors (src/nvtt/icbc.h:1638-1683), threshold 1/256: merges near-equal colours of
 // positive weight into `col` (weighted mean, summed weight). Returns the colour count.
-__device__ __forceinline__ int reduce_colors(const Lane<float4> &in, const Lane<float> &wi, const Lane<float4> &col,
+template <typename W>
+__device__ __forceinline__ int reduce_colors(const Lane<float4> &in, const W &wi, const Lane<float4> &col,
                                              bool &any_black) {
     const float thr = 1.0f / 256;
     int cnt = 0;
@@ -565,14 +600,15 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     }
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
-    // One float4 array and the weights per thread: the reduced colours overwrite the gathered
-    // texels in place (reduce_colors only writes slots it has already read), the summed-area table
-    // overwrites the colours in place, and the texels are gathered again for the output stage once
-    // the cluster fits are done.
+    // 20 float4 slots per thread: the texels (16), then the weights packed in 4. The reduced colours
+    // overwrite the texels in place (reduce_colors only writes slots it has already read), the
+    // summed-area table overwrites the colours in place with a zero entry first (17 entries: the
+    // last takes the first weight slot, whose weights are dead during the fits), and the texels
+    // and weights are gathered again for the output stage once the cluster fits are done.
     Lane<float4> in{smem + t, T};
     Lane<float4> col = in;
     Lane<float4> sat = in;
-    Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
+    LaneW wi{reinterpret_cast<float *>(smem + 16 * T + t), 4 * T};
     const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
     uint8_t *const out = J.out + 8 * (size_t)blk;
 
@@ -643,9 +679,9 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     // compress_dxt1_cluster_fit (src/nvtt/icbc.h:3292-3325); both fits first, then the output stage
     // (pure functions of the texels and the endpoints, so their order does not matter)
     const f3 metric = cw * cw;
-    int sn = compute_sat_inplace(col, cnt);
+    int sn = compute_sat_inplace<true>(col, cnt);
     f3 s0, s1, t0, t1;
-    cluster_fit_four(sat, sn, metric, s0, s1);
+    cluster_fit_four<true>(sat, sn, metric, s0, s1);
     bool run3 = true;
     if (any_black) {
         // the table has replaced the colours: reduce them again (the same colours), then
@@ -660,9 +696,9 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
             col[m++] = q;
         }
         if (m == 0) run3 = false;
-        else sn = compute_sat_inplace(col, m);
+        else sn = compute_sat_inplace<true>(col, m);
     }
-    if (run3) cluster_fit_three(sat, sn, metric, t0, t1);
+    if (run3) cluster_fit_three<true>(sat, sn, metric, t0, t1);
     gather_block(J, blk, in, wi);
     Block1 cf;
     float cerr = output_block4(in, wi, cw, s0, s1, cf);
@@ -705,7 +741,8 @@ struct Frame {
     __device__ f3 from(f3 q) const { return mu + ((v * q.x) + ((u1 * q.y) + (u2 * q.z))) * sigma; }
 };
 
-__device__ __forceinline__ Frame block_frame(const Lane<float4> &in, const Lane<float> &wi, f3 cw) {
+template <typename W>
+__device__ __forceinline__ Frame block_frame(const Lane<float4> &in, const W &wi, f3 cw) {
     Frame f;
     float ws = 0.0f;
     f3 m = mk3(0, 0, 0);
