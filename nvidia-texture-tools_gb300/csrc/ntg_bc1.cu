@@ -907,12 +907,12 @@ __global__ void __launch_bounds__(64) k_bc1_targets(const EncJob *__restrict__ j
 }
 
 // Ordering end of a cumulative weight fraction: the last sorted colour whose cumulative weight is
-// within the fraction (-1 when none is).
+// within the fraction (-1 when none is). `sat` is a ZERO table (entry k: the first k colours).
 __device__ __forceinline__ int frac_end(const Lane<float4> &sat, int n, float frac) {
-    const float lim = frac * sat[n - 1].w * (1.0f + 1e-5f) + 1e-7f;
+    const float lim = frac * sat[n].w * (1.0f + 1e-5f) + 1e-7f;
     int e = -1;
     for (int k = 0; k < n; k++)
-        if (sat[k].w <= lim) e = k;
+        if (sat[k + 1].w <= lim) e = k;
     return e;
 }
 
@@ -923,7 +923,7 @@ __device__ __forceinline__ uint32_t pack_order(int e0, int e1, int e2) {
 // cluster_fit_four over the orderings whose cluster ends lie within r of (e0, e1, e2), in the full
 // search's order (last end, then first, then second); returns the number evaluated.
 __device__ int pruned_four(const Lane<float4> &sat, int n, f3 metric, int e0, int e1, int e2, int r, f3 &start, f3 &end) {
-    const float4 s = sat[n - 1];
+    const float4 s = sat[n];  // a ZERO table
     const f3 sum = xyz(s);
     const float wsum = s.w;
     float best = FLT_MAX;
@@ -935,18 +935,18 @@ __device__ int pruned_four(const Lane<float4> &sat, int n, f3 metric, int e0, in
             for (int b = max(a, e1 - r); b <= min(c, e1 + r); b++) {
                 f3 pa, pb;
                 const uint32_t o = pack_order(a, b, c);
-                const float e = four_eval(sat, o, sum, wsum, metric, pa, pb);
+                const float e = four_eval<true>(sat, o, sum, wsum, metric, pa, pb);
                 evaluated++;
                 if (e < best) { best = e; bo = o; found = true; }
             }
     start = mk3(0, 0, 0);
     end = mk3(0, 0, 0);
-    if (found) four_eval(sat, bo, sum, wsum, metric, start, end);
+    if (found) four_eval<true>(sat, bo, sum, wsum, metric, start, end);
     return evaluated;
 }
 
 __device__ int pruned_three(const Lane<float4> &sat, int n, f3 metric, int e0, int e1, int r, f3 &start, f3 &end) {
-    const float4 s = sat[n - 1];
+    const float4 s = sat[n];  // a ZERO table
     const f3 sum = xyz(s);
     const float wsum = s.w;
     float best = FLT_MAX;
@@ -957,13 +957,13 @@ __device__ int pruned_three(const Lane<float4> &sat, int n, f3 metric, int e0, i
         for (int a = max(-1, e0 - r); a <= min(c, e0 + r); a++) {
             f3 pa, pb;
             const uint32_t o = (uint32_t)(a + 1) | ((uint32_t)(c + 1) << 8);
-            const float e = three_eval(sat, o, sum, wsum, metric, pa, pb);
+            const float e = three_eval<true>(sat, o, sum, wsum, metric, pa, pb);
             evaluated++;
             if (e < best) { best = e; bo = o; found = true; }
         }
     start = mk3(0, 0, 0);
     end = mk3(0, 0, 0);
-    if (found) three_eval(sat, bo, sum, wsum, metric, start, end);
+    if (found) three_eval<true>(sat, bo, sum, wsum, metric, start, end);
     return evaluated;
 }
 
@@ -989,12 +989,12 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
     if (gblk >= nblocks) return;
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
-    // the layout of k_bc1: colours reduced over the texels in place, the SAT built over the colours
-    // in place, texels gathered again for the output stage
+    // the layout of k_bc1: colours reduced over the texels in place, the ZERO SAT built over the
+    // colours in place, texels and weights gathered again for the output stage
     Lane<float4> in{smem + t, T};
     Lane<float4> col = in;
     Lane<float4> sat = in;
-    Lane<float> wi{reinterpret_cast<float *>(smem + 16 * T) + t, T};
+    LaneW wi{reinterpret_cast<float *>(smem + 16 * T + t), 4 * T};
     const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
     uint8_t *const out = J.out + 8 * (size_t)blk;
     gather_block(J, blk, in, wi);
@@ -1010,7 +1010,7 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
         const float full_pred = (f.var + 1.0f) * expf(yp[5]) - 1.0f;
         const f3 metric = cw * cw;
         bool rev = false;
-        int sn = compute_sat_inplace(col, cnt, &f.v, &rev);
+        int sn = compute_sat_inplace<true>(col, cnt, &f.v, &rev);
         float q0 = yp[0], q1 = yp[1], q2 = yp[2];
         if (rev) { const float a = q0; q0 = 1 - q2; q1 = 1 - q1; q2 = 1 - a; }
         const int e0 = frac_end(sat, sn, q0), e1 = max(e0, frac_end(sat, sn, q1));
@@ -1032,7 +1032,7 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
                 col[m++] = q;
             }
             if (m == 0) run3 = false;
-            else sn = compute_sat_inplace(col, m, &f.v, &rev);
+            else sn = compute_sat_inplace<true>(col, m, &f.v, &rev);
         }
         if (run3) {
             float r0 = yp[3], r1 = yp[4];
