@@ -249,9 +249,8 @@ __device__ int compute_sat(const Lane<float4> &col, int n, const Lane<float4> &s
 // moved into axis order (each cycle of the permutation followed once) and then summed where they
 // lie, so the table needs no storage of its own. Returns n. With `frame_v`, *reversed tells
 // whether the first colour in axis order projects above the last on frame_v (axis_reversed).
-// ZERO: entry k holds the sum of the first k colours (entry 0 zero, n + 1 entries), so that a
-// cumulative cluster end indexes it directly; else entry k holds the first k + 1 (n entries).
-template <bool ZERO = false>
+// The table is a ZERO one: entry k holds the sum of the first k colours (entry 0 zero, n + 1
+// entries), so that a cumulative cluster end indexes it directly.
 __device__ int compute_sat_inplace(const Lane<float4> &col, int n, const f3 *frame_v = nullptr, bool *reversed = nullptr) {
     // computeCentroid / computeCovariance / firstEigenVector_PowerMethod as in compute_sat
     f3 c = mk3(0, 0, 0);
@@ -321,22 +320,13 @@ __device__ int compute_sat_inplace(const Lane<float4> &col, int n, const f3 *fra
     if (frame_v) *reversed = dot(xyz(col[0]), *frame_v) > dot(xyz(col[n - 1]), *frame_v);
     float4 acc = col[0];
     acc = make_float4(acc.x * acc.w, acc.y * acc.w, acc.z * acc.w, acc.w);
-    if (ZERO) {
-        col[0] = make_float4(0, 0, 0, 0);
-        for (int i = 1; i < n; i++) {
-            float4 p = col[i];  // read colour i before its slot takes the sum of the first i
-            col[i] = acc;
-            acc = make_float4(acc.x + p.x * p.w, acc.y + p.y * p.w, acc.z + p.z * p.w, acc.w + p.w);
-        }
-        col[n] = acc;
-        return n;
-    }
-    col[0] = acc;
+    col[0] = make_float4(0, 0, 0, 0);
     for (int i = 1; i < n; i++) {
-        float4 p = col[i];
-        acc = make_float4(acc.x + p.x * p.w, acc.y + p.y * p.w, acc.z + p.z * p.w, acc.w + p.w);
+        float4 p = col[i];  // read colour i before its slot takes the sum of the first i
         col[i] = acc;
+        acc = make_float4(acc.x + p.x * p.w, acc.y + p.y * p.w, acc.z + p.z * p.w, acc.w + p.w);
     }
+    col[n] = acc;
     return n;
 }
 
@@ -679,7 +669,7 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     // compress_dxt1_cluster_fit (src/nvtt/icbc.h:3292-3325); both fits first, then the output stage
     // (pure functions of the texels and the endpoints, so their order does not matter)
     const f3 metric = cw * cw;
-    int sn = compute_sat_inplace<true>(col, cnt);
+    int sn = compute_sat_inplace(col, cnt);
     f3 s0, s1, t0, t1;
     cluster_fit_four<true>(sat, sn, metric, s0, s1);
     bool run3 = true;
@@ -696,7 +686,7 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
             col[m++] = q;
         }
         if (m == 0) run3 = false;
-        else sn = compute_sat_inplace<true>(col, m);
+        else sn = compute_sat_inplace(col, m);
     }
     if (run3) cluster_fit_three<true>(sat, sn, metric, t0, t1);
     gather_block(J, blk, in, wi);
@@ -1010,7 +1000,7 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
         const float full_pred = (f.var + 1.0f) * expf(yp[5]) - 1.0f;
         const f3 metric = cw * cw;
         bool rev = false;
-        int sn = compute_sat_inplace<true>(col, cnt, &f.v, &rev);
+        int sn = compute_sat_inplace(col, cnt, &f.v, &rev);
         float q0 = yp[0], q1 = yp[1], q2 = yp[2];
         if (rev) { const float a = q0; q0 = 1 - q2; q1 = 1 - q1; q2 = 1 - a; }
         const int e0 = frac_end(sat, sn, q0), e1 = max(e0, frac_end(sat, sn, q1));
@@ -1032,7 +1022,7 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
                 col[m++] = q;
             }
             if (m == 0) run3 = false;
-            else sn = compute_sat_inplace<true>(col, m, &f.v, &rev);
+            else sn = compute_sat_inplace(col, m, &f.v, &rev);
         }
         if (run3) {
             float r0 = yp[3], r1 = yp[4];
