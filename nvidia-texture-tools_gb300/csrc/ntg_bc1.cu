@@ -347,14 +347,9 @@ __device__ __forceinline__ float cf_eval(f3 ax, f3 sum, float a2, float b2, floa
 // SAT, solve, snap, residual. The last end is never 0 (the ordering tables leave out the empty
 // split, src/nvtt/icbc.h:1913-1914), so its SAT entry needs no check; with a ZERO table (entry 0
 // zero) no end does.
-template <bool ZERO = false>
-__device__ __forceinline__ float four_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
-                                           f3 &b) {
-    const int d = ZERO ? 0 : 1;
-    const int c0 = (int)(o & 255) - d, c1 = (int)((o >> 8) & 255) - d, c2 = (int)((o >> 16) & 255) - d;
-    const float4 v0 = (ZERO || c0 >= 0) ? sat[c0] : make_float4(0, 0, 0, 0);
-    const float4 v1 = (ZERO || c1 >= 0) ? sat[c1] : make_float4(0, 0, 0, 0);
-    const float4 v2 = sat[c2];
+// The ordering from the SAT entries of its three cumulative ends.
+__device__ __forceinline__ float four_eval_v(float4 v0, float4 v1, float4 v2, f3 sum, float wsum, f3 metric, f3 &a,
+                                             f3 &b) {
     float w0 = v0.w, w1 = v1.w, w2 = v2.w;
     const float w3 = wsum - w2;
     const f3 x0 = xyz(v0), x1 = xyz(v1) - x0, x2 = xyz(v2) - xyz(v1);
@@ -367,8 +362,20 @@ __device__ __forceinline__ float four_eval(const Lane<float4> &sat, uint32_t o, 
     return cf_eval(ax, sum, a2, b2, ab, metric, a, b);
 }
 
+template <bool ZERO = false>
+__device__ __forceinline__ float four_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
+                                           f3 &b) {
+    const int d = ZERO ? 0 : 1;
+    const int c0 = (int)(o & 255) - d, c1 = (int)((o >> 8) & 255) - d, c2 = (int)((o >> 16) & 255) - d;
+    const float4 v0 = (ZERO || c0 >= 0) ? sat[c0] : make_float4(0, 0, 0, 0);
+    const float4 v1 = (ZERO || c1 >= 0) ? sat[c1] : make_float4(0, 0, 0, 0);
+    return four_eval_v(v0, v1, sat[c2], sum, wsum, metric, a, b);
+}
+
 // The first strict minimum over all orderings wins, as in the scalar build. The search keeps the
-// index of the best ordering; its endpoints are recomputed once at the end.
+// index of the best ordering; its endpoints are recomputed once at the end. Over a ZERO table the
+// orderings are walked as the nest the table lists them in (last end t = 1..n, first end 0..t,
+// second end first..t: build_device_tables), so that the last and first ends' entries stay loaded.
 template <bool ZERO = false>
 __device__ void cluster_fit_four(const Lane<float4> &sat, int n, f3 metric, f3 &start, f3 &end) {
     const float4 s = sat[ZERO ? n : n - 1];
@@ -376,11 +383,26 @@ __device__ void cluster_fit_four(const Lane<float4> &sat, int n, f3 metric, f3 &
     const float wsum = s.w;
     float best = FLT_MAX;
     int bi = -1;
-    const int total = c_tab.four_total[n - 1];
-    for (int i = 0; i < total; i++) {
-        f3 a, b;
-        const float e = four_eval<ZERO>(sat, c_tab.four[i], sum, wsum, metric, a, b);
-        if (e < best) { best = e; bi = i; }
+    if (ZERO) {
+        int i = 0;
+        for (int t = 1; t <= n; t++) {
+            const float4 v2 = sat[t];
+            for (int c0 = 0; c0 <= t; c0++) {
+                const float4 v0 = sat[c0];
+                for (int c1 = c0; c1 <= t; c1++, i++) {
+                    f3 a, b;
+                    const float e = four_eval_v(v0, sat[c1], v2, sum, wsum, metric, a, b);
+                    if (e < best) { best = e; bi = i; }
+                }
+            }
+        }
+    } else {
+        const int total = c_tab.four_total[n - 1];
+        for (int i = 0; i < total; i++) {
+            f3 a, b;
+            const float e = four_eval<ZERO>(sat, c_tab.four[i], sum, wsum, metric, a, b);
+            if (e < best) { best = e; bi = i; }
+        }
     }
     start = mk3(0, 0, 0);
     end = mk3(0, 0, 0);
@@ -404,13 +426,7 @@ __device__ uint32_t best_order_four(const Lane<float4> &sat, int n, f3 metric) {
 
 // One ordering of cluster_fit_three (src/nvtt/icbc.h:2016-2247); its last end is never 0 either
 // (src/nvtt/icbc.h:1948-1949).
-template <bool ZERO = false>
-__device__ __forceinline__ float three_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
-                                            f3 &b) {
-    const int d = ZERO ? 0 : 1;
-    const int c0 = (int)(o & 255) - d, c1 = (int)((o >> 8) & 255) - d;
-    const float4 v0 = (ZERO || c0 >= 0) ? sat[c0] : make_float4(0, 0, 0, 0);
-    const float4 v1 = sat[c1];
+__device__ __forceinline__ float three_eval_v(float4 v0, float4 v1, f3 sum, float wsum, f3 metric, f3 &a, f3 &b) {
     float w0 = v0.w, w1 = v1.w;
     const float w2 = wsum - w1;
     const f3 x0 = xyz(v0), x1 = xyz(v1) - x0;
@@ -420,6 +436,15 @@ __device__ __forceinline__ float three_eval(const Lane<float4> &sat, uint32_t o,
     const float b2 = w2 + ab;
     const f3 ax = x0 + (x1 * 0.5f);
     return cf_eval(ax, sum, a2, b2, ab, metric, a, b);
+}
+
+template <bool ZERO = false>
+__device__ __forceinline__ float three_eval(const Lane<float4> &sat, uint32_t o, f3 sum, float wsum, f3 metric, f3 &a,
+                                            f3 &b) {
+    const int d = ZERO ? 0 : 1;
+    const int c0 = (int)(o & 255) - d, c1 = (int)((o >> 8) & 255) - d;
+    const float4 v0 = (ZERO || c0 >= 0) ? sat[c0] : make_float4(0, 0, 0, 0);
+    return three_eval_v(v0, sat[c1], sum, wsum, metric, a, b);
 }
 
 __device__ uint32_t best_order_three(const Lane<float4> &sat, int n, f3 metric) {
@@ -443,11 +468,23 @@ __device__ void cluster_fit_three(const Lane<float4> &sat, int n, f3 metric, f3 
     const float wsum = s.w;
     float best = FLT_MAX;
     int bi = -1;
-    const int total = c_tab.three_total[n - 1];
-    for (int i = 0; i < total; i++) {
-        f3 a, b;
-        const float e = three_eval<ZERO>(sat, c_tab.three[i], sum, wsum, metric, a, b);
-        if (e < best) { best = e; bi = i; }
+    if (ZERO) {  // the table's nest: last end t = 1..n, first end 0..t
+        int i = 0;
+        for (int t = 1; t <= n; t++) {
+            const float4 v1 = sat[t];
+            for (int c0 = 0; c0 <= t; c0++, i++) {
+                f3 a, b;
+                const float e = three_eval_v(sat[c0], v1, sum, wsum, metric, a, b);
+                if (e < best) { best = e; bi = i; }
+            }
+        }
+    } else {
+        const int total = c_tab.three_total[n - 1];
+        for (int i = 0; i < total; i++) {
+            f3 a, b;
+            const float e = three_eval<ZERO>(sat, c_tab.three[i], sum, wsum, metric, a, b);
+            if (e < best) { best = e; bi = i; }
+        }
     }
     start = mk3(0, 0, 0);
     end = mk3(0, 0, 0);
