@@ -606,6 +606,8 @@ int ensure_device(ntg_context *ctx) {
 
 }  // namespace
 
+int ntg::use_context_device(ntg_context *ctx) { return ensure_device(ctx); }
+
 void ntg::set_last_error(const std::string &msg) { g_error = msg; }
 
 extern "C" {

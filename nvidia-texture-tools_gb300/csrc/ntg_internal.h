@@ -68,6 +68,7 @@ int launch_bc1_list(const EncJob *d_jobs, int njobs, const long long *list, cons
                     long long max_count, cudaStream_t s);
 }  // namespace ntg
 struct ntg_mlp;
+struct ntg_context;
 namespace ntg {
 int mlp_forward_device(ntg_mlp *m, const float *d_x, long long rows, float *d_y, cudaStream_t s);
 
@@ -136,5 +137,7 @@ int upload_tables_decode(const HostTables &t);
 
 // Sets the message ntg_last_error_string() returns on this thread.
 void set_last_error(const std::string &msg);
+// Makes the context's device current (ntg_last_error_string describes a failure).
+int use_context_device(ntg_context *ctx);
 
 }  // namespace ntg

@@ -16,7 +16,8 @@
 // All calls share the one array and it keeps what the last call left there: each call rewrites the
 // parts it reads (job record, quantiser steps, quantised level) before its kernels run. Calls whose
 // work overlaps on the GPU (different streams, or different host threads) race on the array; issue
-// them on one stream, or serialise them.
+// them on one stream, or serialise them. The job record and the quantiser steps reach the array as
+// kernel arguments (written by a one-CTA kernel), so no call reads host memory after it returns.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -72,11 +73,22 @@ int report_status(int st, const char *what) {
     return report(st, what);
 }
 
-const float *srgb_steps_host() {
-    static float steps[256];
+struct StepTable {
+    float v[256];
+};
+
+const StepTable &srgb_steps_host() {
+    static StepTable steps;
     static std::once_flag once;
-    std::call_once(once, [] { ntg::build_srgb_steps(steps); });
+    std::call_once(once, [] { ntg::build_srgb_steps(steps.v); });
     return steps;
+}
+
+// Writes the call's job record (and, when `steps` is non-null, the sRGB quantiser steps) into the
+// scratch array from the launch's own arguments.
+__global__ void k_put_record(ntg::EncJob j, ntg::EncJob *d_job, StepTable t, float *steps) {
+    if (threadIdx.x == 0) *d_job = j;
+    if (steps) steps[threadIdx.x] = t.v[threadIdx.x];
 }
 
 }  // namespace
@@ -103,9 +115,12 @@ extern "C" int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_r
     if (out_xform == NTG_XFORM_GAMMA && gamma != 2.2f)
         return report(NTG_ERROR_UNSUPPORTED_FEATURE, "power-law gamma other than 2.2 is not supported on the GPU");
 
+    // the context's tables live on its device: run there whatever device the caller has current
+    int st = ntg::use_context_device(ctx);
+    if (st != NTG_OK) return st;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     unsigned char *scratch = nullptr;
-    int st = scratch_address(&scratch);
+    st = scratch_address(&scratch);
     if (st != NTG_OK) return report_status(st, "cudaGetSymbolAddress of the scratch array");
 
     ntg::EncJob j;
@@ -116,26 +131,26 @@ extern "C" int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_r
     j.first_block = 0;
     if (cw) { j.cw[0] = cw[0]; j.cw[1] = cw[1]; j.cw[2] = cw[2]; }
     else { j.cw[0] = j.cw[1] = j.cw[2] = 1.0f; }
+    ntg::EncJob *d_job = reinterpret_cast<ntg::EncJob *>(scratch + kJobOffset);
+    float *d_steps = reinterpret_cast<float *>(scratch + kStepsOffset);
+    const bool quantise = format != NTG_FORMAT_BC1 && out_xform != NTG_XFORM_NONE;
     if (format == NTG_FORMAT_BC1) {
         j.rgba = d_rgba;
         j.out_xform = out_xform;  // applied per texel on the device
-    } else if (out_xform != NTG_XFORM_NONE) {
-        // ColorBlock quantises the transformed level: build that level in the scratch array
-        float *d_steps = reinterpret_cast<float *>(scratch + kStepsOffset);
-        uint32_t *d_level = reinterpret_cast<uint32_t *>(scratch + kLevelOffset);
-        if (out_xform == NTG_XFORM_SRGB &&
-            cudaMemcpyAsync(d_steps, srgb_steps_host(), 256 * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess)
-            return report_status(ntg::launch_status(), "copy of the quantiser steps");
-        st = ntg::launch_quantize(d_rgba, (size_t)w * h, out_xform, d_steps, d_level, s);
-        if (st != NTG_OK) return report_status(st, "quantise level");
-        j.bgra = d_level;
+    } else if (quantise) {
+        j.bgra = reinterpret_cast<uint32_t *>(scratch + kLevelOffset);
     } else {
         j.rgba = d_rgba;
     }
-    ntg::EncJob *d_job = reinterpret_cast<ntg::EncJob *>(scratch + kJobOffset);
-    // pageable source: staged before the call returns, so `j` may go out of scope
-    if (cudaMemcpyAsync(d_job, &j, sizeof j, cudaMemcpyHostToDevice, s) != cudaSuccess)
-        return report_status(ntg::launch_status(), "copy of the job record");
+    const bool steps = quantise && out_xform == NTG_XFORM_SRGB;
+    k_put_record<<<1, 256, 0, s>>>(j, d_job, srgb_steps_host(), steps ? d_steps : nullptr);
+    st = ntg::launch_status();
+    if (st != NTG_OK) return report_status(st, "job record");
+    if (quantise) {
+        // ColorBlock quantises the transformed level: build that level in the scratch array
+        st = ntg::launch_quantize(d_rgba, (size_t)w * h, out_xform, d_steps, const_cast<uint32_t *>(j.bgra), s);
+        if (st != NTG_OK) return report_status(st, "quantise level");
+    }
     const long long nblocks = (long long)((w + 3) / 4) * ((h + 3) / 4);
     st = format == NTG_FORMAT_BC1    ? ntg::launch_bc1(d_job, 1, nblocks, quality, 0, s)
          : format == NTG_FORMAT_BC3  ? ntg::launch_bc3(d_job, 1, nblocks, quality, 0, s)

@@ -39,7 +39,11 @@ def noalloc_ctx():
 
 @pytest.mark.parametrize("fmt,quality,alpha_mode,out_xform", [
     (ntg.FORMAT_BC1, ntg.QUALITY_NORMAL, ntg.ALPHA_NONE, ntg.XFORM_NONE),
+    (ntg.FORMAT_BC1, ntg.QUALITY_NORMAL, ntg.ALPHA_TRANSPARENCY, ntg.XFORM_SRGB),
     (ntg.FORMAT_BC3, ntg.QUALITY_NORMAL, ntg.ALPHA_TRANSPARENCY, ntg.XFORM_SRGB),
+    (ntg.FORMAT_BC3, ntg.QUALITY_NORMAL, ntg.ALPHA_NONE, ntg.XFORM_GAMMA),
+    (ntg.FORMAT_BC1A, ntg.QUALITY_NORMAL, ntg.ALPHA_TRANSPARENCY, ntg.XFORM_NONE),
+    (ntg.FORMAT_BC4, ntg.QUALITY_PRODUCTION, ntg.ALPHA_NONE, ntg.XFORM_NONE),
     (ntg.FORMAT_BC5, ntg.QUALITY_NORMAL, ntg.ALPHA_NONE, ntg.XFORM_NONE),
 ])
 def test_noalloc_matches_encode_on_two_calls(noalloc_ctx, fmt, quality, alpha_mode, out_xform):
@@ -60,3 +64,28 @@ def test_noalloc_rejects_levels_above_its_limit(noalloc_ctx):
                                       out.data_ptr(), None)
     assert rc == 1
     assert "scratch limit" in ntg.lib().ntg_last_error_string().decode()
+
+
+def test_noalloc_runs_on_the_context_device():
+    """A caller whose current device is not the context's still gets the context's device (where its
+    tables live): the call switches to it, as ntg_encode does."""
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    ctx = ntg.Context(1)
+    try:
+        L = ntg.lib()
+        w, h = 48, 20
+        rng = np.random.default_rng(5)
+        with torch.cuda.device(1):
+            img = torch.from_numpy(rng.random(4 * w * h, dtype=np.float32)).cuda()
+            ref = _encode(L.ntg_encode, ctx, ntg.FORMAT_BC3, img, w, h, 1, 1, ntg.XFORM_SRGB)
+            out = torch.zeros(16 * ntg.nblocks(w, h), dtype=torch.uint8, device="cuda")
+        torch.cuda.set_device(0)
+        cw = (ctypes.c_float * 3)(1.0, 1.0, 1.0)
+        rc = L.ntg_encode_noalloc(ctx.h, ntg.FORMAT_BC3, img.data_ptr(), w, h, 1, 1, ntg.XFORM_SRGB, 2.2,
+                                  ctypes.cast(cw, ctypes.c_void_p), out.data_ptr(), None)
+        assert rc == 0, L.ntg_last_error_string().decode()
+        torch.cuda.synchronize(1)
+        assert np.array_equal(out.cpu().numpy(), ref)
+    finally:
+        ctx.close()
