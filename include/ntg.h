@@ -273,6 +273,13 @@ int ntg_mlp_train_step(ntg_mlp *mlp, const float *d_x, const float *d_t, int bat
                        void *stream);
 /* Non-zero when a tensor-core wait of an earlier call gave up (synchronises the device). */
 int ntg_mlp_status(ntg_mlp *mlp);
+/* The bounded waits' limit: each tensor-core wait (mbarrier phase) of this network's kernels polls at
+ * most `polls` times (negative: the default, 4,194,304) before it gives up; 0 makes every wait give
+ * up at once, with no fault. A kernel whose wait gave up records it (ntg_mlp_status reports
+ * NTG_ERROR_CUDA), waits with the default limit for the tensor-core work it has already issued, frees
+ * its TMEM and returns, so later calls run normally. Also clears the recorded status; synchronises
+ * the device. No counterpart in the reference. */
+int ntg_mlp_set_wait_limit(ntg_mlp *mlp, int polls);
 /* Learned BC1 encode of a chain (BC1 Normal quality; same options and output layout as
  * ntg_compress_chain). Each block's texels go through the network; the proposal's palette seeds the
  * cluster fit's ordering search, which evaluates only the orderings within `radius` (in each

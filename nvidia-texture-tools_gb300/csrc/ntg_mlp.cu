@@ -10,8 +10,9 @@
 // (8-row x 16-byte core matrices), multiplied by tcgen05.mma (kind::f16, M = 128) issued by one
 // thread into a TMEM accumulator, double-buffered with an mbarrier per stage that the MMA's
 // tcgen05.commit arrives on. The epilogue reads the accumulator back with tcgen05.ld (thread t owns
-// row t) and applies bias + GELU, GELU', or split-K atomics. Every wait is bounded: on timeout the
-// kernel records an error, frees its TMEM and returns.
+// row t) and applies bias + GELU, GELU', or split-K atomics. Every wait is bounded (a poll count the
+// host sets per network, ntg_mlp_set_wait_limit): on timeout the kernel records an error, waits (with
+// the default limit) for the tensor-core work it has already issued, frees its TMEM and returns.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -50,6 +51,7 @@ struct GemmArgs {
     const float *Z;          // pre-activation [M x N] (ldz) for EPI_DGELU
     int ldz;
     int *status;             // set to a non-zero code when a wait gives up
+    int polls;               // polls of each wait before it gives up
 };
 
 // ---- PTX wrappers (tcgen05, mbarrier) ----
@@ -85,9 +87,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the completion of the phase with the given parity.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (int i = 0; i < (1 << 22); i++)
+// Polls of a wait by default, and of the drain after a wait gave up: the MMAs already issued
+// still write the TMEM accumulator, so they must finish before it is freed.
+constexpr int kWaitPolls = 1 << 22;
+
+// Bounded wait for the completion of the phase with the given parity (`limit` polls; 0 gives up at once).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int limit) {
+    for (int i = 0; i < limit; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -195,11 +201,12 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
     tc_fence_after();
     const uint32_t tmem = tmem_base;
     bool ok = true;
+    int committed = -1;  // last chunk whose MMAs were issued and committed
 
     for (int c = 0; c < chunks && ok; c++) {
         const int s = c & 1;
         if (c >= 2) {  // the MMAs of chunk c-2 read this stage; the CTA agrees on the outcome
-            ok = __syncthreads_and(mbar_wait(&bars[s], ((c - 2) >> 1) & 1)) != 0;
+            ok = __syncthreads_and(mbar_wait(&bars[s], ((c - 2) >> 1) & 1, g.polls)) != 0;
             if (!ok) break;
         }
         const int k0 = kbeg + c * BK;
@@ -215,10 +222,15 @@ __global__ void __launch_bounds__(128) k_gemm(GemmArgs g) {
                 mma_bf16(tmem, smem_desc(a0 + j * 2 * LBO), smem_desc(b0 + j * 2 * LBO), IDESC, (c > 0 || j > 0) ? 1u : 0u);
             mma_commit(&bars[s]);
         }
+        committed = c;
     }
     // all MMAs done: the last chunk's commit completes after every earlier one
-    if (ok && chunks > 0) ok = __syncthreads_and(mbar_wait(&bars[(chunks - 1) & 1], ((chunks - 1) >> 1) & 1)) != 0;
-    if (!ok && g.status) atomicExch(g.status, 1);
+    if (ok && chunks > 0) ok = __syncthreads_and(mbar_wait(&bars[(chunks - 1) & 1], ((chunks - 1) >> 1) & 1, g.polls)) != 0;
+    if (!ok) {
+        if (g.status && threadIdx.x == 0) atomicExch(g.status, 1);
+        // drain: the last commit's barrier completes once every MMA issued so far has finished
+        if (committed >= 0) __syncthreads_and(mbar_wait(&bars[committed & 1], (committed >> 1) & 1, kWaitPolls));
+    }
     tc_fence_after();
 
     if (ok) {
@@ -443,7 +455,7 @@ __global__ void __launch_bounds__(512, 1) k_mlp_infer(const __nv_bfloat16 *__res
                                                        const __nv_bfloat16 *__restrict__ w3, const float *__restrict__ b1,
                                                        const float *__restrict__ b2, const float *__restrict__ b3,
                                                        const float *__restrict__ x, long long rows, float *__restrict__ y,
-                                                       int *status) {
+                                                       int *status, int polls) {
     extern __shared__ __align__(16) uint8_t smem[];  // 226 KB of the 227 KB a CTA may have
     __shared__ uint64_t bar;
     __shared__ uint32_t tmem_base;
@@ -522,7 +534,9 @@ __global__ void __launch_bounds__(512, 1) k_mlp_infer(const __nv_bfloat16 *__res
                 }
                 mma_commit(&bar);
             }
-            ok = __syncthreads_and(mbar_wait(&bar, phase & 1)) != 0;
+            ok = __syncthreads_and(mbar_wait(&bar, phase & 1, polls)) != 0;
+            // gave up: drain this layer's MMAs (they write the accumulator) before TMEM is freed
+            if (!ok) __syncthreads_and(mbar_wait(&bar, phase & 1, kWaitPolls));
             phase++;
             tc_fence_after();
             if (!ok) break;
@@ -542,7 +556,7 @@ __global__ void __launch_bounds__(512, 1) k_mlp_infer(const __nv_bfloat16 *__res
             }
         }
     }
-    if (!ok && status) atomicExch(status, 1);
+    if (!ok && status && threadIdx.x == 0) atomicExch(status, 1);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, 512);
@@ -564,6 +578,7 @@ struct ntg_mlp {
     __nv_bfloat16 *w1 = nullptr, *w2 = nullptr, *w2t = nullptr, *w3 = nullptr, *w3t = nullptr;
     float *b3p = nullptr, *wout = nullptr, *loss = nullptr;
     int *status = nullptr;
+    int polls = kWaitPolls;  // polls of each tensor-core wait before it gives up
     // activations and gradients, batch `cap`
     __nv_bfloat16 *xb = nullptr, *xt = nullptr, *h1 = nullptr, *h1t = nullptr, *h2 = nullptr, *h2t = nullptr;
     __nv_bfloat16 *dyb = nullptr, *dyt = nullptr, *dz2b = nullptr, *dz2t = nullptr, *dz1b = nullptr, *dz1t = nullptr;
@@ -623,25 +638,27 @@ int ensure_batch(ntg_mlp *m, int batch) {
     return NTG_OK;
 }
 
-GemmArgs gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K, int epi, int *status) {
+GemmArgs gemm(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K, int epi, int *status,
+              int polls = kWaitPolls) {
     GemmArgs g;
     std::memset(&g, 0, sizeof g);
     g.A = A; g.lda = lda; g.B = B; g.ldb = ldb; g.M = M; g.N = N; g.K = K; g.epi = epi; g.status = status;
+    g.polls = polls;
     return g;
 }
 
 // Forward pass: X (bf16) -> Z1, H1, Z2, H2 -> Y [batch x OUTP]. `train` also writes the
 // transposed activations the weight gradients need.
 int forward(ntg_mlp *m, int batch, bool train, cudaStream_t s) {
-    GemmArgs g = gemm(m->xb, IN, m->w1, IN, batch, HID, IN, EPI_GELU, m->status);
+    GemmArgs g = gemm(m->xb, IN, m->w1, IN, batch, HID, IN, EPI_GELU, m->status, m->polls);
     g.bias = m->p + OFF_B1; g.C = train ? m->z1 : nullptr; g.ldc = HID; g.H = m->h1; g.ldh = HID;
     g.HT = train ? m->h1t : nullptr; g.ldht = batch;
     MLP_LAUNCH(launch_gemm(g, 1, s));
-    g = gemm(m->h1, HID, m->w2, HID, batch, HID, HID, EPI_GELU, m->status);
+    g = gemm(m->h1, HID, m->w2, HID, batch, HID, HID, EPI_GELU, m->status, m->polls);
     g.bias = m->p + OFF_B2; g.C = train ? m->z2 : nullptr; g.ldc = HID; g.H = m->h2; g.ldh = HID;
     g.HT = train ? m->h2t : nullptr; g.ldht = batch;
     MLP_LAUNCH(launch_gemm(g, 1, s));
-    g = gemm(m->h2, HID, m->w3, HID, batch, OUTP, HID, EPI_F32, m->status);
+    g = gemm(m->h2, HID, m->w3, HID, batch, OUTP, HID, EPI_F32, m->status, m->polls);
     g.bias = m->b3p; g.C = m->y; g.ldc = OUTP;
     MLP_LAUNCH(launch_gemm(g, 1, s));
     return NTG_OK;
@@ -657,26 +674,26 @@ int backward(ntg_mlp *m, const float *d_t, int batch, cudaStream_t s) {
     MLP_CUDA(cudaMemsetAsync(m->dw2, 0, sizeof(float) * HID * HID, s));
     MLP_CUDA(cudaMemsetAsync(m->dw1, 0, sizeof(float) * HID * IN, s));
     // dW3^T = H2^T dY
-    GemmArgs g = gemm(m->h2t, batch, m->dyt, batch, HID, OUTP, batch, EPI_ATOMIC, m->status);
+    GemmArgs g = gemm(m->h2t, batch, m->dyt, batch, HID, OUTP, batch, EPI_ATOMIC, m->status, m->polls);
     g.C = m->dw3t; g.ldc = OUTP;
     MLP_LAUNCH(launch_gemm(g, splits, s));
     k_colsum<<<OUTP, 256, 0, s>>>(m->dy, batch, OUTP, m->db3);
     // dZ2 = (dY W3) * gelu'(Z2)
-    g = gemm(m->dyb, OUTP, m->w3t, OUTP, batch, HID, OUTP, EPI_DGELU, m->status);
+    g = gemm(m->dyb, OUTP, m->w3t, OUTP, batch, HID, OUTP, EPI_DGELU, m->status, m->polls);
     g.Z = m->z2; g.ldz = HID; g.C = m->dz2; g.ldc = HID; g.H = m->dz2b; g.ldh = HID; g.HT = m->dz2t; g.ldht = batch;
     MLP_LAUNCH(launch_gemm(g, 1, s));
     k_colsum<<<HID, 256, 0, s>>>(m->dz2, batch, HID, m->db2);
     // dW2 = dZ2^T H1
-    g = gemm(m->dz2t, batch, m->h1t, batch, HID, HID, batch, EPI_ATOMIC, m->status);
+    g = gemm(m->dz2t, batch, m->h1t, batch, HID, HID, batch, EPI_ATOMIC, m->status, m->polls);
     g.C = m->dw2; g.ldc = HID;
     MLP_LAUNCH(launch_gemm(g, splits, s));
     // dZ1 = (dZ2 W2) * gelu'(Z1)
-    g = gemm(m->dz2b, HID, m->w2t, HID, batch, HID, HID, EPI_DGELU, m->status);
+    g = gemm(m->dz2b, HID, m->w2t, HID, batch, HID, HID, EPI_DGELU, m->status, m->polls);
     g.Z = m->z1; g.ldz = HID; g.C = m->dz1; g.ldc = HID; g.H = m->dz1b; g.ldh = HID; g.HT = m->dz1t; g.ldht = batch;
     MLP_LAUNCH(launch_gemm(g, 1, s));
     k_colsum<<<HID, 256, 0, s>>>(m->dz1, batch, HID, m->db1);
     // dW1 = dZ1^T X
-    g = gemm(m->dz1t, batch, m->xt, batch, HID, IN, batch, EPI_ATOMIC, m->status);
+    g = gemm(m->dz1t, batch, m->xt, batch, HID, IN, batch, EPI_ATOMIC, m->status, m->polls);
     g.C = m->dw1; g.ldc = IN;
     MLP_LAUNCH(launch_gemm(g, splits, s));
     k_gather_grads<<<grid_of(NPARAM), 256, 0, s>>>(m->dw1, m->db1, m->dw2, m->db2, m->dw3t, m->db3, m->g);
@@ -719,7 +736,7 @@ int mlp_forward_device(ntg_mlp *m, const float *d_x, long long rows, float *d_y,
     const long long tiles = (rows + BM - 1) / BM;
     const int grid = (int)std::min<long long>(tiles, std::max(1, sms));
     k_mlp_infer<<<grid, 512, F_BYTES, s>>>(m->w1, m->w2, m->w3, m->p + OFF_B1, m->p + OFF_B2, m->b3p, d_x, rows, d_y,
-                                           m->status);
+                                           m->status, m->polls);
     MLP_LAUNCH(launch_status());
     return NTG_OK;
 }
@@ -842,7 +859,18 @@ int ntg_mlp_train_step(ntg_mlp *m, const float *d_x, const float *d_t, int batch
 
 int ntg_mlp_status(ntg_mlp *m) {
     if (!m) return mlp_fail(NTG_ERROR_INVALID_INPUT, "null network");
+    MLP_CUDA(cudaSetDevice(m->device));
     return check_status(m, nullptr);
+}
+
+int ntg_mlp_set_wait_limit(ntg_mlp *m, int polls) {
+    if (!m) return mlp_fail(NTG_ERROR_INVALID_INPUT, "null network");
+    MLP_CUDA(cudaSetDevice(m->device));
+    MLP_CUDA(cudaDeviceSynchronize());
+    m->polls = polls < 0 ? kWaitPolls : polls;
+    MLP_CUDA(cudaMemset(m->status, 0, sizeof(int)));
+    MLP_CUDA(cudaDeviceSynchronize());
+    return NTG_OK;
 }
 
 int ntg_gemm_bf16(const void *d_a, const void *d_b, int M, int N, int K, float *d_c, void *stream) {

@@ -19,6 +19,8 @@ WRAP_CLAMP, WRAP_REPEAT, WRAP_MIRROR = 0, 1, 2
 FILTER_BOX, FILTER_TRIANGLE, FILTER_KAISER = 0, 1, 2
 ALPHA_NONE, ALPHA_TRANSPARENCY = 0, 1
 XFORM_NONE, XFORM_GAMMA, XFORM_SRGB = 0, 1, 2
+# status codes (nvtt::Error values)
+NTG_OK, NTG_ERROR_INVALID_INPUT, NTG_ERROR_UNSUPPORTED_FEATURE, NTG_ERROR_CUDA = 0, 1, 2, 3
 
 BLOCK_BYTES = {FORMAT_BC1: 8, FORMAT_BC1A: 8, FORMAT_BC3: 16, FORMAT_BC4: 8, FORMAT_BC5: 16}
 
@@ -123,6 +125,7 @@ def lib():
         "ntg_mlp_gradients": (_i, [_vp, _vp, _vp, _i, _vp, ctypes.POINTER(_f), _vp]),
         "ntg_mlp_train_step": (_i, [_vp, _vp, _vp, _i, _f, _vp, _vp]),
         "ntg_mlp_status": (_i, [_vp]),
+        "ntg_mlp_set_wait_limit": (_i, [_vp, _i]),
         "ntg_gemm_bf16": (_i, [_vp, _vp, _i, _i, _i, _vp, _vp]),
         "ntg_compress_chain_learned": (_i, [_vp, _vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _i, _f, _vp,
                                             ctypes.POINTER(ctypes.c_ulonglong), _vp]),
@@ -489,6 +492,10 @@ class MLP:
 
     def status(self):
         _check(lib().ntg_mlp_status(self.h))
+
+    def set_wait_limit(self, polls: int = -1):
+        """Polls of each tensor-core wait before it gives up (-1: the default); clears the status."""
+        _check(lib().ntg_mlp_set_wait_limit(self.h, polls))
 
     def close(self):
         if self.h:

@@ -105,3 +105,33 @@ def test_training_reduces_loss():
         assert loss1 < 0.2 * loss0, (loss0, loss1)
     finally:
         net.close()
+
+
+def test_bounded_waits_run_out_without_a_fault():
+    """A wait limit of zero polls makes every tensor-core wait give up at once: the kernels record the
+    timeout (the status reports it, the gradient call returns the error), drain their issued MMAs, free
+    TMEM and return. With the default limit back, the same network gives the results it gave before."""
+    torch = _torch()
+    net = ntg.MLP(seed=21)
+    try:
+        x, t = _data(1000, 9)
+        dx, dt = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+        before = net.infer(dx).cpu().numpy()
+        grads_before, _ = net.gradients(dx, dt)
+        net.set_wait_limit(0)
+        net.infer(dx)          # the fused kernel's first wait gives up
+        with pytest.raises(ntg.NtgError) as e:
+            net.status()
+        assert e.value.code == ntg.NTG_ERROR_CUDA and "timed out" in str(e.value)
+        with pytest.raises(ntg.NtgError):
+            net.gradients(dx, dt)  # the product kernels' waits give up too
+        net.set_wait_limit(-1)     # default limit, status cleared
+        net.status()
+        after = net.infer(dx).cpu().numpy()
+        grads_after, _ = net.gradients(dx, dt)
+        net.status()
+        assert np.array_equal(before, after)
+        assert torch.equal(torch.isfinite(grads_after), torch.isfinite(grads_before))
+        assert torch.allclose(grads_after, grads_before, rtol=1e-4, atol=1e-6)
+    finally:
+        net.close()
