@@ -26,7 +26,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc") if os.path.exists(os.path.join(CUDA, "b
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["ntg_bc1.cu", "ntg_bc3.cu", "ntg_mip.cu", "ntg_decode.cu", "ntg_noalloc.cu", "ntg_mlp.cu"]
-CPP_SOURCES = ["ntg_api.cpp", "ntg_host_tables.cpp", "nvtt_api.cpp"]
+CPP_SOURCES = ["ntg_api.cpp", "ntg_host_tables.cpp", "nvtt_api.cpp", "nvtt_wrapper.cpp"]
 HEADERS = ["ntg_device.cuh", "ntg_internal.h", "ntg_host_tables.h"]
 
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -61,7 +61,8 @@ def _run(cmd):
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "ntg.h"),
-                                                           os.path.join(ROOT, "include", "nvtt", "nvtt.h")]
+                                                           os.path.join(ROOT, "include", "nvtt", "nvtt.h"),
+                                                           os.path.join(ROOT, "include", "nvtt", "nvtt_wrapper.h")]
     jobs, objs = [], []
     for s in CU_SOURCES:
         src, obj = os.path.join(CSRC, s), os.path.join(OUT, s + ".o")
