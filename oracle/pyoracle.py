@@ -20,7 +20,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libntg_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libnvtt_ref.so")
-REF_SRC = "/root/reference"
+# Where the reference's source tree is: $NTG_REFERENCE_ROOT, else the default of the build recipe
+# oracle/ref/Makefile (asked with `make print-ref`).
+REF_ENV = "NTG_REFERENCE_ROOT"
 
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
@@ -33,9 +35,20 @@ def build_oracle() -> str:
     return ORACLE_SO
 
 
-def build_reference(ref_root: str = REF_SRC) -> str | None:
+def reference_root() -> str:
+    """The reference source tree this machine builds from ($NTG_REFERENCE_ROOT or the recipe's default)."""
+    root = os.environ.get(REF_ENV)
+    if root:
+        return root
+    r = subprocess.run(["make", "-s", "--no-print-directory", "-C", os.path.join(HERE, "ref"), "print-ref"],
+                       capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+def build_reference(ref_root: str | None = None) -> str | None:
     """Compile the reference library when its source tree is present; None otherwise."""
-    if not os.path.isdir(os.path.join(ref_root, "src", "nvtt")):
+    ref_root = ref_root or reference_root()
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src", "nvtt")):
         return None
     subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), f"REF={ref_root}"], check=True)
     return REF_SO

@@ -48,7 +48,7 @@ def float_blocks(n, seed):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=pyoracle.REF_SRC)
+    ap.add_argument("--ref", default=None, help="reference source tree (default: $NTG_REFERENCE_ROOT, else the recipe's)")
     ap.add_argument("--only", choices=["blocks", "dds", "bc1a_bc4"],
                     help="write only the block/chain, the DDS or the BC1a/BC4 block fixtures")
     args = ap.parse_args()
