@@ -17,13 +17,25 @@ import time
 
 import numpy as np
 
-from . import (ALPHA_NONE, ALPHA_TRANSPARENCY, FILTER_BOX, FILTER_KAISER, FORMAT_BC1, MLP, QUALITY_NORMAL, XFORM_NONE,
-               XFORM_SRGB, ChainOptions, Context, chain_levels, nblocks)
+from . import (ALPHA_NONE, ALPHA_TRANSPARENCY, FILTER_BOX, FILTER_KAISER, FORMAT_BC1, FORMAT_BC3, MLP, QUALITY_NORMAL,
+               XFORM_NONE, XFORM_SRGB, ChainOptions, Context, chain_levels, nblocks)
 from . import synth
 
 
 def generator_options(kind: int) -> ChainOptions:
-    """kind 0: linear, box mips, opaque; kind 1: sRGB, Kaiser mips, transparency weighting."""
+    """BC1 blocks: kind 0: linear, box mips, opaque; kind 1: sRGB, Kaiser mips, transparency weighting;
+    kind 2: linear, Kaiser mips, opaque (the batched workloads' BC1 textures). BC3 blocks: kind 3:
+    linear, Kaiser mips, alpha field with transparency weighting (the batched workloads' BC3
+    textures); kind 4: sRGB, Kaiser mips, transparency (the 4096x4096 workload's texture style)."""
+    if kind == 3:
+        return ChainOptions.make(format=FORMAT_BC3, quality=QUALITY_NORMAL, filter=FILTER_KAISER,
+                                 alpha_mode=ALPHA_TRANSPARENCY, in_xform=XFORM_NONE, out_xform=XFORM_NONE)
+    if kind == 4:
+        return ChainOptions.make(format=FORMAT_BC3, quality=QUALITY_NORMAL, filter=FILTER_KAISER,
+                                 alpha_mode=ALPHA_TRANSPARENCY, in_xform=XFORM_SRGB, out_xform=XFORM_SRGB)
+    if kind == 2:
+        return ChainOptions.make(format=FORMAT_BC1, quality=QUALITY_NORMAL, filter=FILTER_KAISER, alpha_mode=ALPHA_NONE,
+                                 in_xform=XFORM_NONE, out_xform=XFORM_NONE)
     if kind == 0:
         return ChainOptions.make(format=FORMAT_BC1, quality=QUALITY_NORMAL, filter=FILTER_BOX, alpha_mode=ALPHA_NONE,
                                  in_xform=XFORM_NONE, out_xform=XFORM_NONE)
@@ -34,18 +46,40 @@ def generator_options(kind: int) -> ChainOptions:
 def generator_texture(kind: int, size: int, seed: int) -> np.ndarray:
     if kind == 0:
         return synth.colour_texture(size, size, seed, scale=size / 512.0)
+    if kind == 2:
+        return synth.batch_texture(size, size, FORMAT_BC1, seed)
+    if kind == 3:
+        return synth.batch_texture(size, size, FORMAT_BC3, seed)
     scale = 8.0 * size / 4096.0
     return synth.colour_texture(size, size, seed, scale=scale, alpha=synth.alpha_field(size, size, seed, scale=scale))
 
 
-def training_set(ctx: Context, n_blocks: int, seed: int = 0x5EED, size: int = 2048):
-    """(x [n x 48], t [n x 8]) float32 CUDA tensors from whole chains of seeded textures,
-    alternating the two generators, until n_blocks samples."""
+def _texture_job(job):
+    return generator_texture(*job)
+
+
+def _generate(jobs):
+    """generator_texture(kind, size, seed) for every job, on every core (spawned processes)."""
+    import multiprocessing as mp
+    import os
+    workers = min(len(jobs), os.cpu_count() or 1)
+    if workers <= 1:
+        return [_texture_job(j) for j in jobs]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        return pool.map(_texture_job, jobs, chunksize=1)
+
+
+def training_set(ctx: Context, n_blocks: int, seed: int = 0x5EED, size: int = 2048, kinds=(0, 1)):
+    """(x [n x 48], t [n x 8]) float32 CUDA tensors from whole chains of seeded textures, cycling
+    through the generators `kinds` (all of one format), until n_blocks samples."""
     import torch
+    per = sum(nblocks(lw, lh) for lw, lh in chain_levels(size, size))
+    count = (n_blocks + per - 1) // per
+    imgs = _generate([(kinds[i % len(kinds)], size, seed + 7919 * i) for i in range(count)])
     xs, ts, have, i = [], [], 0, 0
     while have < n_blocks:
-        kind = i % 2
-        img = generator_texture(kind, size, seed + 7919 * i)
+        kind = kinds[i % len(kinds)]
+        img = imgs[i]
         opt = generator_options(kind)
         d = torch.from_numpy(img).cuda()
         blocks = ctx.compress_chain(d, size, size, opt)
@@ -101,6 +135,32 @@ def chain_rmse(ctx: Context, bgra, w: int, h: int, opt: ChainOptions, blocks) ->
         loff += 4 * n
         boff += 8 * nb
     return math.sqrt(sse / texels)
+
+
+def chain_sse(ctx: Context, bgra, w: int, h: int, opt: ChainOptions, blocks_list):
+    """Per blocks tensor of `blocks_list` (encodings of the same chain): the colour squared-error sum
+    of its decoded levels against the levels the encoder read (linear chains: the mip levels
+    themselves), over all texels of all levels - nvtt::rmsError's sum (alpha-weighted under
+    transparency), in double. One mip chain, then every level's decode and error sums with no host
+    round trip. Returns (list of sums, texels)."""
+    import torch
+    fmt = opt.format
+    bb = 8 if fmt in (1, 2, 6) else 16
+    levels = ctx.mip_chain(bgra, w, h, opt)
+    lv = chain_levels(w, h, opt.max_levels)
+    sums = torch.zeros((len(blocks_list), len(lv), 2), dtype=torch.float64, device=levels.device)
+    texels, loff, boff = 0, 0, 0
+    for li, (lw, lh) in enumerate(lv):
+        n = lw * lh
+        nb = nblocks(lw, lh)
+        ref = levels[loff:loff + 4 * n]
+        for k, blocks in enumerate(blocks_list):
+            dec = ctx.decode(fmt, blocks[boff:boff + bb * nb], lw, lh)
+            ctx.error_sums(ref, dec, lw, lh, opt.alpha_mode, out=sums[k, li])
+        texels += n
+        loff += 4 * n
+        boff += bb * nb
+    return [float(v) for v in sums[:, :, 0].sum(dim=1).cpu()], texels
 
 
 def uniform_proposals(n: int, device="cuda"):

@@ -125,6 +125,31 @@ def batch_texture(w: int, h: int, fmt: int, seed: int) -> np.ndarray:
     return colour_texture(w, h, seed, scale=scale)
 
 
+def _batch_image(args):
+    w, h, fmt, seed = args
+    return batch_texture(w, h, fmt, seed)
+
+
+def batch_workload(count: int, seed: int, kmin: int, kmax: int, workers: int = 0):
+    """The textures of a mixed batch: (w, h, format, image) per texture, in batch_specs order. One
+    seeded image per distinct (size, format), shared by the textures that have both; the distinct
+    images are generated by `workers` processes (0: every core; spawned, so that callers may already
+    hold a GPU context)."""
+    import os
+    specs = batch_specs(count, seed, kmin, kmax)
+    keys = sorted({(w, h, fmt) for (w, h, fmt, _s) in specs}, key=lambda k: (-k[0] * k[1], k))
+    jobs = [(w, h, fmt, seed ^ (w * 131 + h * 7 + fmt)) for (w, h, fmt) in keys]
+    workers = workers or os.cpu_count() or 1
+    if workers > 1 and len(jobs) > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(workers, len(jobs))) as pool:
+            imgs = pool.map(_batch_image, jobs, chunksize=1)
+    else:
+        imgs = [_batch_image(j) for j in jobs]
+    by_key = dict(zip(keys, imgs))
+    return [(w, h, fmt, by_key[(w, h, fmt)]) for (w, h, fmt, _s) in specs]
+
+
 def random_blocks(n: int, seed: int, kind: str = "mixed") -> np.ndarray:
     """n random 4x4 BGRA8 blocks (n, 16, 4) covering smooth, noisy, few-colour and flat cases."""
     rng = np.random.default_rng(seed)

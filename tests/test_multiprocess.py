@@ -55,3 +55,71 @@ def test_reference_arm_under_torchrun_two_ranks(oracle):
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
+
+
+# ---- textures of a batch across ranks (ntg.partition) ----
+
+def test_partition_is_a_balanced_cover():
+    sys.path.insert(0, os.path.join(ROOT, "nvidia-texture-tools_gb300"))
+    from ntg import partition, synth
+    specs = synth.batch_specs(1024, 0xC4, 7, 12)
+    sizes = [(w, h) for (w, h, _f, _s) in specs]
+    work = [partition.chain_texels(w, h) for (w, h) in sizes]
+    for world in (1, 2, 3, 8):
+        parts = partition.partition_textures(sizes, world)
+        assert sorted(i for p in parts for i in p) == list(range(len(sizes)))
+        assert all(p == sorted(p) for p in parts)
+        loads = [sum(work[i] for i in p) for p in parts]
+        bound = max(max(work), sum(work) / world)   # no split can beat this
+        assert max(loads) <= 4 / 3 * bound
+    assert partition.partition([5, 1, 1, 1, 1, 1], 2) == [[0], [1, 2, 3, 4, 5]]
+    with pytest.raises(ValueError):
+        partition.partition([1], 0)
+
+
+def _oracle_chain_bytes(oracle, w, h, fmt, seed):
+    import numpy as np
+    from ntg import synth
+    img = synth.batch_texture(w, h, fmt, seed)
+    _, enc = oracle.mip_chain(img, w, h, 1, 1.0, 0.0, 0.0, 2, 0, 0, 0, 2.2)
+    return np.concatenate([oracle.bc1_image(l.reshape(-1), l.shape[2], l.shape[1], 0, 1) for l in enc])
+
+
+def _partition_rank(rank, world, port, out_dir):
+    import pickle
+    import torch.distributed as dist
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "nvidia-texture-tools_gb300"), os.path.join(ROOT, "oracle")]
+    import pyoracle
+    from ntg import partition, synth
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        specs = synth.batch_specs(10, 0x5A, 3, 6)
+        parts = partition.partition_textures([(w, h) for (w, h, _f, _s) in specs], world)
+        oracle = pyoracle.Oracle()
+        # this rank's textures, whole chains encoded by the CPU oracle (the test machine has no GPU)
+        local = [_oracle_chain_bytes(oracle, *specs[i]) for i in parts[rank]]
+        got = partition.gather(local, parts, rank, world)
+        if rank == 0:
+            with open(os.path.join(out_dir, "gathered.pkl"), "wb") as f:
+                pickle.dump(got, f)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_partitioned_batch_gathers_to_the_one_rank_bytes(tmp_path, oracle):
+    """Two gloo ranks each encode their part of a batch and gather on rank 0: the result is the
+    one-rank batch's bytes, texture by texture, in the batch's order."""
+    import pickle
+    import numpy as np
+    import torch.multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "nvidia-texture-tools_gb300"))
+    from ntg import synth
+    port = _free_port()
+    mp.spawn(_partition_rank, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    with open(tmp_path / "gathered.pkl", "rb") as f:
+        got = pickle.load(f)
+    specs = synth.batch_specs(10, 0x5A, 3, 6)
+    assert len(got) == len(specs)
+    for spec, g in zip(specs, got):
+        assert np.array_equal(g, _oracle_chain_bytes(oracle, *spec))
