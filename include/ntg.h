@@ -280,6 +280,11 @@ int ntg_mlp_status(ntg_mlp *mlp);
  * its TMEM and returns, so later calls run normally. Also clears the recorded status; synchronises
  * the device. No counterpart in the reference. */
 int ntg_mlp_set_wait_limit(ntg_mlp *mlp, int polls);
+/* Search of the learned encode: `radius` is the half-width of the window of orderings around the
+ * proposal's, in each cumulative cluster end; NTG_PROPOSAL_DESCENT | k instead runs a steepest descent
+ * from the proposal's ordering (each move evaluates the orderings one step away in any end and goes to
+ * the lowest error below the current one), at most k moves (BC1). */
+#define NTG_PROPOSAL_DESCENT 256
 /* Learned BC1 encode of a chain (BC1 Normal quality; same options and output layout as
  * ntg_compress_chain). Each block's texels go through the network; the proposal's palette seeds the
  * cluster fit's ordering search, which evaluates only the orderings within `radius` (in each

@@ -8,6 +8,7 @@
 // the cluster-fit search never conflict on banks. The ordering index of the search loop is the
 // same in every thread of a warp, so ordering records are read as constant-cache broadcasts.
 // Built with --fmad=false: results are bit-identical to the reference's scalar build.
+#include "ntg.h"
 #include "ntg_device.cuh"
 #include "ntg_internal.h"
 
@@ -814,9 +815,11 @@ __device__ __forceinline__ Frame block_frame(const Lane<float4> &in, const W &wi
 }
 
 // The network's input: the block's 16 texels as RGB in [0, 1] (as the encoder sees them), in
-// order of their projection on the block's principal axis v (stable; texels of weight 0 take the
-// block's mean colour). Each warp stages its 32 rows in shared memory and writes them out as one
-// contiguous, coalesced run.
+// order of their projection on the block's principal axis v (stable), each pulled towards the block's
+// weighted mean colour in proportion to its fit weight, mu + w (c - mu) (w = 1 for opaque texels,
+// saturate(alpha) under transparency: a texel of weight 0 sits at the mean), so that the network sees
+// how much each texel counts. Each warp stages its 32 rows in shared memory and writes them out as
+// one contiguous, coalesced run.
 constexpr int FEAT_STRIDE = 49;  // floats per staged row (odd: conflict-free)
 
 __global__ void __launch_bounds__(64) k_bc1_features(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
@@ -834,7 +837,8 @@ __global__ void __launch_bounds__(64) k_bc1_features(const EncJob *__restrict__ 
         float key[16];
 #pragma unroll
         for (int k = 0; k < 16; k++) {
-            const f3 c = wi[k] > 0 ? xyz(in[k]) : f.mu;
+            const float wk = wi[k];
+            const f3 c = wk > 0 ? f.mu + (xyz(in[k]) - f.mu) * fminf(wk, 1.0f) : f.mu;
             in[k] = make_float4(c.x, c.y, c.z, 0.0f);
             const float p = dot(c - f.mu, f.v);
             key[k] = p == p ? p : 0.0f;  // NaN texels rank as the mean, so the ranks stay a permutation
@@ -994,6 +998,68 @@ __device__ int pruned_three(const Lane<float4> &sat, int n, f3 metric, int e0, i
     return evaluated;
 }
 
+// Steepest descent over cluster_fit_four's orderings from (e0, e1, e2): each move evaluates the
+// orderings one step away in any of the three ends (up to 26) and goes to the lowest error if it is
+// strictly below the current one; at most `moves` moves. Returns the number evaluated.
+__device__ int descend_four(const Lane<float4> &sat, int n, f3 metric, int e0, int e1, int e2, int moves, f3 &start,
+                            f3 &end) {
+    const float4 s = sat[n];  // a ZERO table
+    const f3 sum = xyz(s);
+    const float wsum = s.w;
+    int c = min(max(e2, 0), n - 1), a = min(max(e0, -1), c), b = min(max(e1, a), c);
+    f3 pa, pb;
+    float best = four_eval<true>(sat, pack_order(a, b, c), sum, wsum, metric, pa, pb);
+    int evaluated = 1;
+    for (int m = 0; m < moves; m++) {
+        float mbest = best;
+        int na = a, nb = b, nc = c;
+        for (int dc = -1; dc <= 1; dc++)
+            for (int da = -1; da <= 1; da++)
+                for (int db = -1; db <= 1; db++) {
+                    const int cc = c + dc, aa = a + da, bb = b + db;
+                    if ((dc | da | db) == 0 || cc < 0 || cc > n - 1 || aa < -1 || aa > bb || bb > cc) continue;
+                    const float e = four_eval<true>(sat, pack_order(aa, bb, cc), sum, wsum, metric, pa, pb);
+                    evaluated++;
+                    if (e < mbest) { mbest = e; na = aa; nb = bb; nc = cc; }
+                }
+        if (!(mbest < best)) break;
+        best = mbest; a = na; b = nb; c = nc;
+    }
+    start = mk3(0, 0, 0);
+    end = mk3(0, 0, 0);
+    if (best < FLT_MAX) four_eval<true>(sat, pack_order(a, b, c), sum, wsum, metric, start, end);
+    return evaluated;
+}
+
+__device__ int descend_three(const Lane<float4> &sat, int n, f3 metric, int e0, int e1, int moves, f3 &start, f3 &end) {
+    const float4 s = sat[n];  // a ZERO table
+    const f3 sum = xyz(s);
+    const float wsum = s.w;
+    int c = min(max(e1, 0), n - 1), a = min(max(e0, -1), c);
+    f3 pa, pb;
+    float best = three_eval<true>(sat, (uint32_t)(a + 1) | ((uint32_t)(c + 1) << 8), sum, wsum, metric, pa, pb);
+    int evaluated = 1;
+    for (int m = 0; m < moves; m++) {
+        float mbest = best;
+        int na = a, nc = c;
+        for (int dc = -1; dc <= 1; dc++)
+            for (int da = -1; da <= 1; da++) {
+                const int cc = c + dc, aa = a + da;
+                if ((dc | da) == 0 || cc < 0 || cc > n - 1 || aa < -1 || aa > cc) continue;
+                const float e = three_eval<true>(sat, (uint32_t)(aa + 1) | ((uint32_t)(cc + 1) << 8), sum, wsum, metric,
+                                                 pa, pb);
+                evaluated++;
+                if (e < mbest) { mbest = e; na = aa; nc = cc; }
+            }
+        if (!(mbest < best)) break;
+        best = mbest; a = na; c = nc;
+    }
+    start = mk3(0, 0, 0);
+    end = mk3(0, 0, 0);
+    if (best < FLT_MAX) three_eval<true>(sat, (uint32_t)(a + 1) | ((uint32_t)(c + 1) << 8), sum, wsum, metric, start, end);
+    return evaluated;
+}
+
 // Warp-aggregated append of this thread's block to `list` (count in *n) when `take`.
 __device__ __forceinline__ void append_block(bool take, long long gblk, long long *list, unsigned long long *n) {
     const unsigned active = __activemask();
@@ -1043,7 +1109,10 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
         const int e0 = frac_end(sat, sn, q0), e1 = max(e0, frac_end(sat, sn, q1));
         const int e2 = max(max(e1, 0), frac_end(sat, sn, q2));
         f3 s0, s1, t0, t1;
-        evaluated += pruned_four(sat, sn, metric, e0, e1, e2, radius, s0, s1);
+        const bool descent = (radius & NTG_PROPOSAL_DESCENT) != 0;
+        const int reach = radius & (NTG_PROPOSAL_DESCENT - 1);
+        evaluated += descent ? descend_four(sat, sn, metric, e0, e1, e2, reach, s0, s1)
+                             : pruned_four(sat, sn, metric, e0, e1, e2, reach, s0, s1);
         Block1 o{0, 0, 0}, cf;
         float err = FLT_MAX;
         bool run3 = true;
@@ -1065,7 +1134,8 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
             float r0 = yp[3], r1 = yp[4];
             if (rev) { const float a = r0; r0 = 1 - r1; r1 = 1 - a; }
             const int f0 = frac_end(sat, sn, r0), f1 = max(max(f0, 0), frac_end(sat, sn, r1));
-            evaluated += pruned_three(sat, sn, metric, f0, f1, radius, t0, t1);
+            evaluated += descent ? descend_three(sat, sn, metric, f0, f1, reach, t0, t1)
+                                 : pruned_three(sat, sn, metric, f0, f1, reach, t0, t1);
         }
         gather_block(J, blk, in, wi);
         float cerr = output_block4(in, wi, cw, s0, s1, cf);

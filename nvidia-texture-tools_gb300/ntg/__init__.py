@@ -19,6 +19,8 @@ WRAP_CLAMP, WRAP_REPEAT, WRAP_MIRROR = 0, 1, 2
 FILTER_BOX, FILTER_TRIANGLE, FILTER_KAISER = 0, 1, 2
 ALPHA_NONE, ALPHA_TRANSPARENCY = 0, 1
 XFORM_NONE, XFORM_GAMMA, XFORM_SRGB = 0, 1, 2
+# learned encode: a steepest descent from the proposal instead of a window (radius = DESCENT | moves)
+NTG_PROPOSAL_DESCENT = 256
 # status codes (nvtt::Error values)
 NTG_OK, NTG_ERROR_INVALID_INPUT, NTG_ERROR_UNSUPPORTED_FEATURE, NTG_ERROR_CUDA = 0, 1, 2, 3
 

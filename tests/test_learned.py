@@ -51,6 +51,23 @@ def test_true_orderings_at_radius_zero(ctx):
     assert _same(out, plain) == 1.0
 
 
+def test_descent_from_true_orderings_stays(ctx):
+    """A steepest descent started at the full search's own orderings finds nothing strictly better one
+    step away (the start is the global minimum), so it keeps them: the full fit's blocks."""
+    import torch
+    size = 128
+    img = learned.generator_texture(2, size, 79)
+    opt = learned.generator_options(2)
+    d = torch.from_numpy(img).cuda()
+    plain = ctx.compress_chain(d, size, size, opt)
+    t = ctx.chain_targets(d, size, size, opt, plain)
+    y = torch.zeros((t.shape[0], 16), dtype=torch.float32, device="cuda")
+    y[:, :6] = t[:, :6]
+    out, st = ctx.compress_chain_proposed(y, d, size, size, opt, radius=ntg.NTG_PROPOSAL_DESCENT | 4, margin=INF)
+    assert _same(out, plain) == 1.0
+    assert st["full_fit"] == 0
+
+
 def test_fallback_list_is_the_full_fit(ctx, net):
     """A margin of -1 sends every fitted block to the full fit through the device-side list."""
     import torch
