@@ -1,20 +1,29 @@
-"""Benchmark: BC1/BC3 + mips Mtexels/s on one GB300 (or N replicas).
+"""Benchmark: BC1/BC3 + mips Mtexels/s on one GB300, learned endpoint proposal vs plain cluster fit.
 
-Workload (default): one 4096x4096 RGBA8 texture, sRGB colour at 8x scale with an independent
-alpha field, Kaiser mip chain (width 3, alpha 4, stretch 1) with sRGB->linear input and
-linear->sRGB output, AlphaMode_Transparency, BC3 Normal quality, 13 levels (22,369,621 texels,
-1,398,103 blocks). A step is one pass of the whole chain: filter every level and encode every
-block. Mtexels/s = encoded texels of all levels / step time.
+Default workload (c4, the configuration the learned proposal's target is quoted on): 1024 textures,
+power-of-two sizes 128..4096 per axis (80% square), 50% BC1 / 30% BC3 (alpha field, transparency) /
+20% BC5 fBm normal maps, linear colour, Normal quality, full Kaiser (width 3, alpha 4, stretch 1) mip
+chains, 4.68e9 texels per step, all in one batch replayed as one CUDA graph (ntg_batch), launch
+shapes autotuned. A step is one replay: filter every level of every texture and encode every block.
+Mtexels/s = encoded texels of all levels / step time.
 
-  value    : device time per step (CUDA events on the launching stream) with the texture resident
-             in HBM; L2 is flushed (256 MiB write) between steps, outside the timed events.
-  e2e      : the same step through the C ABI with host buffers (ntg_compress_chain_host from
-             pinned memory: BGRA8 in, blocks out, copies inside the timed region).
-  roofline : the dominant kernel (the BC3 cluster-fit encoder) against the FP32 issue rate of the
-             clocks seen, plus the mip filter against measured HBM bandwidth.
-  cpu_baseline : the oracle port (C restatement of the reference path) on the host cores.
+  value    : the plain batched cluster fit (bit-identical to the reference), device time per step
+             (CUDA events on the launching stream), inputs resident in HBM; the inputs (14 GB) are far
+             larger than L2, and L2 is also flushed (256 MiB write) between steps.
+  learned  : the same batch with the learned endpoint proposals: per block network -> pruned search ->
+             full fit of the flagged blocks; its Mtexels/s, the ratio to plain, and per texture the
+             RMSE (nvtt::rmsError on the decoded levels) against the plain fit's, at each operating
+             point measured.
+  e2e      : the plain batch through its host-copy binding: every step copies every texture in from
+             pinned host memory and every texture's blocks out, two bindings overlapping copies with
+             the neighbouring steps' graphs.
+  roofline : the dominant kernel (the BC1 cluster fit) against the FP32 rate of the clocks seen, its
+             orderings counted on the device; the mip phase against measured HBM bandwidth.
+  cpu_baseline : the oracle port (C restatement of the reference path) on the host cores, a bounded
+             sample of the workload's textures.
+  c1       : secondary key, the single 4096x4096 sRGB / Kaiser / BC3 chain (workload c1).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload c1|c0]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload c4|c1|c0|c2|c3]
 """
 from __future__ import annotations
 
@@ -56,10 +65,17 @@ BATCHES = {
                                  "graph (ntg_batch), autotuned; BC1 through the learned endpoint proposal"),
 }
 LEARNED_BATCHES = {"c4"}
-# operating point of the learned proposal inside the batched workload (its BC1 textures are linear,
-# noise-dominated colour: the fit's ordering is set by 565 quantisation there, so the network's
-# proposal needs a tighter fallback than on the sRGB workload)
-BATCH_PROPOSAL = {"radius": 2, "margin": 0.1}
+# The learned proposals: per format, the generators (ntg.learned.generator_texture kinds) its network
+# is trained on, and the operating points {format: (search, margin)} measured on the batch (search: a
+# window radius, or DESCENT | moves); the line's headline is the point that keeps the most proposed
+# textures within 0.5% RMSE of the plain fit, the fastest among equals.
+DESCENT = 256
+FORMAT_NAMES = {1: "BC1", 4: "BC3"}
+PROPOSAL_TRAINING = {1: (0, 1, 2)}
+INF = float("inf")
+BATCH_FRONTIER = [{1: (DESCENT | 4, INF)}, {1: (DESCENT | 8, INF)}, {1: (DESCENT | 8, 0.05)}, {1: (2, INF)}]
+# DRAM bytes per block of the BC1 fit (one ncu capture of k_bc1<7>); None until measured
+BC1_TRAFFIC_PER_BLOCK = None
 
 # FP32 operations of one ordering of icbc's cluster fits (src/nvtt/icbc.h:2501-2540 and 2200-2240 in
 # the scalar build), each multiply/add/min/max/round/reciprocal counted once: cluster_fit_four w3 1,
@@ -70,18 +86,25 @@ OPS_PER_ORDERING4 = 140
 OPS_PER_ORDERING3 = 123
 
 # FP32 operations of one cluster-split evaluation of squish's WeightedClusterFit::Compress4
-# (src/nvtt/squish/weightedclusterfit.cpp:505-545), each multiply/add/min/max/floor/divide counted
-# once: w3 3, alpha2 4, beta2 4, alphabeta 2, factor 4, alphax 12, betax 3, a 12, b 12, clamp 12,
-# grid snap 24, e1 39, error 5, compare 1, running sums 4.
-OPS_PER_SPLIT = 141
+# (src/nvtt/squish/weightedclusterfit.cpp:505-545) as the kernel's inner loop runs it, each
+# multiply/add/min/max/floor/reciprocal counted once (no FMA contraction): w3 1, alpha2 2, beta2 3,
+# alphabeta 2, factor 4, alphax 6, betax 3, a and b 24 each (two products, difference, saturating
+# scale, 5:6:5 snap), residual 18, e1 21, error 2, compare 1, running sums 4 = 115.
+OPS_PER_SPLIT = 115
+# Instructions the inner loop issues per split (the FP32 operations plus integer, shared-memory and
+# control instructions), for the issue-slot fraction reported beside the FP32 fraction.
+ISSUE_PER_SPLIT = 141
 
 
 def splits(count: int) -> int:
     return (count + 1) * (count + 2) * (count + 3) // 6
 
 
+T_START = time.perf_counter()
+
+
 def log(*a):
-    print(*a, file=sys.stderr, flush=True)
+    print(f"[{time.perf_counter() - T_START:7.1f} s]", *a, file=sys.stderr, flush=True)
 
 
 class ClockSampler:
@@ -249,8 +272,8 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": desc, "texels_per_step": texels,
                                             "sample": f"top-left {sw}x{sh} quadrant with its full chain"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{sw}x{sh} quadrant of the {name} texture per step; {why}"},
+            "cpu_baseline": dict({"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                  "sample": f"{sw}x{sh} quadrant of the {name} texture per step; {why}"}, **host_cpu()),
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -291,15 +314,58 @@ def split_counts(ctx, levels_flat, spec, steps_table):
     return total_splits
 
 
+def host_cpu():
+    """The host's CPU model, online cores and this process's affinity (recorded with CPU figures)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() in ("Model name", "Model"):
+                model = line.split(":", 1)[1].strip()
+                if not model.isdigit():
+                    break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        import platform
+        model = platform.processor() or platform.machine()
+    try:
+        aff = sorted(os.sched_getaffinity(0))
+    except AttributeError:
+        aff = list(range(os.cpu_count() or 1))
+    ranges, start = [], None
+    for i, c in enumerate(aff):
+        if start is None:
+            start = c
+        if i + 1 == len(aff) or aff[i + 1] != c + 1:
+            ranges.append(f"{start}-{c}" if c != start else f"{c}")
+            start = None
+    return {"cpu_model": model, "nproc": os.cpu_count(), "affinity": ",".join(ranges)}
+
+
 def run_gpu(args):
     import torch
     import ntg
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)
-    name = args.workload
+    ctx = ntg.Context(local)
+    line = measure_chain(ctx, args.workload, args, world, rank, with_cpu=not args.no_cpu and world == 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def measure_chain(ctx, name, args, world, rank, with_cpu):
+    """The single-chain workload `name` (c1, c0): device steps, phase split, e2e through the host-buffer
+    C ABI, rooflines and (with_cpu) the CPU sample; returns the JSON line (rank 0; None elsewhere)."""
+    import torch
+    import ntg
     spec = WORKLOADS[name]
     w, h, fmt, quality, filt, am, ix, ox, desc = spec
-    ctx = ntg.Context(local)
     opt = ntg.ChainOptions.make(format=fmt, quality=quality, filter=filt, alpha_mode=am, in_xform=ix,
                                 out_xform=ox, gamma=2.2)
     bgra = workload_texture(name)
@@ -378,13 +444,16 @@ def run_gpu(args):
             # (22,553,856 B for 349,525 blocks), scaled by the blocks this launch encodes
             blocks = ntg.chain_bytes(w, h, opt) // 16
             traffic = 22553856.0 * blocks / 349525.0
+            issue = nsplits * ISSUE_PER_SPLIT / (enc_ms / 1000.0) / (152 * 4 * sm_mhz * 1e6)
             roof = {"bound": "fp32", "achieved": achieved, "peak": peak_tops, "unit": "TFLOP/s",
-                    "frac": achieved / peak_tops, "traffic": traffic,
+                    "frac": achieved / peak_tops, "traffic": traffic, "issue_slot_frac": issue,
                     "kernel": "k_bc3 (squish weighted cluster fit + DXT5A)",
                     "note": f"peak = 152 SMs x 128 FP32 lanes x median SM clock {sm_mhz:.0f} MHz (derived from the "
                             f"clocks seen; the file of measured peaks has no FP32 figure); {nsplits} splits x "
-                            f"{OPS_PER_SPLIT} ops; encoder phase {enc_ms:.3f} ms (one launch over all levels, "
-                            f"CUDA events on the launching stream, mean of the timed steps)"}
+                            f"{OPS_PER_SPLIT} FP32 ops; issue_slot_frac: {ISSUE_PER_SPLIT} instructions per split over "
+                            f"152 SMs x 4 schedulers x the clock; encoder phase {enc_ms:.3f} ms (one launch over all "
+                            f"levels, CUDA events on the launching stream, mean of 3 runs); traffic: DRAM bytes of one "
+                            f"ncu capture of the same kernel on the 2048x2048 variant, scaled by blocks"}
         # mip filter against HBM: algorithmic bytes = read level l-1 + write level l (FP32 planar),
         # level 0 read as BGRA8, plus the BGRA8 quantised copy each level writes for the encoder
         mip_bytes = 0
@@ -411,11 +480,12 @@ def run_gpu(args):
                     "note": "the Kaiser filter is FP32-bound before it is HBM-bound: 312 FP32 instructions per output "
                             "without FMA contraction"}
         cpu = None
-        if not args.no_cpu and world == 1:
+        if with_cpu:
             try:
                 cpu = cpu_sample(name, bgra, os.cpu_count() or 1)
             except Exception as e:  # reported, not fatal
                 cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+            cpu.update(host_cpu())
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -431,29 +501,21 @@ def run_gpu(args):
                 "split_ms": {"mips": mips_ms, "encode": enc_ms, "chain": chain_ms,
                              "note": "mips and encode from phase events of 3 runs outside the timed region"},
                 "wall_s_timed": wall, "cpu_baseline": cpu}
-        print(json.dumps(line), flush=True)
-    ctx.close()
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
-    return 0
+    return line
 
 
 # ---------------------------------------------------------------------------------------------
 # Batched workloads
 
 def batch_textures(name):
-    """(w, h, format, options tuple, image) per texture. One seeded image per distinct (size, format):
-    textures that share both share the image."""
+    """(w, h, format, options tuple, image) per texture of a batched workload: one seeded image per
+    distinct (size, format), shared by the textures that have both (generated on every core)."""
     import ntg.synth as synth
     count, seed, kmin, kmax, filt, _ = BATCHES[name]
-    cache, out = {}, []
-    for (w, h, fmt, _s) in synth.batch_specs(count, seed, kmin, kmax):
-        key = (w, h, fmt)
-        if key not in cache:
-            cache[key] = synth.batch_texture(w, h, fmt, seed ^ (w * 131 + h * 7 + fmt))
+    out = []
+    for (w, h, fmt, img) in synth.batch_workload(count, seed, kmin, kmax):
         am = 1 if fmt == 4 else 0
-        out.append((w, h, fmt, (fmt, 1, filt, am, 0, 0), cache[key]))
+        out.append((w, h, fmt, (fmt, 1, filt, am, 0, 0), img))
     return out
 
 
@@ -464,15 +526,140 @@ def batch_options(o):
                                  in_xform=ix, out_xform=ox)
 
 
+def timed_launches(batch, steps, warmup, flush, stream):
+    """Per-step device times (ms) of `steps` graph replays after `warmup`, L2 flushed before each."""
+    import torch
+    for _ in range(warmup):
+        batch.launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        batch.launch()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def texture_rmse(ctx, specs, textures, outs_list):
+    """Per texture: the colour RMSE (nvtt::rmsError over all levels) of each encoding in outs_list
+    (a list over encodings of per-texture device blocks), as an [encodings x textures] array."""
+    from ntg import learned
+    r = np.zeros((len(outs_list), len(specs)))
+    for i, ((w, h, fmt, o, img), tex) in enumerate(zip(specs, textures)):
+        sse, n = learned.chain_sse(ctx, tex[0], w, h, tex[3], [outs[i] for outs in outs_list])
+        r[:, i] = np.sqrt(np.asarray(sse) / n)
+    return r
+
+
+def learned_batch(ctx, batch, specs, textures, plain_out, plain_ms, args, flush, stream, world):
+    """The batch with the learned endpoint proposals against the plain fit: one network per format
+    trained on the GPU, timed replays at each operating point of BATCH_FRONTIER, per-texture RMSE of
+    every proposed texture against the plain fit's."""
+    import torch
+    import ntg
+    from ntg import learned
+    cfg = LEARNED
+    nets, training = {}, {}
+    for fmt, kinds in PROPOSAL_TRAINING.items():
+        t0 = time.perf_counter()
+        x, t = learned.training_set(ctx, cfg["train_blocks"], seed=0x5EED + fmt, size=cfg["train_size"], kinds=kinds)
+        data_s = time.perf_counter() - t0
+        net = ntg.MLP(seed=0x4E4554 + fmt)
+        steps = cfg["train_blocks"] // cfg["batch"]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        losses = learned.train(net, x, t, steps=steps, batch=cfg["batch"], lr=cfg["lr"])
+        train_s = time.perf_counter() - t0
+        del x, t
+        torch.cuda.empty_cache()
+        nets[fmt] = net
+        log(f"{FORMAT_NAMES[fmt]} network: data {data_s:.1f} s, training {train_s:.1f} s")
+        training[FORMAT_NAMES[fmt]] = (f"Adam lr {cfg['lr']}, batch {cfg['batch']}, {steps} steps on {cfg['train_blocks']} "
+                                       f"blocks of generators {list(kinds)} (seeds apart from the batch's); data "
+                                       f"{data_s:.1f} s, training {train_s:.1f} s, loss {float(losses[0]):.4f} -> "
+                                       f"{float(losses[-64:].mean()):.4f}")
+    texels = batch.info()["texels"]
+    sel = [i for i, sp in enumerate(specs) if sp[2] in nets]
+    points = []
+    for k, point in enumerate(BATCH_FRONTIER):
+        for fmt, net in nets.items():
+            r_, m_ = point.get(fmt, (None, None))
+            batch.set_proposal(net if r_ is not None else None, radius=r_ or 0, margin=m_ or 0.0, format=fmt)
+        ms = timed_launches(batch, args.steps if k == 0 else max(2, args.steps // 2), args.warmup, flush, stream)
+        step_ms = sum(ms) / len(ms)
+        stats = {FORMAT_NAMES[f]: batch.proposal_stats(format=f) for f in nets if point.get(f, (None,))[0] is not None}
+        points.append({"step_ms": step_ms, "stats": stats, "outs": [textures[i][4].clone() for i in sel]})
+        log(f"learned point {point}: {step_ms:.2f} ms per step")
+    for fmt in nets:
+        batch.set_proposal(None, format=fmt)
+    rm = texture_rmse(ctx, [specs[i] for i in sel], [textures[i] for i in sel],
+                      [[plain_out[i] for i in sel]] + [p["outs"] for p in points])
+    log("per-texture RMSE done")
+    fmts = np.array([specs[i][2] for i in sel])
+    blocks = {f: sum(ntg.chain_bytes(w, h, batch_options(o)) // ntg.BLOCK_BYTES[f] for (w, h, ff, o, img) in specs if ff == f)
+              for f in nets}
+    frontier = []
+    for k, (point, p) in enumerate(zip(BATCH_FRONTIER, points)):
+        d = 100.0 * (rm[k + 1] / np.maximum(rm[0], 1e-30) - 1.0)
+        gated = np.array([point.get(int(f), (None,))[0] is not None for f in fmts])
+        dg = d[gated] if gated.any() else np.zeros(1)
+        f_ = {"point": {FORMAT_NAMES[f]: {"search": (f"descent, {v[0] & (DESCENT - 1)} moves" if v[0] & DESCENT
+                                                     else f"window, radius {v[0]}"),
+                                          "margin": v[1] if v[1] != INF else "inf (no fallback)"}
+                        for f, v in point.items()},
+              "step_ms": p["step_ms"], "value": world * texels / (p["step_ms"] / 1000.0) / 1e6,
+              "speedup_vs_plain": plain_ms / p["step_ms"], "textures_gated": int(gated.sum()),
+              "textures_within_0p5pct": float(np.mean(dg <= 0.5)),
+              "rmse_delta_pct_mean": float(dg.mean()), "rmse_delta_pct_max": float(dg.max()),
+              "textures_bit_equal": int(sum(torch.equal(o, plain_out[i]) for o, i in zip(p["outs"], sel)))}
+        for f in nets:
+            name = FORMAT_NAMES[f]
+            if name in p["stats"]:
+                st = p["stats"][name]
+                f_[name] = {"full_fit_fraction": st["full_fit"] / max(1, blocks[f]),
+                            "orderings_per_kept_block": st["orderings"] / max(1, st["kept"])}
+        frontier.append(f_)
+        del p["outs"]
+    head = max(frontier, key=lambda f: (f["textures_within_0p5pct"], f["speedup_vs_plain"]))
+    fastest = max(frontier, key=lambda f: f["speedup_vs_plain"])
+    for net in nets.values():
+        net.close()
+    return {"value": head["value"], "step_ms": head["step_ms"], "plain_step_ms": plain_ms,
+            "speedup_vs_plain": head["speedup_vs_plain"], "point": head["point"],
+            "textures_within_0p5pct": head["textures_within_0p5pct"], "textures_gated": head["textures_gated"],
+            "rmse_delta_pct_mean": head["rmse_delta_pct_mean"], "rmse_delta_pct_max": head["rmse_delta_pct_max"],
+            "fastest_point": {k: fastest[k] for k in ("point", "speedup_vs_plain", "textures_within_0p5pct",
+                                                       "rmse_delta_pct_mean", "rmse_delta_pct_max")},
+            "gate": "per texture, the colour RMSE over all levels (nvtt::rmsError on the decoded blocks) of the learned "
+                    "encoding within 0.5% of the plain fit's (the plain fit's blocks are the reference's)",
+            "target": ">= 2x the plain fit's Mtexels/s with every texture within 0.5%",
+            "target_met": bool(head["textures_within_0p5pct"] >= 1.0 and head["speedup_vs_plain"] >= 2.0),
+            "formats_with_proposal": [FORMAT_NAMES[f] for f in nets],
+            "network": "per format an MLP 48-256-256-8, GELU (tanh form), BF16 weights/activations, FP32 accumulation "
+                       "(tcgen05), trained on the GPU by the library's own kernels",
+            "training": training, "frontier": frontier}
+
+
 def run_gpu_batch(args):
     import torch
     import ntg
     world, rank, local = dist_setup(args)
-    torch.cuda.set_device(local)
     name = args.workload
     desc = BATCHES[name][5]
+    specs = batch_textures(name)   # before the GPU context: generated by spawned processes
+    log(f"{name}: {len(specs)} textures generated")
+    # N GPUs: the batch's textures split across the ranks (largest first by chain texels), each rank
+    # running the batch of its own part; the whole batch's work is fixed (strong scaling)
+    total_texels = sum(chain_texels(sp[0], sp[1]) for sp in specs)
+    if world > 1:
+        from ntg import partition
+        parts = partition.partition_textures([(sp[0], sp[1]) for sp in specs], world)
+        specs = [specs[i] for i in parts[rank]]
+        log(f"rank {rank}: {len(specs)} textures of the batch")
+    torch.cuda.set_device(local)
     ctx = ntg.Context(local)
-    specs = batch_textures(name)
     textures, host_in = [], []
     for (w, h, fmt, o, img) in specs:
         opt = batch_options(o)
@@ -480,6 +667,7 @@ def run_gpu_batch(args):
         d_out = torch.empty(ntg.chain_bytes(w, h, opt), dtype=torch.uint8, device="cuda")
         textures.append((d_in, w, h, opt, d_out))
         host_in.append(img)
+    log("inputs on the device")
     t0 = time.perf_counter()
     batch = ntg.Batch(ctx, textures)
     build_s = time.perf_counter() - t0
@@ -487,29 +675,19 @@ def run_gpu_batch(args):
     batch.autotune()
     tune_s = time.perf_counter() - t0
     info = batch.info()
-    texels = info["texels"]
+    log(f"batch built ({build_s:.1f} s), autotuned ({tune_s:.1f} s): {info['shape']}")
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
-    for _ in range(args.warmup):
-        batch.launch()
-    torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     barrier(world)
-    torch.cuda.synchronize()
     with ClockSampler(torch.cuda.current_device()) as clk:
         t_wall = time.perf_counter()
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            batch.launch()
-            ends[i].record(stream)
-        torch.cuda.synchronize()
+        step_ms = timed_launches(batch, args.steps, args.warmup, flush, stream)
         barrier(world)
         wall = time.perf_counter() - t_wall
-    dev_ms = max_over_ranks(world, sum(s.elapsed_time(e) for s, e in zip(starts, ends)), torch.device("cuda"))
-    value = world * texels * args.steps / (dev_ms / 1000.0) / 1e6
-    ref_out = [t[4].cpu().numpy() for t in textures]
+    dev_ms = max_over_ranks(world, sum(step_ms), torch.device("cuda"))
+    value = total_texels * args.steps / (dev_ms / 1000.0) / 1e6
+    plain_out = [t[4].clone() for t in textures]
+    log(f"plain: {dev_ms / args.steps:.2f} ms per step")
 
     # end to end: every step copies every texture in from pinned host memory, replays the graph and
     # copies every texture's blocks out; two bindings of the batch (double buffering) let a step's
@@ -518,6 +696,8 @@ def run_gpu_batch(args):
     h_outs = [[torch.empty(t[4].numel(), dtype=torch.uint8).pin_memory() for t in textures] for _ in range(2)]
     bi = sum(int(x.numel()) * 4 for x in h_in)
     bo = sum(int(x.numel()) for x in h_outs[0])
+    # the alternate binding's buffers live as long as the batch: its graph writes them whenever the
+    # batch recaptures
     alt_in = [torch.empty_like(t[0]) for t in textures]
     alt_out = [torch.empty_like(t[4]) for t in textures]
     batch.bind_alternate(alt_in, alt_out)
@@ -555,52 +735,27 @@ def run_gpu_batch(args):
     t0 = time.perf_counter()
     e2e_run(args.steps)
     e2e_s = max_over_ranks(world, time.perf_counter() - t0, torch.device("cuda"))
-    e2e_value = world * texels * args.steps / e2e_s / 1e6
-    same = all(np.array_equal(y.numpy(), r) for y, r in zip(h_outs[(args.steps - 1) & 1], ref_out))
+    e2e_value = total_texels * args.steps / e2e_s / 1e6
+    same = all(torch.equal(y, r.cpu()) for y, r in zip(h_outs[(args.steps - 1) & 1], plain_out))
+    del h_in, h_outs
+    log(f"e2e: {e2e_value:.0f} Mtexels/s")
 
     learned_info = None
-    if name in LEARNED_BATCHES:
-        from ntg import learned
-        cfg = LEARNED
-        x, t = learned.training_set(ctx, cfg["train_blocks"], seed=0x5EED, size=cfg["train_size"])
-        net = ntg.MLP(seed=0x4E4554)
-        learned.train(net, x, t, steps=cfg["train_blocks"] // cfg["batch"], batch=cfg["batch"], lr=cfg["lr"])
-        del x, t
-        plain_out = ref_out
-        batch.set_proposal(net, radius=BATCH_PROPOSAL["radius"], margin=BATCH_PROPOSAL["margin"])
-        for _ in range(args.warmup):
-            batch.launch()
-        torch.cuda.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        for a, b in ev:
-            flush.zero_()
-            a.record(stream)
-            batch.launch()
-            b.record(stream)
-        torch.cuda.synchronize()
-        learned_ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
-        pst = batch.proposal_stats()
-        # per-texture RMSE of the BC1 chains, learned against plain
-        deltas = []
-        for (w, h, fmt, o, img), tex, pl in zip(specs, textures, plain_out):
-            if fmt != 1:
-                continue
-            opt = tex[3]
-            rp = learned.chain_rmse(ctx, tex[0], w, h, opt, torch.from_numpy(pl).cuda())
-            rl = learned.chain_rmse(ctx, tex[0], w, h, opt, tex[4])
-            deltas.append(100 * (rl / rp - 1) if rp > 0 else 0.0)
-        bc1_blocks = sum(ntg.chain_bytes(w, h, batch_options(o)) // 8 for (w, h, fmt, o, img) in specs if fmt == 1)
-        learned_info = {"step_ms": learned_ms, "plain_step_ms": dev_ms / args.steps,
-                        "speedup_vs_plain": (dev_ms / args.steps) / learned_ms,
-                        "value": world * texels / (learned_ms / 1000.0) / 1e6,
-                        "radius": BATCH_PROPOSAL["radius"], "margin": BATCH_PROPOSAL["margin"],
-                        "bc1_full_fit_fraction": pst["full_fit"] / max(1, bc1_blocks),
-                        "bc1_textures": len(deltas), "rmse_delta_pct_max": max(deltas) if deltas else None,
-                        "rmse_delta_pct_mean": float(np.mean(deltas)) if deltas else None,
-                        "textures_within_0p5pct": float(np.mean([d_ <= 0.5 for d_ in deltas])) if deltas else None}
-        batch.set_proposal(None)
-        net.close()
+    if name in LEARNED_BATCHES and not args.no_learned and world == 1:
+        try:
+            learned_info = learned_batch(ctx, batch, specs, textures, plain_out, dev_ms / args.steps, args, flush,
+                                         stream, world)
+        except Exception as e:  # reported in the line; the plain measurement stands
+            import traceback
+            traceback.print_exc()
+            learned_info = {"error": f"{type(e).__name__}: {e}"}
+            for fmt in FORMAT_NAMES:
+                try:
+                    batch.set_proposal(None, format=fmt)
+                except Exception:
+                    pass
 
+    line = None
     if rank == 0:
         phases, blocks = batch.time_phases()
         clocks = clk.summary()
@@ -621,24 +776,32 @@ def run_gpu_batch(args):
                      "algorithmic_bytes": mip_bytes, "ms": phases["mips"], "peak_source": peak_src}
         roof = None
         if dominant == "bc1" and phases["bc1"] > 0:
-            # the BC1 Level8 fit against the FP32 issue peak: orderings counted on the device by the
-            # same gather / reduce_colors the encoder runs, times the operations of one ordering
+            # the BC1 Level8 fit against the FP32 peak: orderings counted on the device by the same
+            # gather / reduce_colors the encoder runs, times the FP32 operations of one ordering
             n4, n3 = batch.count_work()
             sm_mhz_b = clocks["sm_mhz"] or 2070.0
             peak_b = 152 * 128 * sm_mhz_b * 1e6
             ops = n4 * OPS_PER_ORDERING4 + n3 * OPS_PER_ORDERING3
             ach = ops / (phases["bc1"] / 1000.0)
+            nb1 = blocks["bc1"]
             roof = {"bound": "fp32", "achieved": ach / 1e12, "peak": peak_b / 1e12, "unit": "TFLOP/s",
-                    "frac": ach / peak_b, "traffic": None, "kernel": "k_bc1<7> (icbc Level8 cluster fit)",
+                    "frac": ach / peak_b,
+                    "traffic": BC1_TRAFFIC_PER_BLOCK * nb1 if nb1 and BC1_TRAFFIC_PER_BLOCK else None,
+                    "kernel": "k_bc1<7> (icbc Level8 cluster fit)",
                     "note": f"peak = 152 SMs x 128 FP32 lanes x median SM clock {sm_mhz_b:.0f} MHz; {n4} four-cluster x "
-                            f"{OPS_PER_ORDERING4} + {n3} three-cluster x {OPS_PER_ORDERING3} ops over the BC1 phase "
-                            f"({phases['bc1']:.3f} ms, one run outside the graph, CUDA events)"}
+                            f"{OPS_PER_ORDERING4} + {n3} three-cluster x {OPS_PER_ORDERING3} FP32 ops over the BC1 phase "
+                            f"({phases['bc1']:.3f} ms, one run outside the graph, CUDA events); traffic: DRAM bytes per "
+                            f"block of one ncu capture of k_bc1<7>, times the blocks"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": desc, "textures": len(specs), "texels_per_step": texels,
-                           "blocks_per_step": info["blocks"], "l2": "flushed (256 MiB write) between steps",
-                           "method": "plain (non-learned) cluster fit", "replicas": world,
+                "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": desc, "textures": BATCHES[name][0], "texels_per_step": total_texels,
+                           "blocks_per_step": info["blocks"] if world == 1 else None,
+                           "l2": "inputs (14 GB for c4) larger than L2, and L2 flushed (256 MiB write) between steps",
+                           "method": "value: plain (non-learned) cluster fit, bit-identical to the reference; "
+                                     "learned: the endpoint proposals (key 'learned', one GPU)",
+                           "ranks": "one GPU" if world == 1 else f"{world} ranks, the batch's textures partitioned largest "
+                                                                  "first by chain texels (ntg.partition), no exchange",
                            "launch_shape": info["shape"], "build_s": build_s, "autotune_s": tune_s,
                            "images": "one seeded image per distinct (size, format)"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
@@ -646,16 +809,34 @@ def run_gpu_batch(args):
                         "api": "ntg_batch_launch / ntg_batch_launch_alternate (two bindings), copies on two streams"},
                 "gpu_launches": info["launches"] * args.steps,
                 "clocks": clocks, "roofline": roof, "roofline_mips": roof_mips,
-                "phase_ms": phases, "phase_blocks": blocks, "dominant_phase": dominant, "learned": learned_info,
-                "wall_s_timed": wall, "cpu_baseline": None}
+                "phase_ms": phases, "phase_blocks": blocks, "dominant_phase": dominant,
+                "graph_vs_phases_ms": {"step": dev_ms / args.steps, "sum_of_phases": sum(phases.values()),
+                                       "note": "each phase run alone outside the graph; the step replays them all in "
+                                               "one graph"},
+                "learned": learned_info, "wall_s_timed": wall, "cpu_baseline": None}
+    batch.close()
+    del textures, plain_out, alt_in, alt_out
+    torch.cuda.empty_cache()
+    if world == 1 and name == "c4" and not args.no_c1:
+        # secondary key: the single 4096x4096 chain
+        try:
+            c1 = measure_chain(ctx, "c1", args, world, rank, with_cpu=not args.no_cpu)
+            line["c1"] = {k: c1[k] for k in ("value", "ms_per_step", "e2e", "roofline", "roofline_mips", "split_ms",
+                                             "config", "cpu_baseline", "gpu_launches")}
+            log(f"c1: {c1['value']:.0f} Mtexels/s")
+        except Exception as e:  # reported in the line
+            import traceback
+            traceback.print_exc()
+            line["c1"] = {"error": f"{type(e).__name__}: {e}"}
+    if rank == 0:
         if not args.no_cpu and world == 1:
             try:
                 line["cpu_baseline"] = cpu_batch_sample(name, specs, os.cpu_count() or 1, 20.0)
             except Exception as e:  # reported, not fatal
                 line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                         "sample": f"failed: {e}"}
+            line["cpu_baseline"].update(host_cpu())
         print(json.dumps(line), flush=True)
-    batch.close()
     ctx.close()
     if world > 1:
         import torch.distributed as dist
@@ -695,16 +876,21 @@ def run_reference_batch(args):
     sample = cpu_batch_sample(name, specs, threads, budget)
     for _ in range(args.warmup - 1):
         cpu_batch_sample(name, specs, threads, budget)
-    vals = [cpu_batch_sample(name, specs, threads, budget) for _ in range(args.steps)]
+    vals = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        vals.append(cpu_batch_sample(name, specs, threads, budget))
+        vals[-1]["s"] = time.perf_counter() - t0
     value = statistics.mean(v["value"] for v in vals)
     why = ("the reference library itself cannot be built on this host (its source tree is absent), so its C "
            "restatement in oracle/ runs: mips on one thread as the reference filters, encode on every core")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(v["s"] for v in vals),
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": BATCHES[name][5], "sample": sample["sample"]},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample["sample"] + "; " + why},
+            "cpu_baseline": dict({"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                  "sample": sample["sample"] + "; " + why}, **host_cpu()),
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -841,8 +1027,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ntg", choices=["ntg", "reference"])
-    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS) + sorted(BATCHES) + ["c3"])
+    ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS) + sorted(BATCHES) + ["c3"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-learned", action="store_true", help="c4: skip the learned proposals' measurement")
+    ap.add_argument("--no-c1", action="store_true", help="c4: skip the secondary c1 measurement")
     ap.add_argument("--cpu-seconds", type=float, default=5.0, help="CPU work per reference-arm step on batched workloads")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -238,6 +238,11 @@ int ntg_batch_count_work(ntg_batch *batch, void *stream, unsigned long long bc1_
  * (synchronises). */
 int ntg_batch_set_proposal(ntg_batch *batch, struct ntg_mlp *mlp, int radius, float margin);
 int ntg_batch_proposal_stats(ntg_batch *batch, unsigned long long stats[3]);
+/* The same for one format: NTG_FORMAT_BC1 (as above) or NTG_FORMAT_BC3 (the BC3 Normal blocks' colour:
+ * the network, trained on BC3 blocks, proposes squish Compress4's split; see ntg_compress_chain_learned).
+ * Each format keeps its own network, search and margin. */
+int ntg_batch_set_proposal_format(ntg_batch *batch, int format, struct ntg_mlp *mlp, int radius, float margin);
+int ntg_batch_proposal_stats_format(ntg_batch *batch, int format, unsigned long long stats[3]);
 int ntg_batch_destroy(ntg_batch *batch);
 
 /* ---- the learned endpoint proposal's network ----
@@ -285,13 +290,16 @@ int ntg_mlp_set_wait_limit(ntg_mlp *mlp, int polls);
  * from the proposal's ordering (each move evaluates the orderings one step away in any end and goes to
  * the lowest error below the current one), at most k moves (BC1). */
 #define NTG_PROPOSAL_DESCENT 256
-/* Learned BC1 encode of a chain (BC1 Normal quality; same options and output layout as
- * ntg_compress_chain). Each block's texels go through the network; the proposal's palette seeds the
- * cluster fit's ordering search, which evaluates only the orderings within `radius` (in each
- * cumulative cluster end) of the proposal's, with the full search's arithmetic and order; a block
- * whose result's error exceeds (1 + margin) x the network's estimate of the full fit's error gets
- * the full fit. stats (host, may be NULL; then nothing synchronises): {blocks kept from the pruned
- * search, blocks given the full fit, orderings evaluated by the pruned search}. */
+/* Learned encode of a chain (BC1 or BC3 at Normal quality; same options and output layout as
+ * ntg_compress_chain). Each block's texels go through the network; its proposal seeds the cluster
+ * fit's search - icbc's orderings for BC1, squish Compress4's splits for the BC3 colour block - which
+ * evaluates only the orderings within `radius` (in each cumulative cluster end) of the proposal's
+ * (BC1 also: a descent, NTG_PROPOSAL_DESCENT), with the full search's arithmetic and order; a block
+ * whose result's error exceeds (1 + margin) x the network's estimate of the full fit's error gets the
+ * full fit. BC3 alpha is the plain QuickCompress DXT5A. The network must have been trained on blocks
+ * of the chain's format (ntg_chain_features / ntg_chain_targets with the same format). stats (host,
+ * may be NULL; then nothing synchronises): {blocks kept from the pruned search, blocks given the full
+ * fit, orderings evaluated by the pruned search}. */
 int ntg_compress_chain_learned(ntg_context *ctx, ntg_mlp *mlp, const void *d_bgra, int w, int h,
                                const ntg_chain_options *opt, int radius, float margin, void *d_blocks,
                                unsigned long long *stats, void *stream);
@@ -300,10 +308,13 @@ int ntg_compress_chain_learned(ntg_context *ctx, ntg_mlp *mlp, const void *d_bgr
 int ntg_compress_chain_proposed(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,
                                 const float *d_proposals, int radius, float margin, void *d_blocks, unsigned long long *stats,
                                 void *stream);
-/* Training data from a BC1 chain: the network's inputs for every block of every level
- * (d_x [blocks x 48]), and targets (d_t [blocks x 8]) from that chain's encoded blocks d_blocks
- * (e.g. ntg_compress_chain's output): endpoints brighter first and the error term, in the
- * block's frame, then 0. */
+/* Training data from a BC1 or BC3 chain: the network's inputs for every block of every level
+ * (d_x [blocks x 48]: the block's texels as RGB in [0, 1] sorted along its principal axis, each
+ * pulled towards the mean by its fit weight), and targets (d_t [blocks x 8]): the full fit's winning
+ * ordering as cumulative weight fractions (BC1: three four-cluster ends, two three-cluster ends; BC3:
+ * three split ends, then 1/3, 2/3), the fit's error as log((SSE + 1) / (V + 1)) in 8-bit units, 0, 0.
+ * BC1 reads the fit's error from d_blocks (that chain's encoded blocks, e.g. ntg_compress_chain's
+ * output); BC3 runs the search itself (d_blocks is only checked for NULL). */
 int ntg_chain_features(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt, float *d_x,
                        void *stream);
 int ntg_chain_targets(ntg_context *ctx, const void *d_bgra, int w, int h, const ntg_chain_options *opt,

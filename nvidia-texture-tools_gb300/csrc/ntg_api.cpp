@@ -857,7 +857,14 @@ static int chain_common(ntg_context *ctx, const void *d_bgra, int w, int h, cons
     return NTG_OK;
 }
 
-// The learned endpoint proposal over a chain (BC1): the network's inputs for every block of every
+// True when every job has the default colour weights (1, 1, 1): the BC3 fit then skips the metric.
+static bool unit_weights(const std::vector<EncJob> &jobs) {
+    for (const EncJob &j : jobs)
+        if (j.cw[0] != 1.0f || j.cw[1] != 1.0f || j.cw[2] != 1.0f) return false;
+    return true;
+}
+
+// The learned endpoint proposal over a chain (BC1, BC3): the network's inputs for every block of every
 // level, training targets from the plain fit's blocks, or the learned encode (inputs -> network ->
 // pruned fit -> full fit for the listed blocks), all on one stream without host round trips.
 enum { LEARN_FEATURES = 0, LEARN_TARGETS = 1, LEARN_ENCODE = 2 };
@@ -867,7 +874,9 @@ static int chain_learned(ntg_context *ctx, ntg_mlp *mlp, const void *d_bgra, int
                          void *stream, const float *d_proposals = nullptr) {
     NTG_TRY(check_opts(opt_in));
     if (!ctx || !d_bgra || w <= 0 || h <= 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
-    if (opt_in->format != NTG_FORMAT_BC1) return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "the learned proposal is for BC1");
+    const bool bc3 = opt_in->format == NTG_FORMAT_BC3;
+    if (opt_in->format != NTG_FORMAT_BC1 && !bc3)
+        return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "the learned proposal is for BC1 and BC3");
     if (mode == LEARN_ENCODE && ((!mlp && !d_proposals) || opt_in->quality != NTG_QUALITY_NORMAL || radius < 0))
         return fail(NTG_ERROR_INVALID_INPUT, "learned encode needs a network, Quality_Normal and radius >= 0");
     const ntg_chain_options norm = normalized(*opt_in);
@@ -893,21 +902,32 @@ static int chain_learned(ntg_context *ctx, ntg_mlp *mlp, const void *d_bgra, int
     chain_jobs(P, (const uint32_t *)d_bgra, *opt, xt, ws, (uint8_t *)d_blocks, jobs, nblocks);
     NTG_TRY(upload_jobs(ctx, jobs, s));
     const int nj = (int)jobs.size();
-    if (mode == LEARN_FEATURES) return launched(launch_bc1_features(ctx->d_jobs, nj, nblocks, d_aux, s), "block features");
-    if (mode == LEARN_TARGETS) return launched(launch_bc1_targets(ctx->d_jobs, nj, nblocks, d_aux, s), "fit targets");
+    if (mode == LEARN_FEATURES)
+        return launched(bc3 ? launch_bc3_features(ctx->d_jobs, nj, nblocks, d_aux, s)
+                            : launch_bc1_features(ctx->d_jobs, nj, nblocks, d_aux, s), "block features");
+    if (mode == LEARN_TARGETS)
+        return launched(bc3 ? launch_bc3_targets(ctx->d_jobs, nj, nblocks, d_aux, s)
+                            : launch_bc1_targets(ctx->d_jobs, nj, nblocks, d_aux, s), "fit targets");
     float *x = (float *)(ws + xoff), *y = (float *)(ws + yoff);
     long long *list = (long long *)(ws + loff);
     unsigned long long *stats = (unsigned long long *)(ws + soff);
     if (d_proposals) {
         y = const_cast<float *>(d_proposals);
     } else {
-        NTG_TRY(launched(launch_bc1_features(ctx->d_jobs, nj, nblocks, x, s), "block features"));
+        NTG_TRY(launched(bc3 ? launch_bc3_features(ctx->d_jobs, nj, nblocks, x, s)
+                             : launch_bc1_features(ctx->d_jobs, nj, nblocks, x, s), "block features"));
         int r = mlp_forward_device(mlp, x, nblocks, y, s);
         if (r) return fail(r, std::string("proposal network: ") + ntg_last_error_string());
     }
     NTG_CUDA(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), s));
-    NTG_TRY(launched(launch_bc1_learned(ctx->d_jobs, nj, nblocks, y, radius, margin, list, stats, s), "pruned fit"));
-    NTG_TRY(launched(launch_bc1_list(ctx->d_jobs, nj, list, stats + 1, nblocks, s), "full fit of the listed blocks"));
+    if (bc3) {
+        NTG_TRY(launched(launch_bc3_learned(ctx->d_jobs, nj, nblocks, y, radius, margin, unit_weights(jobs), list, stats, s),
+                         "pruned fit"));
+        NTG_TRY(launched(launch_bc3_list(ctx->d_jobs, nj, list, stats + 1, nblocks, s), "full fit of the listed blocks"));
+    } else {
+        NTG_TRY(launched(launch_bc1_learned(ctx->d_jobs, nj, nblocks, y, radius, margin, list, stats, s), "pruned fit"));
+        NTG_TRY(launched(launch_bc1_list(ctx->d_jobs, nj, list, stats + 1, nblocks, s), "full fit of the listed blocks"));
+    }
     if (h_stats) {
         NTG_CUDA(cudaMemcpyAsync(h_stats, stats, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         NTG_CUDA(cudaStreamSynchronize(s));
@@ -1135,11 +1155,12 @@ struct ntg_batch {
     long long texels = 0, blocks = 0;
     int launches = 0;
     std::string key;                      // tuning-cache key (device | batch signature)
-    // learned endpoint proposal for the BC1 Normal blocks (none: the full fit)
-    ntg_mlp *mlp = nullptr;
-    int radius = 1;
-    float margin = 0.5f;
-    uint8_t *d_learn = nullptr;           // network inputs, outputs, full-fit list, statistics
+    // learned endpoint proposals for the BC1 [0] and BC3 [1] Normal blocks (none: the full fit)
+    ntg_mlp *mlp[2] = {nullptr, nullptr};
+    int radius[2] = {1, 1};
+    float margin[2] = {0.5f, 0.5f};
+    uint8_t *d_learn[2] = {nullptr, nullptr};  // network inputs, outputs, full-fit list, statistics
+    bool unit_bc3 = true;                 // every BC3 texture has the default colour weights
     // The alternate binding: the same plan over a second set of inputs and outputs, with its own job
     // lists and graph (double-buffered host copies). Both graphs use the one workspace, so they run
     // one after the other. `which` selects the binding the planning and launching helpers work on.
@@ -1166,7 +1187,8 @@ struct ntg_batch {
         if (d_ws) cudaFree(d_ws);
         if (d_mip) cudaFree(d_mip);
         if (d_enc) cudaFree(d_enc);
-        if (d_learn) cudaFree(d_learn);
+        if (d_learn[0]) cudaFree(d_learn[0]);
+        if (d_learn[1]) cudaFree(d_learn[1]);
     }
 };
 
@@ -1190,9 +1212,13 @@ struct LearnLayout {
     }
 };
 
-bool learned_group(const ntg_batch *b, const ntg_batch::Enc &e) {
-    return b->mlp && e.format == NTG_FORMAT_BC1 && e.quality == NTG_QUALITY_NORMAL;
+// The proposal slot of an encode group (0 BC1, 1 BC3), or -1 when it runs the plain fit.
+int learned_slot(const ntg_batch *b, const ntg_batch::Enc &e) {
+    if (e.quality != NTG_QUALITY_NORMAL) return -1;
+    const int k = e.format == NTG_FORMAT_BC1 ? 0 : (e.format == NTG_FORMAT_BC3 ? 1 : -1);
+    return k >= 0 && b->mlp[k] ? k : -1;
 }
+bool learned_group(const ntg_batch *b, const ntg_batch::Enc &e) { return learned_slot(b, e) >= 0; }
 
 
 // Plans the mip stages and encode launches of a batch for its current tuning and uploads the job
@@ -1286,19 +1312,28 @@ int batch_mips(ntg_batch *b, cudaStream_t s) {
 int batch_encodes(ntg_batch *b, cudaStream_t s, int only_slot = -1) {
     for (const auto &e : b->encodes) {
         if (only_slot >= 0 && enc_slot(e.format) != only_slot) continue;
-        if (learned_group(b, e)) {
+        const int k = learned_slot(b, e);
+        if (k >= 0) {
             const LearnLayout L(e.nblocks);
-            float *x = (float *)(b->d_learn + L.x), *y = (float *)(b->d_learn + L.y);
-            long long *list = (long long *)(b->d_learn + L.list);
-            unsigned long long *stats = (unsigned long long *)(b->d_learn + L.stats);
+            uint8_t *buf = b->d_learn[k];
+            float *x = (float *)(buf + L.x), *y = (float *)(buf + L.y);
+            long long *list = (long long *)(buf + L.list);
+            unsigned long long *stats = (unsigned long long *)(buf + L.stats);
             const EncJob *jobs = b->denc() + e.first;
-            NTG_TRY(launched(launch_bc1_features(jobs, e.njobs, e.nblocks, x, s), "block features"));
-            const int r = mlp_forward_device(b->mlp, x, e.nblocks, y, s);
+            NTG_TRY(launched(k ? launch_bc3_features(jobs, e.njobs, e.nblocks, x, s)
+                               : launch_bc1_features(jobs, e.njobs, e.nblocks, x, s), "block features"));
+            const int r = mlp_forward_device(b->mlp[k], x, e.nblocks, y, s);
             if (r) return fail(r, std::string("proposal network: ") + ntg_last_error_string());
             NTG_CUDA(cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), s));
-            NTG_TRY(launched(launch_bc1_learned(jobs, e.njobs, e.nblocks, y, b->radius, b->margin, list, stats, s),
-                             "pruned fit"));
-            NTG_TRY(launched(launch_bc1_list(jobs, e.njobs, list, stats + 1, e.nblocks, s), "full fit of the listed blocks"));
+            if (k) {
+                NTG_TRY(launched(launch_bc3_learned(jobs, e.njobs, e.nblocks, y, b->radius[k], b->margin[k], b->unit_bc3, list,
+                                                    stats, s), "pruned fit"));
+                NTG_TRY(launched(launch_bc3_list(jobs, e.njobs, list, stats + 1, e.nblocks, s), "full fit of the listed blocks"));
+            } else {
+                NTG_TRY(launched(launch_bc1_learned(jobs, e.njobs, e.nblocks, y, b->radius[k], b->margin[k], list, stats, s),
+                                 "pruned fit"));
+                NTG_TRY(launched(launch_bc1_list(jobs, e.njobs, list, stats + 1, e.nblocks, s), "full fit of the listed blocks"));
+            }
             continue;
         }
         NTG_TRY(launch_encode(e.format, b->denc() + e.first, e.njobs, e.nblocks, e.quality, s, b->enc_threads[enc_slot(e.format)]));
@@ -1679,33 +1714,49 @@ int ntg_batch_count_work(ntg_batch *b, void *stream, unsigned long long bc1_orde
     return status == NTG_OK ? NTG_OK : fail(status, "fit work count failed");
 }
 
-int ntg_batch_set_proposal(ntg_batch *b, ntg_mlp *mlp, int radius, float margin) {
+int ntg_batch_set_proposal_format(ntg_batch *b, int format, ntg_mlp *mlp, int radius, float margin) {
     g_error.clear();
-    if (!b || radius < 0) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    if (!b || radius < 0 || (format != NTG_FORMAT_BC1 && format != NTG_FORMAT_BC3))
+        return fail(NTG_ERROR_INVALID_INPUT, "bad arguments (proposals are for BC1 and BC3)");
     std::lock_guard<std::mutex> lk(b->ctx->mu);
     NTG_TRY(ensure_device(b->ctx));
-    b->mlp = mlp;
-    b->radius = radius;
-    b->margin = margin;
+    const int k = format == NTG_FORMAT_BC3 ? 1 : 0;
+    b->mlp[k] = mlp;
+    b->radius[k] = radius;
+    b->margin[k] = margin;
     long long nb = 0;
     for (const auto &e : b->encodes)
-        if (learned_group(b, e)) nb = std::max(nb, e.nblocks);
-    if (b->d_learn) { cudaFree(b->d_learn); b->d_learn = nullptr; }
-    if (mlp && nb > 0) NTG_CUDA(cudaMalloc((void **)&b->d_learn, LearnLayout(nb).bytes));
+        if (learned_slot(b, e) == k) nb = std::max(nb, e.nblocks);
+    if (b->d_learn[k]) { cudaFree(b->d_learn[k]); b->d_learn[k] = nullptr; }
+    if (mlp && nb > 0) NTG_CUDA(cudaMalloc((void **)&b->d_learn[k], LearnLayout(nb).bytes));
+    b->unit_bc3 = true;
+    for (const auto &o : b->opts)
+        if (o.format == NTG_FORMAT_BC3 && !(o.cw[0] == 0 && o.cw[1] == 0 && o.cw[2] == 0) &&
+            !(o.cw[0] == 1 && o.cw[1] == 1 && o.cw[2] == 1))
+            b->unit_bc3 = false;
     return batch_replan(b);
 }
 
-int ntg_batch_proposal_stats(ntg_batch *b, unsigned long long stats[3]) {
+int ntg_batch_set_proposal(ntg_batch *b, ntg_mlp *mlp, int radius, float margin) {
+    return ntg_batch_set_proposal_format(b, NTG_FORMAT_BC1, mlp, radius, margin);
+}
+
+int ntg_batch_proposal_stats_format(ntg_batch *b, int format, unsigned long long stats[3]) {
     g_error.clear();
     if (!b || !stats) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    const int k = format == NTG_FORMAT_BC3 ? 1 : 0;
     stats[0] = stats[1] = stats[2] = 0;
     for (const auto &e : b->encodes) {
-        if (!learned_group(b, e)) continue;
+        if (learned_slot(b, e) != k) continue;
         NTG_CUDA(cudaDeviceSynchronize());
-        NTG_CUDA(cudaMemcpy(stats, b->d_learn + LearnLayout(e.nblocks).stats, 3 * sizeof(unsigned long long),
+        NTG_CUDA(cudaMemcpy(stats, b->d_learn[k] + LearnLayout(e.nblocks).stats, 3 * sizeof(unsigned long long),
                             cudaMemcpyDeviceToHost));
     }
     return NTG_OK;
+}
+
+int ntg_batch_proposal_stats(ntg_batch *b, unsigned long long stats[3]) {
+    return ntg_batch_proposal_stats_format(b, NTG_FORMAT_BC1, stats);
 }
 
 int ntg_batch_destroy(ntg_batch *b) {

@@ -210,12 +210,16 @@ struct SquishSet {
     uint64_t order;        // 4 bits per sorted position: slot
     f3 xsum;
     float wsum;
+    f3 axis;               // the principal axis the points are sorted along (arbitrary sign)
+    f3 xxsum;              // sum of weight x colour^2 per channel over the points (the error's constant)
 };
 
-template <bool DXT1, typename Arr>
-__device__ __forceinline__ void squish_prepare(const uint32_t px[16], bool weight_by_alpha, f3 metric, Arr wp,
-                                               SquishSet &S) {
-    float X[16], Y[16], Z[16], W[16];
+// The minimal colour set in texel slots (colours, summed weights, live slots, transparent texels,
+// each texel's slot) and its principal axis (ComputeWeightedCovariance, ComputePrincipleComponent).
+template <bool DXT1>
+__device__ __forceinline__ f3 squish_points(const uint32_t px[16], bool weight_by_alpha, f3 metric, float X[16], float Y[16],
+                                            float Z[16], float W[16], uint32_t &live_out, uint32_t &transp_out,
+                                            uint64_t &first_out) {
     uint32_t live = 0;  // bit i: slot i holds a point
     uint32_t transp = 0;
     uint64_t first = 0;
@@ -241,7 +245,6 @@ __device__ __forceinline__ void squish_prepare(const uint32_t px[16], bool weigh
         if (!found) live |= 1u << i;
         first |= (uint64_t)slot << (4 * i);
     }
-    const int count = __popc(live);
     float total = 0.0f;
     f3 cen = mk3(0, 0, 0);
 #pragma unroll
@@ -270,6 +273,20 @@ __device__ __forceinline__ void squish_prepare(const uint32_t px[16], bool weigh
         if (norm == 0.0f) { v = mk3(0, 0, 0); break; }
         v = mk3(x * iv, y * iv, z * iv);
     }
+    live_out = live;
+    transp_out = transp;
+    first_out = first;
+    return v;
+}
+
+template <bool DXT1, typename Arr>
+__device__ __forceinline__ void squish_prepare(const uint32_t px[16], bool weight_by_alpha, f3 metric, Arr wp,
+                                               SquishSet &S) {
+    float X[16], Y[16], Z[16], W[16];
+    uint32_t live, transp;
+    uint64_t first;
+    const f3 v = squish_points<DXT1>(px, weight_by_alpha, metric, X, Y, Z, W, live, transp, first);
+    const int count = __popc(live);
     // stable insertion sort along the axis; slot numbers carried in a packed 64-bit word
     float dps[16];
     uint64_t order = 0;
@@ -297,13 +314,13 @@ __device__ __forceinline__ void squish_prepare(const uint32_t px[16], bool weigh
             }
         }
     }
-    f3 xsum = mk3(0, 0, 0);
+    f3 xsum = mk3(0, 0, 0), xxsum = mk3(0, 0, 0);
     float wsum = 0.0f;
 #pragma unroll
     for (int i = 0; i < 16; i++) {
         f3 p = mk3(X[i], Y[i], Z[i]) * W[i];
         wp[i] = make_float4(p.x, p.y, p.z, W[i]);
-        if (i < count) { xsum = xsum + p; wsum += W[i]; }
+        if (i < count) { xsum = xsum + p; wsum += W[i]; xxsum = xxsum + p * mk3(X[i], Y[i], Z[i]); }
     }
     wp[16] = make_float4(0, 0, 0, 0);
     S.count = count;
@@ -312,6 +329,8 @@ __device__ __forceinline__ void squish_prepare(const uint32_t px[16], bool weigh
     S.order = order;
     S.xsum = xsum;
     S.wsum = wsum;
+    S.axis = v;
+    S.xxsum = xxsum;
 }
 
 // Compress4's split search: the first strict minimum, as best error and split key
@@ -442,11 +461,9 @@ __device__ __forceinline__ int squish_565(f3 c) {
     return (float_to_int(31.0f * c.x, 31) << 11) | (float_to_int(63.0f * c.y, 63) << 5) | float_to_int(31.0f * c.z, 31);
 }
 
-template <bool UNIT_METRIC, typename Arr>
-__device__ __forceinline__ uint2 squish_block4(const SquishSet &S, f3 msq, Arr wp, float &err) {
-    int best;
-    err = squish_search4<UNIT_METRIC>(S, msq, wp, best);
-    if (!(err < FLT_MAX)) return make_uint2(0, 0);
+// WriteColourBlock4 of the split with key `best` (cluster sizes b0 << 10 | b1 << 5 | b2).
+template <typename Arr>
+__device__ __forceinline__ uint2 squish_finish4(const SquishSet &S, Arr wp, int best) {
     const int b0 = best >> 10, b1 = (best >> 5) & 31, b2 = best & 31;
     f3 x0, x1, x2;
     float w0, w1, w2;
@@ -465,6 +482,14 @@ __device__ __forceinline__ uint2 squish_block4(const SquishSet &S, f3 msq, Arr w
     if (ea < eb) { int t = ea; ea = eb; eb = t; idx ^= 0x55555555u; }
     else if (ea == eb) idx = 0;
     return make_uint2((uint32_t)ea | ((uint32_t)eb << 16), idx);
+}
+
+template <bool UNIT_METRIC, typename Arr>
+__device__ __forceinline__ uint2 squish_block4(const SquishSet &S, f3 msq, Arr wp, float &err) {
+    int best;
+    err = squish_search4<UNIT_METRIC>(S, msq, wp, best);
+    if (!(err < FLT_MAX)) return make_uint2(0, 0);
+    return squish_finish4(S, wp, best);
 }
 
 template <bool UNIT_METRIC, typename Arr>
@@ -661,11 +686,17 @@ __device__ __forceinline__ void load_block(const EncJob &J, int x, int y, uint32
 #endif
 
 template <int QUALITY>
-__global__ void __launch_bounds__(128, NTG_BC3_MIN_CTAS) k_bc3(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
+__global__ void __launch_bounds__(128, NTG_BC3_MIN_CTAS) k_bc3(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
+                                                              const long long *__restrict__ list,
+                                                              const unsigned long long *__restrict__ count) {
     extern __shared__ float4 smem[];
     const int T = blockDim.x, t = threadIdx.x;
-    const long long gblk = (long long)blockIdx.x * T + t;
+    long long gblk = (long long)blockIdx.x * T + t;
     if (gblk >= nblocks) return;
+    if (list) {  // a subset of the jobs' blocks (the learned path's fallbacks), *count long
+        if ((unsigned long long)gblk >= *count) return;
+        gblk = list[gblk];
+    }
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
     uint32_t px[16];
@@ -760,15 +791,336 @@ __global__ void __launch_bounds__(128) k_bc4(const EncJob *__restrict__ jobs, in
     pack_alpha(QUALITY >= 2 ? dxt5a_optimal(ch) : dxt5a_quick(ch), J.out + 8 * (size_t)blk);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Learned endpoint proposal for the BC3 colour block (no counterpart in the reference). The network
+// (the same MLP as BC1's, trained on BC3 blocks) reads the block's 16 texels as the encoder sees them
+// (after ColorBlock's quantiser, RGB / 255) in order of their projection on the squish principal axis
+// oriented towards brighter colours (stable), each pulled towards the block's weighted mean colour in
+// proportion to its fit weight (mu + w (c - mu), w = (alpha + 1) / 256 under transparency), and
+// proposes Compress4's winning split as three cumulative weight fractions of the sorted colour set in
+// that orientation, and the fit's error. The pruned search evaluates only the splits whose three
+// cumulative ends lie within `radius` of the proposal's, with the full search's arithmetic and in its
+// order, so a block whose best split is in that window gets exactly the full fit's colour block. A
+// block whose pruned error exceeds (1 + margin) x the network's estimate of the full fit's error is
+// listed for the full k_bc3. Errors are in 8-bit units: SSE8 = 255^2 x (the search's error + the
+// constant it leaves out), V the block's weighted colour variance in the same units; the network's
+// error output is log((SSE8 + 1) / (V + 1)).
+
+struct Bc3Frame {
+    bool reversed;  // the squish axis points towards darker colours
+    float var;      // V
+};
+
+__device__ __forceinline__ f3 texel_rgb(uint32_t p) {
+    return mk3((float)((p >> 16) & 255) / 255.0f, (float)((p >> 8) & 255) / 255.0f, (float)(p & 255) / 255.0f);
+}
+__device__ __forceinline__ float texel_weight(uint32_t p, bool weight_by_alpha) {
+    return weight_by_alpha ? (float)((p >> 24) + 1) / 256.0f : 1.0f;
+}
+
+// The block's frame for its axis `v` (squish's), and, when `row` is given, the network's input row.
+// The texels are read again from the packed words at each use, so that only their sort keys are live.
+__device__ __forceinline__ Bc3Frame bc3_inputs(const uint32_t px[16], bool weight_by_alpha, f3 metric, f3 v, float *row) {
+    Bc3Frame fr;
+    fr.reversed = (v.x + v.y + v.z) < 0.0f;
+    float ws = 0.0f;
+    f3 mu = mk3(0, 0, 0);
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        const float w = texel_weight(px[i], weight_by_alpha);
+        ws += w;
+        mu = mu + texel_rgb(px[i]) * w;
+    }
+    mu = mu * (1.0f / ws);
+    float var = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        const f3 d = ((texel_rgb(px[i]) - mu) * metric) * 255.0f;
+        var += texel_weight(px[i], weight_by_alpha) * dot(d, d);
+    }
+    fr.var = var;
+    if (row) {
+        float key[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const float p = dot(texel_rgb(px[i]), v);
+            key[i] = fr.reversed ? -p : p;
+        }
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            int rank = 0;
+#pragma unroll
+            for (int j = 0; j < 16; j++) rank += (key[j] < key[i]) | ((key[j] == key[i]) & (j < i));
+            const f3 c = mu + (texel_rgb(px[i]) - mu) * texel_weight(px[i], weight_by_alpha);
+            row[3 * rank] = c.x; row[3 * rank + 1] = c.y; row[3 * rank + 2] = c.z;
+        }
+    }
+    return fr;
+}
+
+// Compress4's splits whose cumulative ends lie in [lo_k, hi_k] (e1 <= e2 <= e3 <= count), in the full
+// search's order, with its running sums: every sum is accumulated point by point from its cluster's
+// first point as squish_search4's loops accumulate it (the partial sums before a window's start are
+// built the same way), and each split's error uses the loops' operations in their order, so every
+// evaluated split's error equals the full search's bit for bit. Returns the best error (first strict
+// minimum) and its key in `best` (-1 when none compares below FLT_MAX); `evaluated` counts the splits.
+template <bool UNIT_METRIC, typename Arr>
+__device__ __forceinline__ float squish_window4(const SquishSet &S, f3 msq, Arr wp, int lo1, int hi1, int lo2, int hi2,
+                                               int lo3, int hi3, int &best, int &evaluated) {
+    const int n = S.count;
+    float besterr = FLT_MAX;
+    best = -1;
+    f3 x0 = mk3(0, 0, 0);
+    float w0 = 0.0f;
+    for (int i = 0; i < lo1; i++) { const float4 q = wp[i]; x0 = x0 + mk3(q.x, q.y, q.z); w0 += q.w; }
+    for (int e1 = lo1; e1 <= hi1; e1++) {
+        const int a2lo = max(e1, lo2);
+        f3 x1 = mk3(0, 0, 0);
+        float w1 = 0.0f;
+        for (int i = e1; i < a2lo; i++) { const float4 q = wp[i]; x1 = x1 + mk3(q.x, q.y, q.z); w1 += q.w; }
+        for (int e2 = a2lo; e2 <= hi2; e2++) {
+            const float wr = S.wsum - w0 - w1;
+            const float a2p = w0 + w1 * (4.0f / 9.0f);
+            const float w1n = w1 * (1.0f / 9.0f);
+            const f3 axp = x0 + (x1 * (2.0f / 3.0f));
+            const int a3lo = max(e2, lo3);
+            f3 x2 = mk3(0, 0, 0);
+            float w2 = 0.0f;
+            for (int i = e2; i < a3lo; i++) { const float4 q = wp[i]; x2 = x2 + mk3(q.x, q.y, q.z); w2 += q.w; }
+            for (int e3 = a3lo; e3 <= hi3; e3++) {
+                const float w3 = wr - w2;
+                const float a2 = a2p + w2 * (1.0f / 9.0f);
+                const float b2s = w3 + w2 * (4.0f / 9.0f) + w1n;
+                const float ab = (w1 + w2) * (2.0f / 9.0f);
+                const float f = 1.0f / (a2 * b2s - ab * ab);
+                const f3 ax = axp + (x2 * (1.0f / 3.0f));
+                const f3 bx = S.xsum - ax;
+                const f3 a = snap565((ax * b2s) - (bx * ab), f);
+                const f3 b = snap565((bx * a2) - (ax * ab), f);
+                const f3 t = (((a * b) * ab) - (a * ax)) - (b * bx);
+                const f3 e = (((a * a) * a2) + ((b * b) * b2s)) + (t * 2.0f);
+                const float err = UNIT_METRIC ? (e.x + e.y) + e.z : dot(e, msq);
+                evaluated++;
+                if (err < besterr) { besterr = err; best = (e1 << 10) | ((e2 - e1) << 5) | (e3 - e2); }
+                if (e3 < n) { const float4 q = wp[e3]; x2 = x2 + mk3(q.x, q.y, q.z); w2 += q.w; }
+            }
+            if (e2 < n) { const float4 q = wp[e2]; x1 = x1 + mk3(q.x, q.y, q.z); w1 += q.w; }
+        }
+        if (e1 < n) { const float4 q = wp[e1]; x0 = x0 + mk3(q.x, q.y, q.z); w0 += q.w; }
+    }
+    return besterr;
+}
+
+// Cumulative end of a weight fraction over the sorted points: the number of leading points whose
+// cumulative weight is within it.
+template <typename Arr>
+__device__ __forceinline__ int frac_count(const SquishSet &S, Arr wp, float frac) {
+    const float lim = frac * S.wsum * (1.0f + 1e-5f) + 1e-7f;
+    float cum = 0.0f;
+    int e = 0;
+    for (int i = 0; i < S.count; i++) {
+        cum += wp[i].w;
+        if (cum <= lim) e = i + 1;
+    }
+    return e;
+}
+
+// The search error of the block's best split in 8-bit units.
+__device__ __forceinline__ float squish_sse8(const SquishSet &S, f3 msq, float err) {
+    return (err + dot(S.xxsum, msq)) * 65025.0f;
+}
+
+// The network's inputs for every block: x [nblocks x 48], staged per warp and written coalesced.
+constexpr int BC3_FEAT_STRIDE = 49;
+
+__global__ void __launch_bounds__(64, 8) k_bc3_features(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
+                                                        float *__restrict__ x) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x, lane = t & 31;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    float *stage = reinterpret_cast<float *>(smem) + (t >> 5) * 32 * BC3_FEAT_STRIDE;
+    if (gblk < nblocks) {
+        const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+        const int blk = (int)(gblk - J.first_block);
+        uint32_t px[16];
+        load_block(J, 4 * (blk % J.bw), 4 * (blk / J.bw), px);
+        const f3 metric = mk3(J.cw[0], J.cw[1], J.cw[2]);
+        float X[16], Y[16], Z[16], W[16];  // only the axis is needed here: the points are not sorted
+        uint32_t live, transp;
+        uint64_t first;
+        const f3 v = squish_points<false>(px, J.alpha_mode == 1, metric, X, Y, Z, W, live, transp, first);
+        bc3_inputs(px, J.alpha_mode == 1, metric, v, stage + lane * BC3_FEAT_STRIDE);
+    }
+    __syncwarp();
+    const long long base = (long long)blockIdx.x * T + (t & ~31);
+    const int rows = (int)min(32LL, nblocks - base);
+    for (int q = lane; q < rows * 48; q += 32) x[base * 48 + q] = stage[(q / 48) * BC3_FEAT_STRIDE + q % 48];
+}
+
+// Training targets from the full fit: tg [nblocks x 8] = the winning split's three cumulative weight
+// fractions (in the inputs' orientation), 1/3 and 2/3 (the network's three-cluster outputs, unused
+// for BC3), log((SSE8 + 1) / (V + 1)), 0, 0. Single-colour blocks (no search) get 0, 0, 0.
+__global__ void __launch_bounds__(128) k_bc3_targets(const EncJob *__restrict__ jobs, int njobs, long long nblocks,
+                                                     float *__restrict__ tg) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    uint32_t px[16];
+    load_block(J, 4 * (blk % J.bw), 4 * (blk / J.bw), px);
+    float *o = tg + gblk * 8;
+    o[3] = 1.0f / 3.0f; o[4] = 2.0f / 3.0f; o[6] = 0.0f; o[7] = 0.0f;
+    bool single = true;
+#pragma unroll
+    for (int i = 1; i < 16; i++) single = single && ((px[i] & 0xFFFFFF) == (px[0] & 0xFFFFFF));
+    struct { float4 *b; int s; __device__ float4 &operator[](int k) const { return b[k * s]; } } wp{smem + t, T};
+    const f3 metric = mk3(J.cw[0], J.cw[1], J.cw[2]);
+    SquishSet S;
+    squish_prepare<false>(px, J.alpha_mode == 1, metric, wp, S);
+    const Bc3Frame fr = bc3_inputs(px, J.alpha_mode == 1, metric, S.axis, nullptr);
+    if (single) {
+        o[0] = o[1] = o[2] = 0.0f;
+        o[5] = logf(1.0f / (fr.var + 1.0f));
+        return;
+    }
+    int best;
+    const f3 msq = metric * metric;
+    const float err = squish_search4<false>(S, msq, wp, best);
+    const int e1 = best >> 10, e2 = e1 + ((best >> 5) & 31), e3 = e2 + (best & 31);
+    float c1 = 0.0f, c2 = 0.0f, c3 = 0.0f, cum = 0.0f;
+    for (int i = 0; i < S.count; i++) {
+        cum += wp[i].w;
+        if (i + 1 == e1) c1 = cum;
+        if (i + 1 == e2) c2 = cum;
+        if (i + 1 == e3) c3 = cum;
+    }
+    float f1 = c1 / S.wsum, f2 = c2 / S.wsum, f3v = c3 / S.wsum;
+    if (fr.reversed) { const float a = f1; f1 = 1.0f - f3v; f2 = 1.0f - f2; f3v = 1.0f - a; }
+    o[0] = f1; o[1] = f2; o[2] = f3v;
+    const float sse = err < FLT_MAX ? squish_sse8(S, msq, err) : fr.var;
+    o[5] = logf((fmaxf(sse, 0.0f) + 1.0f) / (fr.var + 1.0f));
+}
+
+// Learned BC3 Normal encode: alpha as k_bc3<1> (QuickCompress DXT5A), colour from the pruned split
+// search around the network's proposal y [nblocks x 16]; a listed block is rewritten whole by the
+// full k_bc3. radius: the window half-width in each cumulative end. stats[0] += blocks kept here,
+// stats[1] = list length, stats[2] += splits evaluated.
+template <bool UNIT_METRIC>
+__global__ void __launch_bounds__(128, NTG_BC3_MIN_CTAS) k_bc3_learned(const EncJob *__restrict__ jobs, int njobs,
+                                                                      long long nblocks, const float *__restrict__ y,
+                                                                      int radius, float margin, long long *__restrict__ list,
+                                                                      unsigned long long *__restrict__ stats) {
+    extern __shared__ float4 smem[];
+    const int T = blockDim.x, t = threadIdx.x;
+    const long long gblk = (long long)blockIdx.x * T + t;
+    if (gblk >= nblocks) return;
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    uint32_t px[16];
+    load_block(J, 4 * (blk % J.bw), 4 * (blk / J.bw), px);
+    uint8_t *dst = J.out + 16 * (size_t)blk;
+    {   // alpha first, so that the texels are dead during the search
+        int al[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) al[i] = (int)(px[i] >> 24);
+        pack_alpha(dxt5a_quick(al), dst);
+    }
+    bool single = true;
+#pragma unroll
+    for (int i = 1; i < 16; i++) single = single && ((px[i] & 0xFFFFFF) == (px[0] & 0xFFFFFF));
+    bool take = false;
+    int evaluated = 0;
+    uint2 col = make_uint2(0, 0);
+    if (single) {
+        col = dxt1_single_color((px[0] >> 16) & 255, (px[0] >> 8) & 255, px[0] & 255);
+    } else {
+        struct { float4 *b; int s; __device__ float4 &operator[](int k) const { return b[k * s]; } } wp{smem + t, T};
+        const f3 metric = mk3(J.cw[0], J.cw[1], J.cw[2]);
+        const f3 msq = metric * metric;
+        SquishSet S;
+        squish_prepare<false>(px, J.alpha_mode == 1, metric, wp, S);
+        const Bc3Frame fr = bc3_inputs(px, J.alpha_mode == 1, metric, S.axis, nullptr);
+        const float *yp = y + gblk * 16;
+        const float pred = (fr.var + 1.0f) * expf(yp[5]) - 1.0f;
+        float q1 = yp[0], q2 = yp[1], q3 = yp[2];
+        if (fr.reversed) { const float a = q1; q1 = 1.0f - q3; q2 = 1.0f - q2; q3 = 1.0f - a; }
+        const int n = S.count;
+        const int p1 = frac_count(S, wp, q1), p2 = max(p1, frac_count(S, wp, q2)), p3 = max(p2, frac_count(S, wp, q3));
+        int bkey;
+        const float best = squish_window4<UNIT_METRIC>(S, msq, wp, max(0, p1 - radius), min(n, p1 + radius),
+                                                       max(0, p2 - radius), min(n, p2 + radius), max(0, p3 - radius),
+                                                       min(n, p3 + radius), bkey, evaluated);
+        take = bkey < 0 || !(squish_sse8(S, msq, best) <= (1.0f + margin) * pred);  // NaN estimates fall back too
+        if (!take) col = squish_finish4(S, wp, bkey);
+    }
+    if (!take) *reinterpret_cast<uint2 *>(dst + 8) = col;
+    // the list and the statistics, warp-aggregated
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync(active, take);
+    const int lane = threadIdx.x & 31, leader = __ffs(active) - 1;
+    unsigned long long kept = take ? 0 : 1, ev = (unsigned long long)evaluated;
+    for (int off = 16; off > 0; off >>= 1) {
+        kept += __shfl_down_sync(active, kept, off);
+        ev += __shfl_down_sync(active, ev, off);
+    }
+    unsigned long long base = 0;
+    if (lane == leader) {
+        if (mask) base = atomicAdd(&stats[1], (unsigned long long)__popc(mask));
+        atomicAdd(&stats[0], kept);
+        atomicAdd(&stats[2], ev);
+    }
+    base = __shfl_sync(active, base, leader);
+    if (take) list[base + __popc(mask & ((1u << lane) - 1))] = gblk;
+}
+
+int launch_bc3_features(const EncJob *d_jobs, int njobs, long long nblocks, float *x, cudaStream_t stream) {
+    if (nblocks == 0) return 0;
+    const int T = 64;
+    const size_t sm = 2 * 32 * BC3_FEAT_STRIDE * sizeof(float);
+    k_bc3_features<<<(unsigned)((nblocks + T - 1) / T), T, sm, stream>>>(d_jobs, njobs, nblocks, x);
+    return launch_status();
+}
+
+int launch_bc3_targets(const EncJob *d_jobs, int njobs, long long nblocks, float *tg, cudaStream_t stream) {
+    if (nblocks == 0) return 0;
+    const int T = 128;
+    k_bc3_targets<<<(unsigned)((nblocks + T - 1) / T), T, (size_t)T * 17 * sizeof(float4), stream>>>(d_jobs, njobs, nblocks,
+                                                                                                      tg);
+    return launch_status();
+}
+
+int launch_bc3_learned(const EncJob *d_jobs, int njobs, long long nblocks, const float *y, int radius, float margin,
+                       bool unit_metric, long long *list, unsigned long long *stats, cudaStream_t stream) {
+    if (nblocks == 0) return 0;
+    const int T = 128;
+    const size_t sm = (size_t)T * 17 * sizeof(float4);
+    const unsigned grid = (unsigned)((nblocks + T - 1) / T);
+    if (unit_metric) k_bc3_learned<true><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks, y, radius, margin, list, stats);
+    else k_bc3_learned<false><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks, y, radius, margin, list, stats);
+    return launch_status();
+}
+
+// The full BC3 Normal fit over the first *d_count entries of `list` (at most max_count).
+int launch_bc3_list(const EncJob *d_jobs, int njobs, const long long *list, const unsigned long long *d_count,
+                    long long max_count, cudaStream_t stream) {
+    if (max_count == 0) return 0;
+    const int T = 128;
+    const size_t sm = (size_t)T * 17 * sizeof(float4);
+    k_bc3<1><<<(unsigned)((max_count + T - 1) / T), T, sm, stream>>>(d_jobs, njobs, max_count, list, d_count);
+    return launch_status();
+}
+
 int launch_bc3(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
     const int T = threads == 32 || threads == 64 ? threads : 128;  // blocks per CTA
     const size_t sm = (size_t)T * 17 * sizeof(float4);
     const unsigned grid = (unsigned)((nblocks + T - 1) / T);
     switch (quality) {
-        case 0: k_bc3<0><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks); break;
-        case 3: k_bc3<3><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks); break;
-        default: k_bc3<1><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks); break;
+        case 0: k_bc3<0><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks, nullptr, nullptr); break;
+        case 3: k_bc3<3><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks, nullptr, nullptr); break;
+        default: k_bc3<1><<<grid, T, sm, stream>>>(d_jobs, njobs, nblocks, nullptr, nullptr); break;
     }
     return launch_status();
 }

@@ -60,6 +60,14 @@ int launch_bc1_features(const EncJob *d_jobs, int njobs, long long nblocks, floa
 int launch_bc1_targets(const EncJob *d_jobs, int njobs, long long nblocks, float *tg, cudaStream_t s);
 int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const float *y, int radius, float margin,
                        long long *fallback, unsigned long long *stats, cudaStream_t s);
+// The same for BC3 Normal colour (squish Compress4 splits): inputs, targets, pruned fit (unit_metric:
+// all colour weights 1), and the full k_bc3 over a list.
+int launch_bc3_features(const EncJob *d_jobs, int njobs, long long nblocks, float *x, cudaStream_t s);
+int launch_bc3_targets(const EncJob *d_jobs, int njobs, long long nblocks, float *tg, cudaStream_t s);
+int launch_bc3_learned(const EncJob *d_jobs, int njobs, long long nblocks, const float *y, int radius, float margin,
+                       bool unit_metric, long long *fallback, unsigned long long *stats, cudaStream_t s);
+int launch_bc3_list(const EncJob *d_jobs, int njobs, const long long *list, const unsigned long long *d_count,
+                    long long max_count, cudaStream_t s);
 // Orderings the Level8 fit evaluates over the jobs' blocks (four-cluster, three-cluster), added to
 // work[0], work[1] (measurement only).
 int launch_bc1_work(const EncJob *d_jobs, int njobs, long long nblocks, unsigned long long *work, cudaStream_t s);

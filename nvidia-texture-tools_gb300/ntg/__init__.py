@@ -117,6 +117,8 @@ def lib():
         "ntg_batch_count_work": (_i, [_vp, _vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "ntg_batch_set_proposal": (_i, [_vp, _vp, _i, _f]),
         "ntg_batch_proposal_stats": (_i, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+        "ntg_batch_set_proposal_format": (_i, [_vp, _i, _vp, _i, _f]),
+        "ntg_batch_proposal_stats_format": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_ulonglong)]),
         "ntg_mlp_create": (_i, [_i, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
         "ntg_mlp_destroy": (_i, [_vp]),
         "ntg_mlp_param_count": (_i, []),
@@ -408,14 +410,16 @@ class Batch:
         keys = ("strip", "threads", "tail_texels", "bc1_blocks_per_cta", "bc3_blocks_per_cta", "bc5_blocks_per_cta")
         return {"texels": tex.value, "blocks": blk.value, "launches": n.value, "shape": dict(zip(keys, list(shape)))}
 
-    def set_proposal(self, mlp, radius=1, margin=0.5):
-        """Learned endpoint proposal for the batch's BC1 Normal blocks (mlp None: the full fit)."""
-        self._mlp = mlp
-        _check(lib().ntg_batch_set_proposal(self.h, mlp.h if mlp is not None else None, radius, margin))
+    def set_proposal(self, mlp, radius=1, margin=0.5, format=FORMAT_BC1):
+        """Learned endpoint proposal for the batch's BC1 (or BC3) Normal blocks (mlp None: the full fit)."""
+        if not hasattr(self, "_mlps"):
+            self._mlps = {}
+        self._mlps[format] = mlp
+        _check(lib().ntg_batch_set_proposal_format(self.h, format, mlp.h if mlp is not None else None, radius, margin))
 
-    def proposal_stats(self):
+    def proposal_stats(self, format=FORMAT_BC1):
         st = (ctypes.c_ulonglong * 3)()
-        _check(lib().ntg_batch_proposal_stats(self.h, st))
+        _check(lib().ntg_batch_proposal_stats_format(self.h, format, st))
         return {"kept": st[0], "full_fit": st[1], "orderings": st[2]}
 
     def time_phases(self, stream=None):
