@@ -444,14 +444,15 @@ def measure_chain(ctx, name, args, world, rank, with_cpu):
             # (22,553,856 B for 349,525 blocks), scaled by the blocks this launch encodes
             blocks = ntg.chain_bytes(w, h, opt) // 16
             traffic = 22553856.0 * blocks / 349525.0
-            issue = nsplits * ISSUE_PER_SPLIT / (enc_ms / 1000.0) / (152 * 4 * sm_mhz * 1e6)
+            # thread instructions / 32 = warp instructions, against one issue per scheduler per clock
+            issue = nsplits * ISSUE_PER_SPLIT / 32 / (enc_ms / 1000.0) / (152 * 4 * sm_mhz * 1e6)
             roof = {"bound": "fp32", "achieved": achieved, "peak": peak_tops, "unit": "TFLOP/s",
                     "frac": achieved / peak_tops, "traffic": traffic, "issue_slot_frac": issue,
                     "kernel": "k_bc3 (squish weighted cluster fit + DXT5A)",
                     "note": f"peak = 152 SMs x 128 FP32 lanes x median SM clock {sm_mhz:.0f} MHz (derived from the "
                             f"clocks seen; the file of measured peaks has no FP32 figure); {nsplits} splits x "
-                            f"{OPS_PER_SPLIT} FP32 ops; issue_slot_frac: {ISSUE_PER_SPLIT} instructions per split over "
-                            f"152 SMs x 4 schedulers x the clock; encoder phase {enc_ms:.3f} ms (one launch over all "
+                            f"{OPS_PER_SPLIT} FP32 ops; issue_slot_frac: {ISSUE_PER_SPLIT} instructions per split (per "
+                            f"thread; / 32 per warp) over 152 SMs x 4 schedulers x the clock; encoder phase {enc_ms:.3f} ms (one launch over all "
                             f"levels, CUDA events on the launching stream, mean of 3 runs); traffic: DRAM bytes of one "
                             f"ncu capture of the same kernel on the 2048x2048 variant, scaled by blocks"}
         # mip filter against HBM: algorithmic bytes = read level l-1 + write level l (FP32 planar),

@@ -290,6 +290,10 @@ int ntg_mlp_set_wait_limit(ntg_mlp *mlp, int polls);
  * from the proposal's ordering (each move evaluates the orderings one step away in any end and goes to
  * the lowest error below the current one), at most k moves (BC1). */
 #define NTG_PROPOSAL_DESCENT 256
+/* Also with the BC1 search: after it, the block's endpoints are refitted by weighted least squares for
+ * its indices (at most twice, kept only when the error drops) - a step the plain Level8 fit does not
+ * take, so refitted blocks can be better than the reference's. */
+#define NTG_PROPOSAL_REFIT 512
 /* Learned encode of a chain (BC1 or BC3 at Normal quality; same options and output layout as
  * ntg_compress_chain). Each block's texels go through the network; its proposal seeds the cluster
  * fit's search - icbc's orderings for BC1, squish Compress4's splits for the BC3 colour block - which

@@ -1060,6 +1060,37 @@ __device__ int descend_three(const Lane<float4> &sat, int n, f3 metric, int e0, 
     return evaluated;
 }
 
+// Least-squares refit of a four-colour block's endpoints (an addition of the learned path; the plain
+// Level8 fit has none): the weighted least-squares endpoints of the block's texels for its current
+// indices (index 0 -> first endpoint, 1 -> second, 2 -> 2/3 first + 1/3 second, 3 -> 1/3 + 2/3), snapped
+// to 5:6:5 and re-indexed by the output stage; kept when the block's error drops, twice at most.
+// Returns the block's error. Three-colour blocks are left as they are.
+template <typename W>
+__device__ float ls_refit(const Lane<float4> &in, const W &wi, f3 cw, float err, Block1 &o) {
+    for (int it = 0; it < 2 && o.c0 > o.c1; it++) {
+        float a2 = 0, b2 = 0, ab = 0;
+        f3 ax = mk3(0, 0, 0), bx = mk3(0, 0, 0);
+        for (int i = 0; i < 16; i++) {
+            const unsigned bits = (o.idx >> (2 * i)) & 3;
+            const float beta = bits == 0 ? 0.0f : (bits == 1 ? 1.0f : (bits == 2 ? 1.0f / 3.0f : 2.0f / 3.0f));
+            const float alpha = 1.0f - beta, w = wi[i];
+            const f3 p = xyz(in[i]);
+            a2 += w * alpha * alpha; b2 += w * beta * beta; ab += w * alpha * beta;
+            ax = ax + p * (w * alpha); bx = bx + p * (w * beta);
+        }
+        const float den = a2 * b2 - ab * ab;
+        if (!(fabsf(den) > 1e-6f)) break;
+        const float f = 1.0f / den;
+        const f3 na = sat3(((ax * b2) - (bx * ab)) * f), nb = sat3(((bx * a2) - (ax * ab)) * f);
+        Block1 t;
+        const float e = output_block4(in, wi, cw, na, nb, t);
+        if (!(e < err)) break;
+        err = e;
+        o = t;
+    }
+    return err;
+}
+
 // Warp-aggregated append of this thread's block to `list` (count in *n) when `take`.
 __device__ __forceinline__ void append_block(bool take, long long gblk, long long *list, unsigned long long *n) {
     const unsigned active = __activemask();
@@ -1110,7 +1141,7 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
         const int e2 = max(max(e1, 0), frac_end(sat, sn, q2));
         f3 s0, s1, t0, t1;
         const bool descent = (radius & NTG_PROPOSAL_DESCENT) != 0;
-        const int reach = radius & (NTG_PROPOSAL_DESCENT - 1);
+        const int reach = radius & (NTG_PROPOSAL_DESCENT - 1);  // the flags are above the reach's bits
         evaluated += descent ? descend_four(sat, sn, metric, e0, e1, e2, reach, s0, s1)
                              : pruned_four(sat, sn, metric, e0, e1, e2, reach, s0, s1);
         Block1 o{0, 0, 0}, cf;
@@ -1145,6 +1176,7 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
             if (e3 < cerr) { cerr = e3; cf = b3; }
         }
         if (cerr < err) { o = cf; err = cerr; }
+        if (radius & NTG_PROPOSAL_REFIT) err = ls_refit(in, wi, cw, err, o);
         take = !(err <= (1.0f + margin) * full_pred);  // NaN estimates fall back too
         if (!take) store_block(out, o);
     }

@@ -21,6 +21,7 @@ ALPHA_NONE, ALPHA_TRANSPARENCY = 0, 1
 XFORM_NONE, XFORM_GAMMA, XFORM_SRGB = 0, 1, 2
 # learned encode: a steepest descent from the proposal instead of a window (radius = DESCENT | moves)
 NTG_PROPOSAL_DESCENT = 256
+NTG_PROPOSAL_REFIT = 512     # BC1: least-squares endpoint refit after the search
 # status codes (nvtt::Error values)
 NTG_OK, NTG_ERROR_INVALID_INPUT, NTG_ERROR_UNSUPPORTED_FEATURE, NTG_ERROR_CUDA = 0, 1, 2, 3
 
