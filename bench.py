@@ -71,9 +71,10 @@ LEARNED_BATCHES = {"c4"}
 # textures within 0.5% RMSE of the plain fit, the fastest among equals.
 DESCENT = 256
 FORMAT_NAMES = {1: "BC1", 4: "BC3"}
-PROPOSAL_TRAINING = {1: (0, 1, 2)}
+PROPOSAL_TRAINING = {1: (0, 1, 2), 4: (3, 4)}
 INF = float("inf")
-BATCH_FRONTIER = [{1: (DESCENT | 4, INF)}, {1: (DESCENT | 8, INF)}, {1: (DESCENT | 8, 0.05)}, {1: (2, INF)}]
+BATCH_FRONTIER = [{1: (DESCENT | 4, INF)}, {1: (DESCENT | 8, 0.05)}, {1: (DESCENT | 4, INF), 4: (2, INF)},
+                  {1: (2, INF)}]
 # DRAM bytes per block of the BC1 fit (one ncu capture of k_bc1<7>); None until measured
 BC1_TRAFFIC_PER_BLOCK = None
 

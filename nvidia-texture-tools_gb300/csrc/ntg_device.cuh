@@ -98,6 +98,36 @@ __device__ __forceinline__ float powf_5_11(float x) {
     return c_tab.pow_5_11[u >> 23] * pm;
 }
 
+// Packed FP32 pairs: two floats in one 64-bit register (the first in the low half) added by one
+// instruction (add.rn.f32x2, sm_100 and later), which rounds each half exactly as the scalar
+// add.rn.f32 does. The products that feed it stay scalar multiplies: a packed multiply whose result
+// feeds a packed add is contracted into a packed fused multiply-add after PTX (one rounding instead
+// of two, measured on sm_103a), which would change the sums, while a scalar multiply feeding a packed
+// add is not. So a tap sum += k * v over four channels is 4 multiplies and 2 packed adds, bit for bit
+// the 8 scalar instructions' result.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// A float4 as two pairs (x, y) and (z, w), and back: the same 16 bytes.
+struct F4x2 { f32x2 xy, zw; };
+__device__ __forceinline__ float4 f4_of(const F4x2 &p) {
+    const ulonglong2 u = make_ulonglong2(p.xy, p.zw);
+    return *reinterpret_cast<const float4 *>(&u);
+}
+// sum += k * v on all four channels.
+__device__ __forceinline__ void tap2(F4x2 &sum, float k, const float4 &v) {
+    sum.xy = f2_add(sum.xy, f2_pack(k * v.x, k * v.y));
+    sum.zw = f2_add(sum.zw, f2_pack(k * v.z, k * v.w));
+}
+
 // ColorBlock::init(float) quantiser (src/nvimage/ColorBlock.cpp:103-106).
 __device__ __forceinline__ uint32_t quant_u8(float x) { return (uint32_t)(uint8_t)(255 * ic_clamp(x, 0.0f, 1.0f)); }
 

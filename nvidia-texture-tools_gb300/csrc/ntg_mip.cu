@@ -448,13 +448,21 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
     for (int j = 0; j < WS; j++) { kx[j] = __ldg(L.kx + j); ky[j] = __ldg(L.ky + j); }
 
     // X taps of every window row: output column x (= lane) reads source columns 2x .. 2x + WS - 1
+    // (unweighted: two channels per packed add, the same roundings as the scalar taps)
     for (int r = tid >> 5; r < rh; r += nwarps) {
         const float4 *row = region + r * ROW + lane;
-        float4 sum = make_float4(0, 0, 0, 0);
-        float norm = 0;
+        if constexpr (WEIGHTED) {
+            float4 sum = make_float4(0, 0, 0, 0);
+            float norm = 0;
 #pragma unroll
-        for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, kx[j], row[(j & 1) * HALF + (j >> 1)]);
-        tmp[r * TW + lane] = finish<WEIGHTED>(sum, norm);
+            for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, kx[j], row[(j & 1) * HALF + (j >> 1)]);
+            tmp[r * TW + lane] = finish<WEIGHTED>(sum, norm);
+        } else {
+            F4x2 sum{0, 0};
+#pragma unroll
+            for (int j = 0; j < WS; j++) tap2(sum, kx[j], row[(j & 1) * HALF + (j >> 1)]);
+            tmp[r * TW + lane] = f4_of(sum);
+        }
     }
     __syncthreads();
 
@@ -465,11 +473,19 @@ __global__ void __launch_bounds__(512, 2) k_tile2x(const MipJob *__restrict__ jo
     uint32_t *const qd = L.q_out ? L.q_out + (size_t)y0 * w + x0 + lane : nullptr;
     for (int y = tid >> 5; y < ty; y += nwarps) {
         const float4 *col = tmp + (2 * y) * TW + lane;
-        float4 sum = make_float4(0, 0, 0, 0);
-        float norm = 0;
+        float4 v;
+        if constexpr (WEIGHTED) {
+            float4 sum = make_float4(0, 0, 0, 0);
+            float norm = 0;
 #pragma unroll
-        for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, ky[j], col[j * TW]);
-        const float4 v = finish<WEIGHTED>(sum, norm);
+            for (int j = 0; j < WS; j++) tap<WEIGHTED>(sum, norm, ky[j], col[j * TW]);
+            v = finish<WEIGHTED>(sum, norm);
+        } else {
+            F4x2 sum{0, 0};
+#pragma unroll
+            for (int j = 0; j < WS; j++) tap2(sum, ky[j], col[j * TW]);
+            v = f4_of(sum);
+        }
         float *const d = dst + (size_t)y * w;
         d[0] = v.x;
         d[dn] = v.y;
@@ -615,16 +631,29 @@ __global__ void __launch_bounds__(1024, 1) k_tile2x_u8(const MipJob *__restrict_
                 __syncwarp();
                 // X taps: lane -> output columns 2 lane, 2 lane + 1 = staged columns D + 4 lane + t,
                 // t in [0, WS) and [2, WS + 2)
-                float4 s0 = make_float4(0, 0, 0, 0), s1 = s0;
-                float n0 = 0, n1 = 0;
+                if constexpr (WEIGHTED) {
+                    float4 s0 = make_float4(0, 0, 0, 0), s1 = s0;
+                    float n0 = 0, n1 = 0;
 #pragma unroll
-                for (int t = 0; t < WS + 2; t++) {
-                    const float4 v = scratch[((D + t) & 3) * QP + ((D + t) >> 2) + lane];
-                    if (t < WS) tap<WEIGHTED>(s0, n0, kx[t], v);
-                    if (t >= 2) tap<WEIGHTED>(s1, n1, kx[t - 2], v);
+                    for (int t = 0; t < WS + 2; t++) {
+                        const float4 v = scratch[((D + t) & 3) * QP + ((D + t) >> 2) + lane];
+                        if (t < WS) tap<WEIGHTED>(s0, n0, kx[t], v);
+                        if (t >= 2) tap<WEIGHTED>(s1, n1, kx[t - 2], v);
+                    }
+                    xp[r * TW + 2 * lane] = finish<WEIGHTED>(s0, n0);
+                    xp[r * TW + 2 * lane + 1] = finish<WEIGHTED>(s1, n1);
+                } else {
+                    // two channels per packed add, the same roundings as the scalar taps
+                    F4x2 s0{0, 0}, s1{0, 0};
+#pragma unroll
+                    for (int t = 0; t < WS + 2; t++) {
+                        const float4 v = scratch[((D + t) & 3) * QP + ((D + t) >> 2) + lane];
+                        if (t < WS) tap2(s0, kx[t], v);
+                        if (t >= 2) tap2(s1, kx[t - 2], v);
+                    }
+                    xp[r * TW + 2 * lane] = f4_of(s0);
+                    xp[r * TW + 2 * lane + 1] = f4_of(s1);
                 }
-                xp[r * TW + 2 * lane] = finish<WEIGHTED>(s0, n0);
-                xp[r * TW + 2 * lane + 1] = finish<WEIGHTED>(s1, n1);
             } else {
                 // Y taps of tile i - 1: output rows 2 p, 2 p + 1 (p = k / 2) of column 32 (k % 2) + lane
                 // read X rows 4 p + t, t in [0, WS) and [2, WS + 2)
@@ -632,11 +661,23 @@ __global__ void __launch_bounds__(1024, 1) k_tile2x_u8(const MipJob *__restrict_
                 const float4 *const col = yp + (4 * p) * TW + x;
                 float4 s0 = make_float4(0, 0, 0, 0), s1 = s0;
                 float n0 = 0, n1 = 0;
+                if constexpr (WEIGHTED) {
 #pragma unroll
-                for (int t = 0; t < WS + 2; t++) {
-                    const float4 v = col[t * TW];
-                    if (t < WS) tap<WEIGHTED>(s0, n0, s_ky[t], v);
-                    if (t >= 2) tap<WEIGHTED>(s1, n1, s_ky[t - 2], v);
+                    for (int t = 0; t < WS + 2; t++) {
+                        const float4 v = col[t * TW];
+                        if (t < WS) tap<WEIGHTED>(s0, n0, s_ky[t], v);
+                        if (t >= 2) tap<WEIGHTED>(s1, n1, s_ky[t - 2], v);
+                    }
+                } else {
+                    F4x2 p0{0, 0}, p1{0, 0};
+#pragma unroll
+                    for (int t = 0; t < WS + 2; t++) {
+                        const float4 v = col[t * TW];
+                        if (t < WS) tap2(p0, s_ky[t], v);
+                        if (t >= 2) tap2(p1, s_ky[t - 2], v);
+                    }
+                    s0 = f4_of(p0);
+                    s1 = f4_of(p1);
                 }
                 const TilePos pos = tile_u8_pos<WS>(jobs, njobs, blockIdx.x + (i - 1) * g);
                 const MipJob &L = *pos.L;
