@@ -75,8 +75,10 @@ PROPOSAL_TRAINING = {1: (0, 1, 2), 4: (3, 4)}
 INF = float("inf")
 BATCH_FRONTIER = [{1: (DESCENT | 4, INF)}, {1: (DESCENT | 8, 0.05)}, {1: (DESCENT | 4, INF), 4: (2, INF)},
                   {1: (2, INF)}]
-# DRAM bytes per block of the BC1 fit (one ncu capture of k_bc1<7>); None until measured
-BC1_TRAFFIC_PER_BLOCK = None
+# DRAM bytes per block of the BC1 fit: one ncu capture of k_bc1<7> over 262,144 blocks of a 2048x2048
+# planar FP32 level (67,384,064 B read + 712,192 B written, profiles/k_bc1_7_cases_2048.md), per block;
+# the batch's BC1 levels are planar FP32 too, so the traffic scales with the blocks
+BC1_TRAFFIC_PER_BLOCK = (67384064 + 712192) / 262144
 
 # FP32 operations of one ordering of icbc's cluster fits (src/nvtt/icbc.h:2501-2540 and 2200-2240 in
 # the scalar build), each multiply/add/min/max/round/reciprocal counted once: cluster_fit_four w3 1,
