@@ -331,15 +331,30 @@ __device__ int compute_sat_inplace(const Lane<float4> &col, int n, const f3 *fra
     return n;
 }
 
+// round_ept on a packed endpoint: the same operations per channel (saturating scale, k x + 0.5,
+// truncation, 1 / k), the additions and the final scale packed for x and y.
+__device__ __forceinline__ P3 round_eptp(P3 n, float f) {
+    float nx, ny;
+    f2_unpack(n.xy, nx, ny);
+    const float x = mul_sat(nx, f), y = mul_sat(ny, f), z = mul_sat(n.z, f);
+    float gx, gy;
+    f2_unpack(f2_add(f2_pack(x * 31.0f, y * 63.0f), f2_pack(0.5f, 0.5f)), gx, gy);
+    return P3{f2_mul(f2_pack((float)(int)gx, (float)(int)gy), f2_pack(1.0f / 31.0f, 1.0f / 63.0f)), round5(z)};
+}
+
 // Shared solve / snap / residual of cluster_fit_three and cluster_fit_four
-// (src/nvtt/icbc.h:2200-2240, 2501-2540).
-__device__ __forceinline__ float cf_eval(f3 ax, f3 sum, float a2, float b2, float ab, f3 metric, f3 &pa, f3 &pb) {
+// (src/nvtt/icbc.h:2200-2240, 2501-2540): bx = sum - ax, a = snap((ax b2 - bx ab) factor),
+// b = snap((bx a2 - ax ab) factor), e2 = 2 (a (b ab - ax) - b bx), e1 = (a a) a2 + ((b b) b2 + e2),
+// with x and y packed where that is exact (sums, differences, products that feed no sum).
+__device__ __forceinline__ float cf_eval(P3 axq, P3 sum, float a2, float b2, float ab, f3 metric, f3 &pa, f3 &pb) {
     float factor = 1.0f / (a2 * b2 - ab * ab);
-    f3 bx = sum - ax;
-    const f3 a = round_ept((ax * b2) - (bx * ab), factor);
-    const f3 b = round_ept((bx * a2) - (ax * ab), factor);
-    f3 e2 = ((a * ((b * ab) - ax)) - (b * bx)) * 2.0f;
-    f3 e1 = ((a * a) * a2) + (((b * b) * b2) + e2);
+    const P3 bxq = p3_sub(sum, axq);
+    const f3 ax = u3(axq), bx = u3(bxq);
+    const P3 aq = round_eptp(p3_sub(p3(ax * b2), p3(bx * ab)), factor);
+    const P3 bq = round_eptp(p3_sub(p3(bx * a2), p3(ax * ab)), factor);
+    const f3 a = u3(aq), b = u3(bq);
+    const f3 e2 = u3(p3_sub(p3(a * u3(p3_sub(p3(b * ab), axq))), p3(b * bx))) * 2.0f;
+    const f3 e1 = u3(p3_add(p3(u3(p3_mul(aq, aq)) * a2), p3_add(p3(u3(p3_mul(bq, bq)) * b2), p3(e2))));
     pa = a; pb = b;
     return dot(e1, metric);
 }
@@ -353,14 +368,15 @@ __device__ __forceinline__ float four_eval_v(float4 v0, float4 v1, float4 v2, f3
                                              f3 &b) {
     float w0 = v0.w, w1 = v1.w, w2 = v2.w;
     const float w3 = wsum - w2;
-    const f3 x0 = xyz(v0), x1 = xyz(v1) - x0, x2 = xyz(v2) - xyz(v1);
+    const P3 x0 = p3(xyz(v0)), x1 = p3_sub(p3(xyz(v1)), x0), x2 = p3_sub(p3(xyz(v2)), p3(xyz(v1)));
     w2 = w2 - w1;
     w1 = w1 - w0;
     const float a2 = w2 * (1.0f / 9.0f) + (w1 * (4.0f / 9.0f) + w0);
     const float b2 = w1 * (1.0f / 9.0f) + (w2 * (4.0f / 9.0f) + w3);
     const float ab = (w1 + w2) * (2.0f / 9.0f);
-    const f3 ax = (x2 * (1.0f / 3.0f)) + ((x1 * (2.0f / 3.0f)) + x0);
-    return cf_eval(ax, sum, a2, b2, ab, metric, a, b);
+    // ax = x2 / 3 + (2 x1 / 3 + x0)
+    const P3 ax = p3_add(p3(u3(x2) * (1.0f / 3.0f)), p3_add(p3(u3(x1) * (2.0f / 3.0f)), x0));
+    return cf_eval(ax, p3(sum), a2, b2, ab, metric, a, b);
 }
 
 template <bool ZERO = false>
@@ -430,13 +446,13 @@ __device__ uint32_t best_order_four(const Lane<float4> &sat, int n, f3 metric) {
 __device__ __forceinline__ float three_eval_v(float4 v0, float4 v1, f3 sum, float wsum, f3 metric, f3 &a, f3 &b) {
     float w0 = v0.w, w1 = v1.w;
     const float w2 = wsum - w1;
-    const f3 x0 = xyz(v0), x1 = xyz(v1) - x0;
+    const P3 x0 = p3(xyz(v0)), x1 = p3_sub(p3(xyz(v1)), x0);
     w1 = w1 - w0;
     const float ab = w1 * 0.25f;
     const float a2 = w0 + ab;
     const float b2 = w2 + ab;
-    const f3 ax = x0 + (x1 * 0.5f);
-    return cf_eval(ax, sum, a2, b2, ab, metric, a, b);
+    const P3 ax = p3_add(x0, p3(u3(x1) * 0.5f));
+    return cf_eval(ax, p3(sum), a2, b2, ab, metric, a, b);
 }
 
 template <bool ZERO = false>

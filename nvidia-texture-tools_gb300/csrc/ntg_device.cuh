@@ -116,6 +116,35 @@ __device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
+__device__ __forceinline__ void f2_unpack(f32x2 p, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(p));
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// A packed multiply, for products that feed no addition or subtraction (only multiplies, floors,
+// comparisons): there is nothing for it to be contracted with.
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// An f3 as a packed (x, y) pair and a scalar z. Sums and differences run x and y in one instruction;
+// so do products that feed no sum (p3_mul); products that feed a sum are scalar multiplies, packed
+// afterwards (p3 of an f3 product). Each component is rounded exactly as the f3 operations round it.
+struct P3 { f32x2 xy; float z; };
+__device__ __forceinline__ P3 p3(f3 v) { return P3{f2_pack(v.x, v.y), v.z}; }
+__device__ __forceinline__ f3 u3(P3 p) {
+    float x, y;
+    f2_unpack(p.xy, x, y);
+    return f3{x, y, p.z};
+}
+__device__ __forceinline__ P3 p3_add(P3 a, P3 b) { return P3{f2_add(a.xy, b.xy), a.z + b.z}; }
+__device__ __forceinline__ P3 p3_sub(P3 a, P3 b) { return P3{f2_sub(a.xy, b.xy), a.z - b.z}; }
+__device__ __forceinline__ P3 p3_mul(P3 a, P3 b) { return P3{f2_mul(a.xy, b.xy), a.z * b.z}; }
+
 // A float4 as two pairs (x, y) and (z, w), and back: the same 16 bytes.
 struct F4x2 { f32x2 xy, zw; };
 __device__ __forceinline__ float4 f4_of(const F4x2 &p) {
