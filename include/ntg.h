@@ -106,6 +106,17 @@ int ntg_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, 
 int ntg_mip_level(ntg_context *ctx, const float *d_src, int w, int h, float *d_dst, int filter, float width,
                   const float *params, int wrap, int alpha_mode, int weighted, void *stream);
 
+/* Bounded waits of the mip filter: the TMA-staged FP32 2:1 tile kernel waits on an mbarrier for each
+ * tile's source window, at most `polls` polls per wait on the context's device (negative: the
+ * default, 4,194,304); 0 makes every wait give up at once, with no fault. A kernel whose wait gave
+ * up records it (ntg_mip_status), waits with the default limit for the copy in flight and returns
+ * without writing its remaining tiles, so later calls run normally. Synchronises the device. No
+ * counterpart in the reference. */
+int ntg_mip_set_wait_limit(ntg_context *ctx, int polls);
+/* *gave_up = 1 when a mip wait gave up since the previous call, else 0; clears the record.
+ * Synchronises the device. */
+int ntg_mip_status(ntg_context *ctx, int *gave_up);
+
 /* CompressorInterface::compress (src/nvtt/Compressor.h:34-38) for one planar FP32 level, as
  * CompressorDXT1 / CompressorDXT5 / FastCompressorBC5 etc. encode it (chooseCpuCompressor,
  * src/nvtt/Context.cpp:1038-1163). out_xform / gamma apply the output transform to RGB first

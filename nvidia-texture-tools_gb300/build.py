@@ -27,7 +27,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["ntg_bc1.cu", "ntg_bc3.cu", "ntg_mip.cu", "ntg_decode.cu", "ntg_noalloc.cu", "ntg_mlp.cu"]
 CPP_SOURCES = ["ntg_api.cpp", "ntg_host_tables.cpp", "nvtt_api.cpp", "nvtt_wrapper.cpp"]
-HEADERS = ["ntg_device.cuh", "ntg_internal.h", "ntg_host_tables.h"]
+HEADERS = ["ntg_device.cuh", "ntg_async.cuh", "ntg_internal.h", "ntg_host_tables.h"]
 
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

@@ -377,6 +377,15 @@ int plan_step(ntg_context *ctx, const ntg_chain_options &o, float width, const f
         key.taps.insert(key.taps.end(), ay->row0.begin(), ay->row0.end());
         return NTG_OK;
     }
+    if (!u8 && !weighted && ax->half && ay->half && ax->ws == ay->ws && poly2x_supported(ax->ws) &&
+        ((ax->left0 % 4) + 4) % 4 == tile_f32_phase(ax->ws)) {
+        J.cx = ax->left0; J.cy = ay->left0;
+        J.tiles_x = (D.w + tile_f32_w() - 1) / tile_f32_w();
+        J.strip = tile_f32_h();
+        key = {MIP_TILE_F32, ax->ws, 0, 0, nullptr, steps, ax->row0};
+        key.taps.insert(key.taps.end(), ay->row0.begin(), ay->row0.end());
+        return NTG_OK;
+    }
     if (ax->half && ay->half && ax->ws == ay->ws && poly2x_supported(ax->ws)) {
         J.cx = ax->left0; J.cy = ay->left0;
         J.tiles_x = (D.w + 31) / 32;
@@ -395,24 +404,99 @@ int plan_step(ntg_context *ctx, const ntg_chain_options &o, float width, const f
 
 long long mip_units(const MipKey &k, const MipJob &J) {
     if (k.kernel == MIP_FAST_BOX) return (long long)J.w * J.h;
-    if (k.kernel == MIP_POLY2X || k.kernel == MIP_TILE_U8) return (long long)J.tiles_x * ((J.h + J.strip - 1) / J.strip);
+    if (k.kernel == MIP_POLY2X || k.kernel == MIP_TILE_U8 || k.kernel == MIP_TILE_F32)
+        return (long long)J.tiles_x * ((J.h + J.strip - 1) / J.strip);
     return (long long)J.tiles_x * ((J.h + poly_tile_h() - 1) / poly_tile_h());
 }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against the driver
+// library); null when the driver does not provide it.
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (EncodeTiledFn) nullptr;
+        }
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// The tensor map of an FP32 tile job's source level, its four planes as a W x H x 4 tensor whose box
+// is one tile's source window. Left unset (tma = 0: the kernel copies with its threads) when the
+// level's base or rows are not 16-byte aligned, the box is too large for the TMA, or the driver
+// cannot encode it.
+void encode_tile_map(MipJob &J, int ws) {
+    J.tma = 0;
+    const EncodeTiledFn enc = encode_tiled();
+    const cuuint64_t row = (cuuint64_t)J.W * 4;
+    const int bw = tile_box_cols(ws), bh = tile_box_rows(ws, J.strip);
+    if (!enc || !J.src || ((uintptr_t)J.src & 15) || (row & 15) || bw > 256 || bh > 256 || J.W < 1 || J.H < 1) return;
+    const cuuint64_t dims[3] = {(cuuint64_t)J.W, (cuuint64_t)J.H, 4};
+    const cuuint64_t strides[2] = {row, row * (cuuint64_t)J.H};
+    const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 4};
+    const cuuint32_t unit[3] = {1, 1, 1};
+    const CUresult r = enc(&J.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(J.src), dims, strides, box, unit,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    J.tma = r == CUDA_SUCCESS ? 1 : 0;
+}
+
+// Where the TMA-staged FP32 tile kernel is used. Measured on GB300 against the one-tile-per-CTA
+// kernel (k_tile2x) on Kaiser 2:1 steps: 15% faster from a 4096 x 4096 source (54 tiles per SM),
+// even from 2048 x 2048 (13.5 tiles per SM), slower below: a persistent CTA with few tiles exposes
+// the box latency, and windows at the level's edges (a third of the tiles of a 512 x 512 source)
+// cost extra. So it takes a job from a source of at least kTmaMinSide texels in each direction,
+// and only when such jobs give a launch at least kTmaMinTilesPerSm tiles per SM; every other FP32
+// 2:1 job runs on k_tile2x.
+constexpr int kTmaMinSide = 2048;
+constexpr long long kTmaMinTilesPerSm = 16;
 
 // Groups the jobs of one chain depth by kernel variant into launches; appends the jobs to `all`.
 void group_launches(const std::vector<std::pair<MipKey, MipJob>> &items, const MipTuning &tune, std::vector<MipJob> &all,
                     std::vector<MipLaunch> &out) {
     std::map<MipKey, std::vector<MipJob>> groups;
     for (const auto &it : items) groups[it.first].push_back(it.second);
+    // FP32 2:1 jobs the TMA tile kernel does not take go to k_tile2x (same tile width and job fields)
+    for (auto it = groups.begin(); it != groups.end(); ++it) {
+        if (it->first.kernel != MIP_TILE_F32) continue;
+        std::vector<MipJob> big, small;
+        long long tiles = 0;
+        for (const MipJob &J : it->second) {
+            if (std::min(J.W, J.H) >= kTmaMinSide) {
+                big.push_back(J);
+                tiles += (long long)J.tiles_x * ((J.h + tile_f32_h() - 1) / tile_f32_h());
+            } else {
+                small.push_back(J);
+            }
+        }
+        if (tiles < kTmaMinTilesPerSm * 152) {
+            small.insert(small.end(), big.begin(), big.end());
+            big.clear();
+        }
+        if (!small.empty()) {
+            MipKey k{MIP_POLY2X, it->first.ws, 0, 0};
+            std::vector<MipJob> &dst = groups[k];
+            dst.insert(dst.end(), small.begin(), small.end());
+        }
+        it->second.swap(big);
+    }
     for (auto &g : groups) {
+        if (g.second.empty()) continue;
         MipLaunch m;
         std::memset(&m, 0, sizeof m);
         m.kernel = g.first.kernel; m.ws = g.first.ws; m.weighted = g.first.weighted; m.u8 = g.first.u8;
         m.first_job = (int)all.size();
         m.njobs = (int)g.second.size();
         m.threads = tune.threads;
-        int tile_h = std::min(32, std::max(4, tune.strip));
-        if (m.kernel == MIP_POLY2X) {
+        int tile_h = std::min(m.kernel == MIP_TILE_F32 ? tile_f32_h() : 32, std::max(4, tune.strip));
+        if (m.kernel == MIP_POLY2X || m.kernel == MIP_TILE_F32) {
             // lower tiles for small levels, so that the launch still spreads over the SMs
             for (;;) {
                 long long n = 0;
@@ -427,13 +511,14 @@ void group_launches(const std::vector<std::pair<MipKey, MipJob>> &items, const M
         for (MipJob J : g.second) {
             J.first_unit = units;
             units += mip_units(g.first, J);
+            if (m.kernel == MIP_TILE_F32) encode_tile_map(J, m.ws);
             rx = std::max(rx, J.rx_max);
             ry = std::max(ry, J.ry_max);
             all.push_back(J);
         }
         m.units = units;
         m.smem = m.kernel == MIP_POLY ? poly_smem_bytes(rx, ry) : m.kernel == MIP_POLY2X ? poly2x_smem_bytes(m.ws, tile_h) : 0;
-        if (m.kernel == MIP_TILE_U8) m.threads = 1024;  // shared memory sized inside the launcher
+        if (m.kernel == MIP_TILE_U8 || m.kernel == MIP_TILE_F32) m.threads = 1024;  // shared memory sized inside the launcher
         out.push_back(m);
     }
 }
@@ -719,6 +804,28 @@ int ntg_resize(ntg_context *ctx, const float *d_src, int w, int h, float *d_dst,
     NTG_TRY(ctx->workspace((size_t)dw * h * 4 * sizeof(float), s, &tmp));
     return launched(launch_resize(d_src, w, h, (float *)tmp, dw, dh, ax->d_w, ax->d_left, ax->ws, ay->d_w, ay->d_left,
                                   ay->ws, wrap, d_dst, s), "resize");
+}
+
+int ntg_mip_set_wait_limit(ntg_context *ctx, int polls) {
+    g_error.clear();
+    if (!ctx) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    NTG_CUDA(cudaDeviceSynchronize());
+    const int st = set_mip_wait_polls(polls < 0 ? 1 << 22 : polls);
+    if (st) return cuda_fail((cudaError_t)(st - kLaunchErrorBase), "mip wait limit");
+    NTG_CUDA(cudaDeviceSynchronize());
+    return NTG_OK;
+}
+
+int ntg_mip_status(ntg_context *ctx, int *gave_up) {
+    g_error.clear();
+    if (!ctx || !gave_up) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    NTG_TRY(ensure_device(ctx));
+    NTG_CUDA(cudaDeviceSynchronize());
+    const int st = read_mip_status(gave_up);
+    return st ? cuda_fail((cudaError_t)(st - kLaunchErrorBase), "mip status") : NTG_OK;
 }
 
 int ntg_selftest_srgb_quantizer(ntg_context *ctx, unsigned long long *mismatches) {

@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <cuda.h>  // CUtensorMap (maps are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 namespace ntg {
@@ -101,9 +102,12 @@ struct MipJob {
     int strip;               // 2:1 kernel: output rows per tile
     int rx_max, ry_max;      // general kernel: widest source window of a tile (host side, for shared memory)
     long long first_unit;    // running unit count of the launch (tail launches: the chain's index)
+    int tma;                 // TMA-staged FP32 tile kernel: `map` describes the source level
+    CUtensorMap map;         // the source level's FP32 planes as a 3-D (x, y, plane) tensor map whose box is
+                             // a tile's source window (64-byte aligned, as the TMA requires)
 };
 
-enum MipKernel { MIP_FAST_BOX = 0, MIP_POLY = 1, MIP_POLY2X = 2, MIP_TAIL = 3, MIP_TILE_U8 = 4 };
+enum MipKernel { MIP_FAST_BOX = 0, MIP_POLY = 1, MIP_POLY2X = 2, MIP_TAIL = 3, MIP_TILE_U8 = 4, MIP_TILE_F32 = 5 };
 
 // One launch over jobs [first_job, first_job + njobs) of a device job array.
 struct MipLaunch {
@@ -126,6 +130,18 @@ bool poly2x_supported(int ws);
 int tile_u8_phase(int ws);
 int tile_u8_w();
 int tile_u8_h();
+// 2:1 steps between FP32 levels without alpha weighting (persistent, TMA-staged 32 x strip tiles,
+// strip at most tile_f32_h()): the same window phase rule and the tile width / tallest tile.
+int tile_f32_phase(int ws);
+int tile_f32_w();
+int tile_f32_h();
+// The TMA box of the FP32 tile kernel's source window: columns, and rows for a tile of `strip` output rows.
+int tile_box_cols(int ws);
+int tile_box_rows(int ws, int strip);
+// Poll limit of the FP32 tile kernel's mbarrier waits on the current device, and the status word a
+// wait that ran out sets (read and cleared by read_mip_status).
+int set_mip_wait_polls(int polls);
+int read_mip_status(int *status);
 size_t poly_smem_bytes(int rx_max, int ry_max);
 size_t poly2x_smem_bytes(int ws, int tile_h);  // dynamic shared memory of a 2:1 tile launch
 int poly_tile_w();

@@ -10,10 +10,18 @@
 // sequential tap-order sum the reference computes, so levels are bit-identical to the CPU path.
 #include <algorithm>
 
+#include "ntg_async.cuh"
 #include "ntg_device.cuh"
 #include "ntg_internal.h"
 
 namespace ntg {
+
+// Polls of each mbarrier wait of the TMA-staged tile kernels before it gives up, and the word such a
+// wait sets (1) before its kernel drains its copy in flight and returns.
+constexpr int kMipWaitPolls = 1 << 22;
+__device__ int g_mip_wait_polls = kMipWaitPolls;
+__device__ unsigned int g_mip_status = 0;
+
 
 // ---------------------------------------------------------------------------------------------
 // Surface::setImage(InputFormat_BGRA_8UB) (src/nvtt/Surface.cpp:728-760) fused with the input
@@ -224,6 +232,24 @@ __device__ __forceinline__ int wrap_index(int x, int w, int wm) {
     while (x >= w) x = abs(w + w - x - 2);
     return x;
 }
+
+// Windows at the level's edges. A TMA box reads 0 where it reaches past the level; with the clamp
+// and mirror wraps the texel that belongs there (the wrapped position) usually lies inside the same
+// box, so the threads that read such a position read the wrapped one instead (a column or row index
+// remap inside shared memory: no extra copy from global memory, no extra barrier). box_remap(x) is
+// that index for position x of a box starting at b0; in_box checks, per tile, that the needed
+// positions lo..hi (of a level of n) map into the box [b0, b0 + bn) with at most one reflection.
+// Tiles where they do not (the repeat wrap, levels narrower than a window) are copied by the
+// threads with the wrap applied.
+__device__ __forceinline__ bool in_box(int lo, int hi, int b0, int bn, int n, int wrap) {
+    if (lo >= 0 && hi < n) return true;
+    if (wrap == 1) return false;
+    if (wrap == 0) return true;  // clamp: 0 and n - 1 lie in the box whenever lo < 0 or hi >= n
+    if (lo < 0 && (-lo >= n || -lo >= b0 + bn)) return false;
+    if (hi >= n && (hi >= 2 * n - 1 || 2 * n - 2 - hi < b0)) return false;
+    return true;
+}
+__device__ __forceinline__ int box_remap(int x, int b0, int n, int wrap) { return wrap_index(b0 + x, n, wrap) - b0; }
 
 template <bool SRC_U8>
 __device__ __forceinline__ float4 load_texel(const MipJob &L, size_t s, size_t sn) {
@@ -702,6 +728,266 @@ __global__ void __launch_bounds__(1024, 1) k_tile2x_u8(const MipJob *__restrict_
     }
 }
 
+// The thread that issues the FP32 tile kernel's TMA loads: lane 0 of the last warp, which has no
+// filter item. It acquires a job's tensor map once, before its first load through it (`fenced`).
+__device__ __forceinline__ bool tma_issuer() { return threadIdx.x == blockDim.x - 32; }
+
+__device__ __forceinline__ void tma_tile(const MipJob &L, const MipJob *&fenced, void *dst, uint32_t bytes, int x, int y,
+                                         uint64_t *bar) {
+    if (fenced != &L) {
+        tensormap_acquire(&L.map);
+        fenced = &L;
+    }
+    mbar_expect_tx(bar, bytes);
+    tma_load_3d(dst, &L.map, x, y, 0, bar);
+}
+
+// 2:1 steps between FP32 levels (level 2 on), unweighted: persistent like k_tile2x_u8, one
+// 1024-thread CTA per SM walking 32 x TH output tiles (TH = the job's strip, at most 16) with one
+// barrier per tile, the X taps of tile i beside the Y taps of tile i - 1. A tile's source window, four
+// planes of ROWS x NC floats, is one TMA box of the level's 3-D tensor map (x, y, plane), loaded into
+// one of NBUF buffers while the tiles before it are filtered (a third buffer, for two boxes in flight,
+// measured slower: its shared memory and the extra state cost more than the hidden latency gave).
+// Positions of an edge box outside the level read 0; the half-warp that filters a row first fills them
+// from their wrapped positions in the same box (box_remap). Windows that cannot be remapped, and
+// levels without a tensor map, are copied by the threads (cp.async) with the wrap applied, into the
+// same layout. The X pass reads the planes directly: a half-warp per source row, each lane two
+// adjacent outputs from NV consecutive float4 of each plane (conflict-free). Sums start at 0 and take their taps in window order as in
+// applyKernelX/Y (src/nvimage/FloatImage.cpp:1115-1176), so the levels equal k_tile2x's.
+template <int WS>
+struct TileF32 {
+    static constexpr int TW = 32, TH = 16, WARPS = 32;
+    static constexpr int D = WS == 3 ? 0 : 3;                    // window start of output column 0, mod 4
+    static constexpr int RW = 2 * (TW - 1) + WS;                 // source columns of a tile
+    static constexpr int NC = (D + RW + 3) / 4 * 4;              // staged columns, from a multiple of 4
+    static constexpr int NV = (D + WS + 1) / 4 + 1;              // float4 per plane under a lane's two outputs
+    static_assert(4 * (TW / 2 - 1) + 4 * NV <= NC, "X reads stay inside the staged row");
+    static constexpr int ROWS = 2 * (TH - 1) + WS;               // source rows of the tallest tile
+    static constexpr int RAW = (4 * ROWS * NC + 31) / 32 * 32;   // floats per window buffer (128-byte multiple)
+    static constexpr int NBUF = 2;                               // window buffers
+    static constexpr int XPLANE = ROWS * TW;                     // float4
+    static constexpr size_t smem() { return 128 + (size_t)NBUF * RAW * 4 + (size_t)2 * XPLANE * 16; }
+    static __host__ __device__ constexpr int rows(int th) { return 2 * (th - 1) + WS; }
+};
+
+struct TileF32Pos {
+    const MipJob *L;
+    int x0, y0;    // first output column / row
+    int a0, r0;    // first staged source column (a multiple of 4) / row, before wrapping
+    int th, rows;  // output rows of the tile (its job's strip) and source rows of its window
+    bool tma;      // one TMA box (the job has a tensor map, and the edges can be remapped)
+    bool remap;    // tma, and the box reaches past the level's edges: edge rows fixed in place
+};
+
+template <int WS>
+__device__ __forceinline__ TileF32Pos tile_f32_pos(const MipJob *__restrict__ jobs, int njobs, long long u) {
+    using P = TileF32<WS>;
+    const MipJob &L = jobs[find_mip_job(jobs, njobs, u)];
+    const unsigned lu = (unsigned)(u - L.first_unit), tx = (unsigned)L.tiles_x;  // 32-bit division
+    TileF32Pos p;
+    p.L = &L;
+    p.th = L.strip;
+    p.rows = P::rows(p.th);
+    p.x0 = (int)(lu % tx) * P::TW;
+    p.y0 = (int)(lu / tx) * p.th;
+    p.a0 = 2 * p.x0 + L.cx - P::D;
+    p.r0 = 2 * p.y0 + L.cy;
+    const bool edge = p.a0 < 0 || p.a0 + P::NC > L.W || p.r0 < 0 || p.r0 + p.rows > L.H;
+    p.tma = L.tma && (!edge || (in_box(p.a0 + P::D, p.a0 + P::D + P::RW - 1, p.a0, P::NC, L.W, L.wrap) &&
+                                in_box(p.r0, p.r0 + p.rows - 1, p.r0, p.rows, L.H, L.wrap)));
+    p.remap = p.tma && edge;
+    return p;
+}
+
+// Issues the copies of a tile's source window into `raw` (plane c, row r at (c rows + r) NC).
+template <int WS>
+__device__ __forceinline__ void tile_f32_fetch(const TileF32Pos &p, float *raw, uint64_t *bar, const MipJob *&fenced) {
+    using P = TileF32<WS>;
+    const MipJob &L = *p.L;
+    if (p.tma) {
+        if (tma_issuer()) tma_tile(L, fenced, raw, (uint32_t)(4 * p.rows * P::NC * 4), p.a0, p.r0, bar);
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t sn = (size_t)L.W * L.H;
+    for (int row = warp; row < 4 * p.rows; row += P::WARPS) {
+        const int c = row / p.rows, r = row - c * p.rows;
+        const float *srow = L.src + c * sn + (size_t)wrap_index(p.r0 + r, L.H, L.wrap) * L.W;
+        float *drow = raw + (size_t)row * P::NC;
+        for (int k = lane; k < P::NC; k += 32) cp_async4(drow + k, srow + wrap_index(p.a0 + k, L.W, L.wrap));
+    }
+    cp_async_commit();
+}
+
+template <int WS>
+__global__ void __launch_bounds__(1024, 1) k_tile2x_f32(const MipJob *__restrict__ jobs, int njobs, long long units) {
+    using P = TileF32<WS>;
+    constexpr int TW = P::TW, D = P::D, NC = P::NC, NV = P::NV;
+    extern __shared__ float4 sm4[];
+    __shared__ float s_steps[256];
+    __shared__ uint8_t s_buckets[kSrgbBuckets];
+    __shared__ float s_ky[WS];
+    __shared__ uint64_t s_bar[TileF32<WS>::NBUF];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    float *const raw0 = reinterpret_cast<float *>(sm4 + ((128 - (smem_u32(sm4) & 127)) & 127) / 16);  // NBUF x RAW
+    float4 *const xplane0 = reinterpret_cast<float4 *>(raw0 + P::NBUF * P::RAW);                     // 2 x XPLANE
+    constexpr int NB = P::NBUF;
+    const long long g = gridDim.x;
+    if (blockDim.x != 32 * P::WARPS || (long long)blockIdx.x >= units) return;
+    const int polls = g_mip_wait_polls;
+    if (tid == 0) {
+        for (int k = 0; k < NB; k++) mbar_init(&s_bar[k], 1);
+        fence_barrier_init();
+    }
+
+    // quantiser tables and taps, shared by every job of the launch
+    const MipJob &J0 = jobs[0];
+    if (tid < WS) s_ky[tid] = __ldg(J0.ky + tid);
+    if (J0.steps) {
+        for (int i = tid; i < 256; i += blockDim.x) s_steps[i] = __ldg(J0.steps + i);
+        const uint32_t *b = reinterpret_cast<const uint32_t *>(J0.steps + 256);
+        for (int i = tid; i < kSrgbBuckets / 4; i += blockDim.x) reinterpret_cast<uint32_t *>(s_buckets)[i] = __ldg(b + i);
+    }
+    float kx[WS];
+#pragma unroll
+    for (int j = 0; j < WS; j++) kx[j] = __ldg(J0.kx + j);
+    __syncthreads();  // barriers initialised before any thread waits on them
+
+    // iteration i X-filters tile blockIdx + i g (t0, window in buffer i % NB) and Y-filters tile
+    // blockIdx + (i - 1) g (prev); the boxes of the next AHEAD tiles (t1, t2) are in flight meanwhile.
+    // Buffer k's barrier completes once per box loaded into it (phase bit k of ph).
+    constexpr int AHEAD = NB - 1;
+    const long long n = (units - blockIdx.x + g - 1) / g;
+    TileF32Pos t0 = tile_f32_pos<WS>(jobs, njobs, blockIdx.x), t1 = t0, prev = t0;
+    const MipJob *fenced = nullptr;
+    uint32_t ph = 0;
+    auto fetch = [&](const TileF32Pos &t, int k) { tile_f32_fetch<WS>(t, raw0 + k * P::RAW, &s_bar[k], fenced); };
+    fetch(t0, 0);
+    if (AHEAD > 1 && n > 1) {
+        t1 = tile_f32_pos<WS>(jobs, njobs, blockIdx.x + g);
+        fetch(t1, 1);
+    }
+    for (long long i = 0; i <= n; i++) {
+        const int b = (int)(i % NB), bx = (int)(i & 1);
+        bool ok = true;
+        if (i < n) {
+            cp_async_wait<0>();
+            if (t0.tma) {
+                // one thread polls the barrier; the others wait at the CTA barrier below, which
+                // makes the box visible to them and keeps them off the issue slots meanwhile
+                if (tma_issuer()) ok = mbar_wait(&s_bar[b], (ph >> b) & 1, polls);
+                ph ^= 1u << b;
+            }
+        }
+        if (!__syncthreads_and(ok)) {
+            // a wait ran out: record it, let the boxes in flight (tile i, and i + 1 with two ahead)
+            // land, and leave
+            if (tma_issuer()) {
+                atomicOr(&g_mip_status, 1u);
+                mbar_wait(&s_bar[b], ((ph >> b) & 1) ^ 1, kMipWaitPolls);
+                const int b1 = (int)((i + 1) % NB);
+                if (AHEAD > 1 && i + 1 < n && t1.tma) mbar_wait(&s_bar[b1], (ph >> b1) & 1, kMipWaitPolls);
+            }
+            return;
+        }
+        TileF32Pos t2 = t1;
+        if (i + AHEAD < n) {
+            t2 = tile_f32_pos<WS>(jobs, njobs, blockIdx.x + (i + AHEAD) * g);
+            fetch(t2, (int)((i + AHEAD) % NB));
+        }
+        const TileF32Pos &cur = t0;
+        const float *const raw = raw0 + b * P::RAW;
+        float4 *const xp = xplane0 + bx * P::XPLANE;
+        const float4 *const yp = xplane0 + (1 - bx) * P::XPLANE;
+        const int nx = i < n ? (cur.rows + 1) / 2 : 0, ny = i > 0 ? prev.th / 2 : 0;
+        for (int item = warp; item < nx + ny; item += P::WARPS) {
+            if (item < nx) {
+                // X taps of source rows 2 item (lanes 0-15) and 2 item + 1 (lanes 16-31): lane l -> output
+                // columns 2 l, 2 l + 1 = staged columns D + 4 l + t, t in [0, WS) and [2, WS + 2)
+                const int r = 2 * item + (lane >> 4), l = lane & 15;
+                if (cur.remap) {
+                    // an edge box: the half-warp fills its row's positions outside the level from
+                    // their wrapped positions (inside the level, so read-only for every lane)
+                    if (r < cur.rows) {
+                        const MipJob &L = *cur.L;
+                        const int rr = box_remap(r, cur.r0, L.H, L.wrap);
+                        const bool row_out = rr != r;
+#pragma unroll 1
+                        for (int c = 0; c < 4; c++) {
+                            float *row = const_cast<float *>(raw) + ((size_t)c * cur.rows + r) * NC;
+                            const float *from = raw + ((size_t)c * cur.rows + rr) * NC;
+                            for (int k = l; k < NC; k += 16) {
+                                const int sx = cur.a0 + k;
+                                if (row_out || sx < 0 || sx >= L.W) {
+                                    const int kk = box_remap(k, cur.a0, L.W, L.wrap);
+                                    if (kk >= 0 && kk < NC) row[k] = from[kk];  // outside the box: feeds no output
+                                }
+                            }
+                        }
+                        fence_async_smem();  // a later TMA box overwrites this row
+                    }
+                    __syncwarp();
+                }
+                if (r < cur.rows) {
+                    float o0[4], o1[4];
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const float4 *src = reinterpret_cast<const float4 *>(raw + ((size_t)c * cur.rows + r) * NC) + l;
+                        float v[4 * NV];
+#pragma unroll
+                        for (int k = 0; k < NV; k++) {
+                            const float4 q = src[k];
+                            v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+                        }
+                        f32x2 sum = f2_pack(0.0f, 0.0f);
+#pragma unroll
+                        for (int t = 0; t < WS; t++) sum = f2_add(sum, f2_pack(kx[t] * v[D + t], kx[t] * v[D + 2 + t]));
+                        f2_unpack(sum, o0[c], o1[c]);
+                    }
+                    xp[r * TW + 2 * l] = make_float4(o0[0], o0[1], o0[2], o0[3]);
+                    xp[r * TW + 2 * l + 1] = make_float4(o1[0], o1[1], o1[2], o1[3]);
+                }
+            } else {
+                // Y taps of tile i - 1: output rows 2 q, 2 q + 1 of column `lane` read X rows 4 q + t,
+                // t in [0, WS) and [2, WS + 2)
+                const int q = item - nx;
+                const float4 *const col = yp + (4 * q) * TW + lane;
+                F4x2 p0{0, 0}, p1{0, 0};
+#pragma unroll
+                for (int t = 0; t < WS + 2; t++) {
+                    const float4 v = col[t * TW];
+                    if (t < WS) tap2(p0, s_ky[t], v);
+                    if (t >= 2) tap2(p1, s_ky[t - 2], v);
+                }
+                const MipJob &L = *prev.L;
+                const int w = L.w, h = L.h, gx = prev.x0 + lane, gy = prev.y0 + 2 * q;
+                if (gx >= w) continue;
+                const size_t dn = (size_t)w * h;
+                const bool srgb = L.q_out && L.xform == 2;
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    if (gy + e >= h) break;
+                    const float4 v = f4_of(e == 0 ? p0 : p1);
+                    const size_t o = (size_t)(gy + e) * w + gx;
+                    L.dst[o] = v.x;
+                    L.dst[dn + o] = v.y;
+                    L.dst[2 * dn + o] = v.z;
+                    L.dst[3 * dn + o] = v.w;
+                    if (L.q_out)
+                        L.q_out[o] = srgb ? quantize_srgb_bgra(v, s_steps, s_buckets) : quantize_bgra(v.x, v.y, v.z, v.w, L.xform, s_steps);
+                }
+            }
+        }
+        prev = t0;
+        if (AHEAD > 1) {
+            t0 = t1;
+            t1 = t2;
+        } else {
+            t0 = t2;
+        }
+    }
+}
+
 // Chain tails: once a texture's level is small (at most TAIL_MAX texels), one CTA finishes every
 // remaining level in shared memory, one level after the other, instead of one latency-bound
 // launch per tiny level. Levels are planar FP32 in shared memory; each polyphase step runs the
@@ -998,6 +1284,47 @@ static int launch_tile2x_u8_ws(const MipLaunch &m, const MipJob *jobs, cudaStrea
     return m.weighted ? launch_tile2x_u8_t<WS, true>(m, jobs, s) : launch_tile2x_u8_t<WS, false>(m, jobs, s);
 }
 
+template <int WS>
+static int launch_tile2x_f32_t(const MipLaunch &m, const MipJob *jobs, cudaStream_t s) {
+    static std::atomic<unsigned long long> configured{0};
+    static int sms = 0;
+    if (first_use_on_device(configured)) {
+        cudaFuncSetAttribute(k_tile2x_f32<WS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TileF32<WS>::smem());
+        int d = 0;
+        cudaGetDevice(&d);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+    }
+    const long long grid = std::min<long long>(m.units, sms > 0 ? sms : 152);
+    k_tile2x_f32<WS><<<(unsigned)grid, 1024, TileF32<WS>::smem(), s>>>(jobs, m.njobs, m.units);
+    return launch_status();
+}
+
+int tile_f32_phase(int ws) {
+    if (ws == 3) return TileF32<3>::D;
+    if (ws == 5) return TileF32<5>::D;
+    if (ws == 13) return TileF32<13>::D;
+    return -1;
+}
+int tile_f32_w() { return TileF32<13>::TW; }
+int tile_f32_h() { return TileF32<13>::TH; }
+
+int tile_box_cols(int ws) { return ws == 3 ? TileF32<3>::NC : ws == 5 ? TileF32<5>::NC : TileF32<13>::NC; }
+int tile_box_rows(int ws, int strip) { return 2 * (strip - 1) + ws; }
+
+int set_mip_wait_polls(int polls) {
+    if (cudaMemcpyToSymbol(g_mip_wait_polls, &polls, sizeof polls) != cudaSuccess) return launch_status();
+    return 0;
+}
+
+int read_mip_status(int *status) {
+    unsigned int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_mip_status, sizeof v) != cudaSuccess ||
+        cudaMemcpyToSymbol(g_mip_status, &zero, sizeof zero) != cudaSuccess)
+        return launch_status();
+    *status = (int)v;
+    return 0;
+}
+
 int tile_u8_phase(int ws) {
     if (ws == 3) return TileU8<3>::D;
     if (ws == 5) return TileU8<5>::D;
@@ -1099,6 +1426,11 @@ int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s) {
             if (m.ws == 3) return launch_tile2x_u8_ws<3>(m, jobs, s);
             if (m.ws == 5) return launch_tile2x_u8_ws<5>(m, jobs, s);
             if (m.ws == 13) return launch_tile2x_u8_ws<13>(m, jobs, s);
+            return 2;
+        case MIP_TILE_F32:
+            if (m.ws == 3) return launch_tile2x_f32_t<3>(m, jobs, s);
+            if (m.ws == 5) return launch_tile2x_f32_t<5>(m, jobs, s);
+            if (m.ws == 13) return launch_tile2x_f32_t<13>(m, jobs, s);
             return 2;
         case MIP_POLY2X:
             if (m.threads < 64 || m.threads > 512 || m.threads % 32 || m.smem > 200 * 1024) return 1;

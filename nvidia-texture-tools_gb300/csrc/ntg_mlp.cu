@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "ntg.h"
+#include "ntg_async.cuh"
 #include "ntg_internal.h"
 
 namespace ntg {
@@ -56,8 +57,6 @@ struct GemmArgs {
 
 // ---- PTX wrappers (tcgen05, mbarrier) ----
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
 // Shared-memory matrix descriptor: start address, leading (K) and stride (row-group) byte offsets,
 // the fixed 0b001 field at bits 46-48, no swizzle.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo = SBO) {
@@ -73,32 +72,10 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
 // Polls of a wait by default, and of the drain after a wait gave up: the MMAs already issued
 // still write the TMEM accumulator, so they must finish before it is freed.
 constexpr int kWaitPolls = 1 << 22;
 
-// Bounded wait for the completion of the phase with the given parity (`limit` polls; 0 gives up at once).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int limit) {
-    for (int i = 0; i < limit; i++)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 

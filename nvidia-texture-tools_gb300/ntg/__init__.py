@@ -90,6 +90,8 @@ def lib():
         "ntg_resize": (_i, [_vp, _vp, _i, _i, _vp, _i, _i, _i, _f, _vp, _i, _i, _vp]),
         "ntg_target_extent": (_i, [_i, _i, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
         "ntg_selftest_srgb_quantizer": (_i, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+        "ntg_mip_set_wait_limit": (_i, [_vp, _i]),
+        "ntg_mip_status": (_i, [_vp, ctypes.POINTER(ctypes.c_int)]),
         "ntg_encode": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
         "ntg_encode_noalloc": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _f, _vp, _vp, _vp]),
         "ntg_chain_levels": (_i, [_i, _i, _i]),
@@ -228,6 +230,16 @@ class Context:
         n = ctypes.c_ulonglong()
         _check(lib().ntg_selftest_srgb_quantizer(self.h, ctypes.byref(n)))
         return n.value
+
+    def set_mip_wait_limit(self, polls: int = -1):
+        """Polls of each mbarrier wait of the TMA-staged mip kernels before it gives up (-1: the default)."""
+        _check(lib().ntg_mip_set_wait_limit(self.h, polls))
+
+    def mip_status(self) -> int:
+        """1 when a mip wait gave up since the previous call (which clears the record), else 0."""
+        v = ctypes.c_int()
+        _check(lib().ntg_mip_status(self.h, ctypes.byref(v)))
+        return v.value
 
     def resize(self, src, w, h, dw, dh, filter=FILTER_BOX, width=0.0, params=(0.0, 0.0), wrap=WRAP_MIRROR,
                alpha_mode=ALPHA_NONE, out=None, stream=None):

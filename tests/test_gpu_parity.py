@@ -196,6 +196,66 @@ def test_weighted_mip_level_matches_oracle(ctx, oracle, filt):
         assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
 
 
+# 2:1 steps between FP32 levels: sources of at least 2048 x 2048 with enough tiles run on the
+# persistent TMA-staged tile kernel (one TMA box per window; boxes at the level's edges read through
+# remapped indices with the clamp and mirror wraps, and are copied by the threads with the repeat
+# wrap); the others on the one-tile-per-CTA kernel. Sizes give both kernels, partial tiles on the
+# right and bottom (4100 x 2050, 1000 x 600) and each tile height the planner picks (16, 8, 4 rows).
+@pytest.mark.parametrize("size", [(4096, 2048), (2048, 4096), (4100, 2050), (1024, 1024), (1000, 600), (192, 96)])
+@pytest.mark.parametrize("filt", [ntg.FILTER_TRIANGLE, ntg.FILTER_KAISER])
+def test_fp32_tile_mip_level_matches_oracle(ctx, oracle, size, filt):
+    w, h = size
+    width = 1.0 if filt == ntg.FILTER_TRIANGLE else 3.0
+    for wrap in (0, 1, 2):
+        img = float_image(w, h, w + 3 * h + wrap, lo=-0.1, hi=1.1)
+        ours = host(ctx.mip_level(dev(img), w, h, filter=filt, params=(4.0, 1.0), wrap=wrap))
+        ref = oracle.resize(img, w, h, w // 2, h // 2, filt, width, 4.0, 1.0, wrap)
+        assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32)), (size, filt, wrap)
+
+
+def test_mip_level_unaligned_source_matches_oracle(ctx, oracle):
+    """A source level 4 bytes past a 16-byte boundary gets no tensor map: the TMA tile kernel's
+    windows are all copied by the threads."""
+    w, h = 4096, 2048
+    img = float_image(w, h, 31)
+    buf = dev(np.concatenate([np.zeros(1, np.float32), img]))
+    ours = host(ctx.mip_level(buf[1:], w, h, filter=ntg.FILTER_KAISER, params=(4.0, 1.0), wrap=ntg.WRAP_MIRROR))
+    ref = oracle.resize(img, w, h, w // 2, h // 2, ntg.FILTER_KAISER, 3.0, 4.0, 1.0, ntg.WRAP_MIRROR)
+    assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+
+
+def test_mip_waits_run_out_without_a_fault(ctx):
+    """The TMA-staged FP32 tile kernel's mbarrier waits are bounded: with a limit of zero polls every
+    wait for a TMA box gives up at once, with nothing faulting; the kernel records it, lets the box land
+    and returns. With the default limit back, the same calls give the same levels and blocks as before
+    (the 4096 x 2048 FP32 step takes TMA boxes; the chain's steps run beside it, unaffected)."""
+    w = h = 1024
+    bgra = synth.colour_texture(w, h, 5, alpha=synth.alpha_field(w, h, 5))
+    fw, fh = 4096, 2048
+    img = float_image(fw, fh, 9)
+    opt = ntg.ChainOptions.make(format=ntg.FORMAT_BC3, quality=ntg.QUALITY_NORMAL, filter=ntg.FILTER_KAISER,
+                                wrap=ntg.WRAP_MIRROR, alpha_mode=ntg.ALPHA_TRANSPARENCY, in_xform=ntg.XFORM_SRGB,
+                                out_xform=ntg.XFORM_SRGB, max_levels=3)
+    d_bgra, d_img = dev(bgra), dev(img)
+
+    def run():
+        lv = host(ctx.mip_level(d_img, fw, fh, filter=ntg.FILTER_KAISER, params=(4.0, 1.0), wrap=ntg.WRAP_MIRROR))
+        return lv, host(ctx.mip_chain(d_bgra, w, h, opt)), host(ctx.compress_chain(d_bgra, w, h, opt))
+
+    before = run()
+    assert ctx.mip_status() == 0
+    ctx.set_mip_wait_limit(0)
+    try:
+        run()
+        assert ctx.mip_status() == 1
+    finally:
+        ctx.set_mip_wait_limit(-1)
+    after = run()
+    assert ctx.mip_status() == 0
+    for a, b in zip(before, after):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
 CHAINS = [
     # (w, h, format, quality, filter, alpha_mode, in_xform, out_xform, wrap)
     (128, 128, 1, 1, 0, 0, 0, 0, 2),    # the box/BC1/linear workload at reduced size
