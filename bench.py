@@ -78,6 +78,9 @@ BATCH_FRONTIER = [{1: (DESCENT | 4, INF)}, {1: (DESCENT | 8, 0.05)}, {1: (DESCEN
 # DRAM bytes per block of the BC1 fit: one ncu capture of k_bc1<7> over 262,144 blocks of a 2048x2048
 # planar FP32 level (67,384,064 B read + 712,192 B written, profiles/k_bc1_7_cases_2048.md), per block;
 # the batch's BC1 levels are planar FP32 too, so the traffic scales with the blocks
+# DRAM bytes (read + write) of the 4096 x 4096 chain's mip launches (k_tile2x_u8, 6 k_tile2x, k_mip_tail)
+# in one ncu capture of `bench.py --workload c1` (dram__bytes_read.sum + dram__bytes_write.sum).
+C1_MIP_TRAFFIC = 191867392
 BC1_TRAFFIC_PER_BLOCK = (67384064 + 712192) / 262144
 
 # FP32 operations of one ordering of icbc's cluster fits (src/nvtt/icbc.h:2501-2540 and 2200-2240 in
@@ -477,12 +480,14 @@ def measure_chain(ctx, name, args, world, rank, with_cpu):
         sm_mhz_m = clocks["sm_mhz"] or 2070.0
         fp32_peak = 152 * 128 * sm_mhz_m * 1e6
         roof_hbm = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
-                    "traffic": None, "kernel": "mip launches of the chain (k_tile2x_u8 / k_tile2x for the 2:1 steps, k_mip_tail for the "
-                                              "levels from 32x32 down)",
+                    "traffic": C1_MIP_TRAFFIC if name == "c1" else None,
+                    "kernel": "mip launches of the chain (k_tile2x_u8 / k_tile2x for the 2:1 steps, k_mip_tail for the "
+                              "levels from 32x32 down)",
                     "algorithmic_bytes": mip_bytes, "ms": mips_ms, "peak_source": peak_src,
                     "fp32_ops": mip_ops, "fp32_frac": mip_ops / (mips_ms / 1000.0) / fp32_peak,
                     "note": "the Kaiser filter is FP32-bound before it is HBM-bound: 312 FP32 instructions per output "
-                            "without FMA contraction"}
+                            "without FMA contraction; traffic: DRAM read + write of the chain's 8 mip launches in one ncu "
+                            "capture (below the algorithmic bytes: each level is read back from L2 by the next step)"}
         cpu = None
         if with_cpu:
             try:
@@ -776,7 +781,7 @@ def run_gpu_batch(args):
         mip_gbs = mip_bytes / (phases["mips"] / 1000.0) / 1e9
         dominant = max(("bc1", "bc3", "bc5", "mips"), key=lambda k: phases[k])
         roof_mips = {"bound": "hbm", "achieved": mip_gbs, "peak": hbm, "unit": "GB/s", "frac": mip_gbs / hbm,
-                     "traffic": None, "kernel": "mip launches of the batch (k_tile2x_u8, k_tile2x, k_poly, k_mip_tail, k_fast_down)",
+                     "traffic": None, "kernel": "mip launches of the batch (k_tile2x_u8, k_tile2x_f32, k_tile2x, k_poly, k_mip_tail, k_fast_down)",
                      "algorithmic_bytes": mip_bytes, "ms": phases["mips"], "peak_source": peak_src}
         roof = None
         if dominant == "bc1" and phases["bc1"] > 0:

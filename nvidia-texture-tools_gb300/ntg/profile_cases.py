@@ -9,6 +9,7 @@ default) and hold a few GB of device memory at most. The learned cases use an un
 no fallback (the pruned search's cost does not depend on the proposal's quality). Kernels per case:
 
   mips_kaiser_srgb   k_tile2x_u8, k_tile2x, k_mip_tail           (Kaiser, sRGB in and out, BC3 levels)
+  mips_tma           k_tile2x_f32                                (one Kaiser 2:1 step from a 2N x N FP32 level)
   mips_odd           k_poly, k_mip_tail                          (odd sizes: the general scale kernel)
   mips_box           k_set_image, k_fast_down                    (box filter)
   bc1                k_bc1<7> (Normal)     bc1_fastest  k_bc1<0>     bc1_production  k_bc1<8>
@@ -30,7 +31,7 @@ from . import (ALPHA_NONE, ALPHA_TRANSPARENCY, BLOCK_BYTES, FILTER_BOX, FILTER_K
                QUALITY_PRODUCTION, XFORM_SRGB, ChainOptions, Context, chain_bytes, chain_levels, nblocks)
 from . import learned, synth
 
-CASES = ["mips_kaiser_srgb", "mips_odd", "mips_box", "bc1", "bc1_fastest", "bc1_production", "bc3", "bc1a", "bc4", "bc5",
+CASES = ["mips_kaiser_srgb", "mips_tma", "mips_odd", "mips_box", "bc1", "bc1_fastest", "bc1_production", "bc3", "bc1a", "bc4", "bc5",
          "decode_rms", "learned_bc1", "learned_bc3", "train"]
 ONCE = False
 
@@ -47,6 +48,15 @@ def _calls(fn):
 def run(case: str, size: int, ctx: Context):
     import torch
     dev = "cuda"
+    if case == "mips_tma":
+        # a source of 2N x N FP32 texels: large enough for the TMA-staged tile kernel
+        w, h = 2 * size, size
+        img = torch.from_numpy(synth.colour_texture(w, h, 9, scale=4.0)).to(dev)
+        src = torch.empty(4 * w * h, dtype=torch.float32, device=dev)
+        ctx.set_image(img, w, h, out=src)
+        out = torch.empty(4 * (w // 2) * (h // 2), dtype=torch.float32, device=dev)
+        _calls(lambda: ctx.mip_level(src, w, h, filter=FILTER_KAISER, params=(4.0, 1.0), out=out))
+        return
     if case.startswith("mips"):
         w, h = (size - 3, size - 5) if case == "mips_odd" else (size, size)
         img = synth.colour_texture(w, h, 7, scale=4.0, alpha=synth.alpha_field(w, h, 7, scale=4.0))
