@@ -142,8 +142,10 @@ int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_rgba, int w,
 
 /* Surface::toLinear(gamma) / toGamma(gamma) / toLinearFromSrgb / toSrgb (src/nvtt/Surface.cpp:1470-1592)
  * on RGB of a planar FP32 level, in place. kind: 0 toLinear, 1 toGamma, 2 toLinearFromSrgb, 3 toSrgb.
- * Gamma 2.2 is bit-exact (the reference's own table-and-quartic powf); the sRGB curves and other
- * gammas use the device powf (may differ from the host libm in the last place). */
+ * Gamma 2.2 is bit-exact (the reference's own table-and-quartic powf), and so are the sRGB curves (the
+ * device powf corrected, per input, to the host libm's result by tables built when the first context
+ * on a device is created); other gammas use the device powf (may differ from the host libm in the
+ * last place). */
 #define NTG_TRANSFORM_TO_LINEAR 0
 #define NTG_TRANSFORM_TO_GAMMA 1
 #define NTG_TRANSFORM_FROM_SRGB 2

@@ -17,6 +17,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -703,6 +704,77 @@ const char *ntg_last_error_string(void) { return g_error.c_str(); }
 
 unsigned long long ntg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
+namespace {
+
+// The sRGB curves' correction tables (ntg_device.cuh), built once per device by the first context on
+// it: the host evaluates every float of both power segments with its libm, on all its cores; a kernel
+// compares each with the device's result and keeps the 4-bit difference. Kept until the process ends.
+std::mutex g_fix_mu;
+uint8_t *g_fix_to[64], *g_fix_from[64];
+
+void host_segment(int which, uint32_t first, uint32_t count, float *out) {
+    const unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; t++) {
+        pool.emplace_back([=] {
+            const uint32_t lo = which ? kFromSrgbLo : kToSrgbLo;
+            for (uint32_t k = (uint32_t)((uint64_t)count * t / nt); k < (uint32_t)((uint64_t)count * (t + 1) / nt); k++) {
+                const uint32_t u = lo + first + k;
+                float f;
+                std::memcpy(&f, &u, 4);
+                out[k] = which ? host_from_srgb(f) : host_to_srgb(f);
+            }
+        });
+    }
+    for (auto &th : pool) th.join();
+}
+
+int build_srgb_fix(int device) {
+    std::lock_guard<std::mutex> lk(g_fix_mu);
+    if (device < 0 || device >= 64) return fail(NTG_ERROR_INVALID_INPUT, "device index out of range");
+    if (g_fix_to[device]) return NTG_OK;
+    const uint32_t chunk = 1u << 24;
+    std::vector<float> h(chunk);
+    uint8_t *fix[2] = {nullptr, nullptr};
+    float *d_chunk = nullptr;
+    unsigned int *d_bad = nullptr;
+    unsigned int bad = 0;
+    int r = NTG_OK;
+    if (cudaMalloc((void **)&fix[0], (kToSrgbCount + 1) / 2) != cudaSuccess ||
+        cudaMalloc((void **)&fix[1], (kFromSrgbCount + 1) / 2) != cudaSuccess ||
+        cudaMalloc((void **)&d_chunk, (size_t)chunk * sizeof(float)) != cudaSuccess ||
+        cudaMalloc((void **)&d_bad, sizeof bad) != cudaSuccess || cudaMemset(d_bad, 0, sizeof bad) != cudaSuccess)
+        r = cuda_fail(cudaGetLastError(), "sRGB correction tables");
+    for (int which = 0; which < 2 && r == NTG_OK; which++) {
+        const uint32_t n = which ? kFromSrgbCount : kToSrgbCount;
+        for (uint32_t first = 0; first < n && r == NTG_OK; first += chunk) {
+            const uint32_t count = std::min(chunk, n - first);
+            host_segment(which, first, count, h.data());
+            if (cudaMemcpy(d_chunk, h.data(), (size_t)count * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+                r = cuda_fail(cudaGetLastError(), "sRGB correction tables");
+            else
+                r = launched(launch_srgb_fix(d_chunk, first, count, which, fix[which], d_bad, nullptr), "sRGB correction tables");
+        }
+    }
+    if (r == NTG_OK && cudaMemcpy(&bad, d_bad, sizeof bad, cudaMemcpyDeviceToHost) != cudaSuccess)
+        r = cuda_fail(cudaGetLastError(), "sRGB correction tables");
+    if (r == NTG_OK && bad) r = fail(NTG_ERROR_CUDA, "device sRGB curve outside the correction range");
+    if (r == NTG_OK && (set_srgb_fix_mip(fix[0], fix[1]) || set_srgb_fix_bc1(fix[0])))
+        r = cuda_fail(cudaGetLastError(), "sRGB correction tables");
+    cudaFree(d_chunk);
+    cudaFree(d_bad);
+    if (r != NTG_OK) {
+        cudaFree(fix[0]);
+        cudaFree(fix[1]);
+        return r;
+    }
+    g_fix_to[device] = fix[0];
+    g_fix_from[device] = fix[1];
+    return NTG_OK;
+}
+
+}  // namespace
+
 int ntg_create(int device, ntg_context **out) {
     g_error.clear();
     if (!out) return fail(NTG_ERROR_INVALID_INPUT, "null output");
@@ -717,6 +789,7 @@ int ntg_create(int device, ntg_context **out) {
     NTG_TRY(upload_tables_bc3(ctx->tables));
     NTG_TRY(upload_tables_mip(ctx->tables));
     NTG_TRY(upload_tables_decode(ctx->tables));
+    NTG_TRY(build_srgb_fix(device));
     *out = ctx.release();
     return NTG_OK;
 }

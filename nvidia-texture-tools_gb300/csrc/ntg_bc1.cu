@@ -29,14 +29,15 @@ struct LaneW {
     __device__ __forceinline__ float &operator[](int k) const { return base[(k >> 2) * stride + (k & 3)]; }
 };
 
-__device__ __forceinline__ float to_srgb(float f) {
-    // toSrgb (src/nvtt/Surface.cpp:1512-1519)
-    if (isnan(f)) return 0.0f;
-    if (f <= 0.0f) return 0.0f;
-    if (f <= 0.0031308f) return 12.92f * f;
-    if (f <= 1.0f) return (powf(f, 0.41666f) * 1.055f) - 0.055f;
-    return 1.0f;
+// The device's toSrgb correction table (set once per device when a context is created).
+static __device__ const uint8_t *g_to_srgb_fix;
+
+int set_srgb_fix_bc1(const uint8_t *to_srgb) {
+    return cudaMemcpyToSymbol(g_to_srgb_fix, &to_srgb, sizeof to_srgb) == cudaSuccess ? 0 : launch_status();
 }
+
+// toSrgb (src/nvtt/Surface.cpp:1512-1519), bit-identical to the host libm's
+__device__ __forceinline__ float to_srgb(float f) { return to_srgb_exact(f, g_to_srgb_fix); }
 
 __device__ __forceinline__ unsigned to565(f3 v) {
     // vector3_to_color16 (src/nvtt/icbc.h:1580-1595)

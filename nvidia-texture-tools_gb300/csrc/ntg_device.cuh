@@ -98,6 +98,37 @@ __device__ __forceinline__ float powf_5_11(float x) {
     return c_tab.pow_5_11[u >> 23] * pm;
 }
 
+// The sRGB curves (toSrgb / toLinearFromSrgb, src/nvtt/Surface.cpp:1512-1519, 1562-1568). Their power
+// segments call powf, and the device's powf and the host libm's (which the reference uses) differ in
+// the last place for ~6% of the floats there. Every float of the two segments' domains is therefore
+// given a correction: the host evaluates the segment with its libm, a kernel evaluates the same
+// expression below and stores the difference of the two results' bit patterns (within -8..7 on
+// every input: 4 bits; the build checks it) in a table per device. The corrected device results
+// equal the host's bit for bit, over the whole domain.
+// (The domains' bounds kToSrgbLo, kFromSrgbLo, kSrgbHi are in ntg_host_tables.h.)
+__device__ __forceinline__ float srgb_pow_segment(float f) { return (powf(f, 0.41666f) * 1.055f) - 0.055f; }
+__device__ __forceinline__ float linear_pow_segment(float f) { return powf((f + 0.055f) / 1.055f, 2.4f); }
+
+// y corrected by entry i of a 4-bit table (two entries per byte, low nibble first, two's complement).
+__device__ __forceinline__ float srgb_fixed(const uint8_t *fix, uint32_t i, float y) {
+    const int b = __ldg(fix + (i >> 1));
+    const int d = (i & 1) ? (b >> 4) : (b & 15);
+    return __uint_as_float(__float_as_uint(y) + (d >= 8 ? d - 16 : d));
+}
+__device__ __forceinline__ float to_srgb_exact(float f, const uint8_t *fix) {
+    if (isnan(f)) return 0.0f;
+    if (f <= 0.0f) return 0.0f;
+    if (f <= 0.0031308f) return 12.92f * f;
+    if (f <= 1.0f) return srgb_fixed(fix, __float_as_uint(f) - kToSrgbLo, srgb_pow_segment(f));
+    return 1.0f;
+}
+__device__ __forceinline__ float from_srgb_exact(float f, const uint8_t *fix) {
+    if (f < 0.0f) return 0.0f;
+    if (f < 0.04045f) return f / 12.92f;
+    if (f <= 1.0f) return srgb_fixed(fix, __float_as_uint(f) - kFromSrgbLo, linear_pow_segment(f));
+    return 1.0f;
+}
+
 // Packed FP32 pairs: two floats in one 64-bit register (the first in the low half) added by one
 // instruction (add.rn.f32x2, sm_100 and later), which rounds each half exactly as the scalar
 // add.rn.f32 does. The products that feed it stay scalar multiplies: a packed multiply whose result

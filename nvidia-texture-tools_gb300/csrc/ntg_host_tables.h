@@ -29,6 +29,12 @@ void build_device_tables(HostTables &t);
 // Colour transforms, 0 none / 1 power-law gamma / 2 sRGB.
 float host_to_srgb(float f);
 float host_from_srgb(float f);
+// Float bit patterns of the sRGB curves' power segments: toSrgb's covers the floats above 0.0031308f
+// up to 1.0f, toLinearFromSrgb's 0.04045f up to 1.0f (the domains of the device correction tables).
+constexpr uint32_t kToSrgbLo = 0x3B4D2E1Du;    // first float above 0.0031308f
+constexpr uint32_t kFromSrgbLo = 0x3D25AEE6u;  // 0.04045f
+constexpr uint32_t kSrgbHi = 0x3F800000u;      // 1.0f
+constexpr uint32_t kToSrgbCount = kSrgbHi - kToSrgbLo + 1, kFromSrgbCount = kSrgbHi - kFromSrgbLo + 1;
 float host_xform_in(float v, int xform, float gamma, const HostTables &t);
 float host_xform_out(float v, int xform, float gamma, const HostTables &t);
 void build_input_lut(int xform, float gamma, const HostTables &t, float lut[256]);

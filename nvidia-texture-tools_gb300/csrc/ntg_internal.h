@@ -124,6 +124,12 @@ int launch_set_image(const uint32_t *bgra, size_t n, const float *lut, float *ou
 int launch_quantize(const float *rgba, size_t n, int xform, const float *steps, uint32_t *out, cudaStream_t s);
 int launch_transform(float *rgba, size_t n, int kind, float p, cudaStream_t s);
 int launch_mip(const MipLaunch &m, const MipJob *d_jobs, cudaStream_t s);
+// The sRGB curves' correction tables (ntg_device.cuh): one chunk of entries from the host's results,
+// and the tables' device addresses for the kernels of each translation unit that evaluates the curves.
+int launch_srgb_fix(const float *host_chunk, uint32_t first, uint32_t count, int which, uint8_t *fix, unsigned int *bad,
+                    cudaStream_t s);
+int set_srgb_fix_mip(const uint8_t *to_srgb, const uint8_t *from_srgb);
+int set_srgb_fix_bc1(const uint8_t *to_srgb);
 bool poly2x_supported(int ws);
 // 2:1 steps from the BGRA8 input (persistent, cp.async-pipelined 64 x 16 tiles): the window start of
 // output column 0 mod 4 that the kernel for `ws` taps is built for (-1: none), and the tile size.

@@ -1181,22 +1181,41 @@ __global__ void __launch_bounds__(1024) k_mip_tail(const MipJob *__restrict__ jo
 // ---------------------------------------------------------------------------------------------
 // Colour transforms of RGB on a planar FP32 level, in place (Surface::toLinear / toGamma /
 // toLinearFromSrgb / toSrgb, src/nvtt/Surface.cpp:1470-1592). Gamma 2.2 uses the reference's own
-// table-and-quartic powf_11_5 / powf_5_11 and is bit-exact; the sRGB curves and other gammas call
-// the device powf, which can differ from the host libm's in the last place.
-__device__ __forceinline__ float dev_to_srgb(float f) {
-    if (isnan(f)) return 0.0f;
-    if (f <= 0.0f) return 0.0f;
-    if (f <= 0.0031308f) return 12.92f * f;
-    if (f <= 1.0f) return (powf(f, 0.41666f) * 1.055f) - 0.055f;
-    return 1.0f;
+// table-and-quartic powf_11_5 / powf_5_11 and the sRGB curves the device's correction tables: both
+// bit-exact. Other gammas call the device powf, which can differ from the host libm's in the last place.
+static __device__ const uint8_t *g_to_srgb_fix_m, *g_from_srgb_fix_m;
+
+__device__ __forceinline__ float dev_to_srgb(float f) { return to_srgb_exact(f, g_to_srgb_fix_m); }
+__device__ __forceinline__ float dev_from_srgb(float f) { return from_srgb_exact(f, g_from_srgb_fix_m); }
+
+int set_srgb_fix_mip(const uint8_t *to_srgb, const uint8_t *from_srgb) {
+    if (cudaMemcpyToSymbol(g_to_srgb_fix_m, &to_srgb, sizeof to_srgb) != cudaSuccess ||
+        cudaMemcpyToSymbol(g_from_srgb_fix_m, &from_srgb, sizeof from_srgb) != cudaSuccess)
+        return launch_status();
+    return 0;
 }
 
-__device__ __forceinline__ float dev_from_srgb(float f) {
-    if (f < 0.0f) return 0.0f;
-    if (f < 0.04045f) return f / 12.92f;
-    if (f <= 1.0f) return powf((f + 0.055f) / 1.055f, 2.4f);
-    return 1.0f;
+// One chunk of a correction table: entries [first, first + count) (first even) of the toSrgb (which 0)
+// or toLinearFromSrgb (which 1) power segment, from the host's results `host` of those entries. One
+// thread per table byte (two entries); entries outside -8..7 count in *bad.
+__global__ void k_srgb_fix(const float *__restrict__ host, uint32_t first, uint32_t count, int which,
+                           uint8_t *__restrict__ fix, unsigned int *__restrict__ bad) {
+    const uint32_t pairs = (count + 1) / 2;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < pairs; t += gridDim.x * blockDim.x) {
+        uint32_t byte = 0;
+        for (int j = 0; j < 2; j++) {
+            const uint32_t k = 2 * t + j;
+            if (k >= count) break;
+            const float f = __uint_as_float((which ? kFromSrgbLo : kToSrgbLo) + first + k);
+            const float y = which ? linear_pow_segment(f) : srgb_pow_segment(f);
+            const int d = (int)(__float_as_uint(host[k]) - __float_as_uint(y));
+            if (d < -8 || d > 7) atomicAdd(bad, 1u);
+            byte |= (uint32_t)(d & 15) << (4 * j);
+        }
+        fix[(first >> 1) + t] = (uint8_t)byte;
+    }
 }
+
 
 // kind: 0 toLinear(2.2), 1 toGamma(2.2), 2 toLinearFromSrgb, 3 toSrgb, 4 pow(max(0, x), p)
 __global__ void k_transform(float *__restrict__ rgb, size_t n3, int kind, float p) {
@@ -1218,6 +1237,13 @@ static int grid_for(size_t n, int threads) {
     size_t g = (n + threads - 1) / threads;
     const size_t cap = 152 * 64;
     return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+int launch_srgb_fix(const float *host_chunk, uint32_t first, uint32_t count, int which, uint8_t *fix, unsigned int *bad,
+                    cudaStream_t s) {
+    if (count == 0) return 0;
+    k_srgb_fix<<<grid_for((count + 1) / 2, 256), 256, 0, s>>>(host_chunk, first, count, which, fix, bad);
+    return launch_status();
 }
 
 int launch_set_image(const uint32_t *bgra, size_t n, const float *lut, float *out, cudaStream_t s) {

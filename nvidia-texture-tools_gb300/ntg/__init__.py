@@ -19,6 +19,7 @@ WRAP_CLAMP, WRAP_REPEAT, WRAP_MIRROR = 0, 1, 2
 FILTER_BOX, FILTER_TRIANGLE, FILTER_KAISER = 0, 1, 2
 ALPHA_NONE, ALPHA_TRANSPARENCY = 0, 1
 XFORM_NONE, XFORM_GAMMA, XFORM_SRGB = 0, 1, 2
+TRANSFORM_TO_LINEAR, TRANSFORM_TO_GAMMA, TRANSFORM_FROM_SRGB, TRANSFORM_TO_SRGB = 0, 1, 2, 3  # ntg_transform kinds
 # learned encode: a steepest descent from the proposal instead of a window (radius = DESCENT | moves)
 NTG_PROPOSAL_DESCENT = 256
 NTG_PROPOSAL_REFIT = 512     # BC1: least-squares endpoint refit after the search

@@ -1,6 +1,8 @@
 """GPU parity: every kernel of libntg.so, called through its C ABI, against the oracle (the C
-restatement pinned to the reference) on the same seeded inputs. Bit-exact everywhere except
-where noted (sRGB output transform on float BC1 levels uses the device's powf)."""
+restatement pinned to the reference) on the same seeded inputs, bit-exact (the sRGB curves on
+float levels included: the device corrects its powf to the host libm's results)."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -148,21 +150,42 @@ def test_bc1a_bc4_golden_blocks(ctx):
 @pytest.mark.parametrize("fmt", [ntg.FORMAT_BC1, ntg.FORMAT_BC3])
 @pytest.mark.parametrize("out_xform", [ntg.XFORM_GAMMA, ntg.XFORM_SRGB])
 def test_encode_with_output_transform(ctx, oracle, fmt, out_xform):
-    """Compressor::compress after toGamma(2.2) / toSrgb of the level (BC3: exact via the quantiser
-    tables; BC1 sRGB: the device powf, compared by decoded error)."""
-    w, h = 48, 24
+    """Compressor::compress after toGamma(2.2) / toSrgb of the level: BC3 through the quantiser
+    tables, BC1 on the float level through the device's corrected sRGB curve; every block exact."""
+    w, h = 96, 64
     img = float_image(w, h, 31)
     enc = img.copy()
     n = w * h
     enc[:3 * n] = oracle.powf_5_11(img[:3 * n]) if out_xform == ntg.XFORM_GAMMA else oracle.to_srgb(img[:3 * n])
-    ours = host(ctx.encode(fmt, dev(img), w, h, quality=1, out_xform=out_xform, gamma=2.2))
-    ref = oracle.bc1_image(enc, w, h, 0, 1, threads=4) if fmt == 1 else oracle.bc3_image(enc, w, h, 0, 1, threads=4)
-    if fmt == ntg.FORMAT_BC1 and out_xform == ntg.XFORM_SRGB:
-        rc, _ = oracle.rms(fmt, enc, ref, w, h)
-        oc, _ = oracle.rms(fmt, enc, ours, w, h)
-        assert oc <= rc * 1.005 + 1e-7
-    else:
-        assert np.array_equal(ours, ref)
+    for q in (0, 1, 2):
+        ours = host(ctx.encode(fmt, dev(img), w, h, quality=q, out_xform=out_xform, gamma=2.2))
+        ref = oracle.bc1_image(enc, w, h, 0, q, threads=4) if fmt == 1 else oracle.bc3_image(enc, w, h, 0, q, threads=4)
+        assert np.array_equal(ours, ref), q
+
+
+def _domain(lo_bits, hi_bits, margin):
+    """Every float from lo_bits - margin to hi_bits + margin, plus zeros, negatives, 2 and NaN."""
+    u = np.arange(lo_bits - margin, hi_bits + margin + 1, dtype=np.uint64).astype(np.uint32)
+    extra = np.array([0.0, -0.0, -1e-8, -0.5, 2.0, np.inf, np.nan, 1.0000001], np.float32).view(np.uint32)
+    return np.concatenate([u, extra]).view(np.float32)
+
+
+@pytest.mark.parametrize("kind", [ntg.TRANSFORM_TO_SRGB, ntg.TRANSFORM_FROM_SRGB])
+def test_srgb_curves_exact_over_their_domains(ctx, oracle, kind):
+    """toSrgb over every float of its power segment (0.0031308, 1] and toLinearFromSrgb over every float
+    of [0.04045, 1] (70.4 M and 39.5 M values, with a margin either side and special values): the
+    device's corrected curves equal the host libm's, bit for bit."""
+    lo = 0x3B4D2E1C if kind == ntg.TRANSFORM_TO_SRGB else 0x3D25AEE6
+    vals = _domain(lo, 0x3F800000, 4096)
+    n = -(-vals.size // 3)
+    planes = np.zeros(4 * n, np.float32)
+    planes[:vals.size] = vals                      # R, G, B planes hold the domain in order
+    d = dev(planes)
+    ntg._check(ntg.lib().ntg_transform(ctx.h, d.data_ptr(), n, 1, kind, ctypes.c_float(2.2), None))
+    ours = host(d)[:vals.size]
+    ref = oracle.to_srgb(vals) if kind == ntg.TRANSFORM_TO_SRGB else oracle.from_srgb(vals)
+    bad = np.flatnonzero(ours.view(np.uint32) != ref.view(np.uint32))
+    assert bad.size == 0, (bad.size, vals[bad[:5]], ours[bad[:5]], ref[bad[:5]])
 
 
 # ---------------------------------------------------------------------------------------------
@@ -272,6 +295,7 @@ CHAINS = [
     (37, 37, 6, 2, 2, 0, 1, 1, 0),      # BC4 Production, Kaiser, gamma
     (1, 4096, 4, 1, 2, 0, 0, 0, 2),     # 1-wide and tall: the tail's X plane keeps the full height
     (4096, 1, 1, 1, 2, 1, 2, 2, 1),     # 1-high and wide, sRGB
+    (256, 192, 1, 1, 2, 1, 2, 2, 2),    # BC1 on float levels through the sRGB curve, transparency weights
     # level 1 from the BGRA8 input: tiles whose window lies inside the level take whole-vector copies
     (384, 128, 4, 1, 2, 1, 2, 2, 2),    # Kaiser / sRGB / BC3, interior tiles at (64, 16) and (64, 32)
     (320, 96, 1, 1, 1, 0, 0, 0, 1),     # triangle, repeat, BC1, interior tiles
