@@ -14,9 +14,9 @@ Mtexels/s = encoded texels of all levels / step time.
              full fit of the flagged blocks; its Mtexels/s, the ratio to plain, and per texture the
              RMSE (nvtt::rmsError on the decoded levels) against the plain fit's, at each operating
              point measured.
-  e2e      : the plain batch through its host-copy binding: every step copies every texture in from
-             pinned host memory and every texture's blocks out, two bindings overlapping copies with
-             the neighbouring steps' graphs.
+  e2e      : the plain batch over host buffers through ntg_batch_process_host: every step copies every
+             texture in from pinned host memory and every texture's blocks out, two bindings taking
+             turns so that the copies run beside the neighbouring steps' graphs.
   roofline : the dominant kernel (the BC1 cluster fit) against the FP32 rate of the clocks seen, its
              orderings counted on the device; the mip phase against measured HBM bandwidth.
   cpu_baseline : the oracle port (C restatement of the reference path) on the host cores, a bounded
@@ -699,8 +699,8 @@ def run_gpu_batch(args):
     log(f"plain: {dev_ms / args.steps:.2f} ms per step")
 
     # end to end: every step copies every texture in from pinned host memory, replays the graph and
-    # copies every texture's blocks out; two bindings of the batch (double buffering) let a step's
-    # copies run beside the neighbouring steps' graphs
+    # copies every texture's blocks out, in one library call over the steps; two bindings of the batch
+    # (double buffering) let a step's copies run beside the neighbouring steps' graphs
     h_in = [torch.from_numpy(img.reshape(-1).view(np.uint32)).pin_memory() for img in host_in]
     h_outs = [[torch.empty(t[4].numel(), dtype=torch.uint8).pin_memory() for t in textures] for _ in range(2)]
     bi = sum(int(x.numel()) * 4 for x in h_in)
@@ -710,32 +710,11 @@ def run_gpu_batch(args):
     alt_in = [torch.empty_like(t[0]) for t in textures]
     alt_out = [torch.empty_like(t[4]) for t in textures]
     batch.bind_alternate(alt_in, alt_out)
-    slots = [([t[0] for t in textures], [t[4] for t in textures]), (alt_in, alt_out)]
-    up, down, comp = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.current_stream()
-    ev_in = [torch.cuda.Event() for _ in range(2)]
-    ev_done = [torch.cuda.Event() for _ in range(2)]
-    ev_out = [torch.cuda.Event() for _ in range(2)]
 
     def e2e_run(n):
-        for k in range(n):
-            slot = k & 1
-            ins, outs = slots[slot]
-            with torch.cuda.stream(up):
-                if k >= 2:
-                    up.wait_event(ev_done[slot])  # the graph of step k-2 has read these inputs
-                for d, x in zip(ins, h_in):
-                    d.copy_(x, non_blocking=True)
-                ev_in[slot].record(up)
-            comp.wait_event(ev_in[slot])
-            if k >= 2:
-                comp.wait_event(ev_out[slot])  # step k-2's blocks are out of these buffers
-            batch.launch(stream=comp, alternate=bool(slot))
-            ev_done[slot].record(comp)
-            with torch.cuda.stream(down):
-                down.wait_event(ev_done[slot])
-                for d, y in zip(outs, h_outs[slot]):
-                    y.copy_(d, non_blocking=True)
-                ev_out[slot].record(down)
+        # one library call over n sets of host buffers: copies in, graph, copies out per set, the two
+        # bindings taking turns (ntg_batch_process_host)
+        batch.process_host([(h_in, h_outs[k & 1]) for k in range(n)])
         torch.cuda.synchronize()
 
     e2e_run(2)
@@ -815,7 +794,7 @@ def run_gpu_batch(args):
                            "images": "one seeded image per distinct (size, format)"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
                         "matches_device_path": same,
-                        "api": "ntg_batch_launch / ntg_batch_launch_alternate (two bindings), copies on two streams"},
+                        "api": "ntg_batch_process_host: host buffers, two bindings taking turns, copies on their own streams"},
                 "gpu_launches": info["launches"] * args.steps,
                 "clocks": clocks, "roofline": roof, "roofline_mips": roof_mips,
                 "phase_ms": phases, "phase_blocks": blocks, "dominant_phase": dominant,

@@ -228,6 +228,17 @@ int ntg_batch_launch(ntg_batch *batch, void *stream);
  * them), never concurrently. Autotuning and ntg_batch_set_proposal recapture both. */
 int ntg_batch_bind_alternate(ntg_batch *batch, const void *const *d_bgra, void *const *d_blocks);
 int ntg_batch_launch_alternate(ntg_batch *batch, void *stream);
+/* The batch over host buffers: for each of `count` sets, copies the set's images in
+ * (h_bgra[set][texture], w * h words each), replays the graph and copies the blocks out
+ * (h_blocks[set][texture], ntg_chain_bytes each), as Compressor::process would for each image and
+ * texture. With an alternate binding the two bindings take turns, so that one set's copies run
+ * beside the neighbouring sets' graphs (copy-in and copy-out on their own streams); without one the
+ * sets run one after the other. Host buffers should be page-locked (cudaHostAlloc / cudaHostRegister)
+ * for the copies to overlap. The batch's own device inputs and outputs (and the alternate binding's)
+ * are overwritten. Returns after the last set's blocks are on the host. No counterpart in the
+ * reference, which compresses one image per process() call (src/nvtt/Context.cpp:217-346). */
+int ntg_batch_process_host(ntg_batch *batch, int count, const void *const *const *h_bgra, void *const *const *h_blocks,
+                           void *stream);
 /* Times candidate launch shapes on this batch (rows per strip and threads per CTA of the 2:1 mip
  * kernel, the tail threshold, blocks per CTA of each encoder), keeps the fastest, recaptures the
  * graph and stores the choice in the tuning cache. Synchronises `stream`. */

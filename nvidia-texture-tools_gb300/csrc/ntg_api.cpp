@@ -1214,15 +1214,23 @@ int ntg_compress_chains_host(ntg_context *ctx, int n, const void *const *h_bgra,
     uint8_t *in[2] = {ctx->slots, ctx->slots + ctx->slot_in};
     uint8_t *out[2] = {ctx->slots + 2 * ctx->slot_in, ctx->slots + 2 * ctx->slot_in + ctx->slot_out};
     // the slots' previous users (an earlier call) are done: they all ended with this call's streams drained
-    for (int i = 0; i < n; i++) {
+    auto copy_in = [&](int i) -> int {
         const int k = i & 1;
         if (i >= 2) NTG_CUDA(cudaStreamWaitEvent(ctx->up, ctx->ev_done[k], 0));      // chain i-2 read in[k]
         NTG_CUDA(cudaMemcpyAsync(in[k], h_bgra[i], in_bytes, cudaMemcpyHostToDevice, ctx->up));
         NTG_CUDA(cudaEventRecord(ctx->ev_in[k], ctx->up));
+        return NTG_OK;
+    };
+    // the next image's copy-in is issued before this chain's copy-out: a copy-out to memory the driver
+    // does not treat as page-locked returns only once it is done, and must not hold back the copy-in
+    if (n > 0) NTG_TRY(copy_in(0));
+    for (int i = 0; i < n; i++) {
+        const int k = i & 1;
         NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_in[k], 0));
         if (i >= 2) NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_out[k], 0));             // blocks of i-2 copied out
         NTG_TRY(chain_common(ctx, in[k], w, h, opt, out[k], nullptr, s));
         NTG_CUDA(cudaEventRecord(ctx->ev_done[k], s));
+        if (i + 1 < n) NTG_TRY(copy_in(i + 1));
         NTG_CUDA(cudaStreamWaitEvent(ctx->down, ctx->ev_done[k], 0));
         NTG_CUDA(cudaMemcpyAsync(h_blocks[i], out[k], out_bytes, cudaMemcpyDeviceToHost, ctx->down));
         NTG_CUDA(cudaEventRecord(ctx->ev_out[k], ctx->down));
@@ -1776,6 +1784,59 @@ int ntg_batch_launch_alternate(ntg_batch *b, void *stream) {
     if (!b || !b->exec_alt) return fail(NTG_ERROR_INVALID_INPUT, "no alternate binding");
     NTG_TRY(ensure_device(b->ctx));
     NTG_CUDA(cudaGraphLaunch(b->exec_alt, S(stream)));
+    return NTG_OK;
+}
+
+int ntg_batch_process_host(ntg_batch *b, int count, const void *const *const *h_bgra, void *const *const *h_blocks,
+                           void *stream) {
+    g_error.clear();
+    if (!b || !b->exec || count < 0 || (count > 0 && (!h_bgra || !h_blocks))) return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    const size_t nt = b->tex.size();
+    for (int i = 0; i < count; i++) {
+        if (!h_bgra[i] || !h_blocks[i]) return fail(NTG_ERROR_INVALID_INPUT, "null set");
+        for (size_t t = 0; t < nt; t++)
+            if (!h_bgra[i][t] || !h_blocks[i][t]) return fail(NTG_ERROR_INVALID_INPUT, "null image or output");
+    }
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    ntg_context *ctx = b->ctx;
+    NTG_TRY(ensure_device(ctx));
+    NTG_TRY(ctx->copy_streams());
+    cudaStream_t s = S(stream);
+    const bool two = b->exec_alt != nullptr;
+    const int lag = two ? 2 : 1;  // sets between two uses of one binding
+    auto slot = [&](int i) { return two ? (i & 1) : 0; };
+    // copy-in of set i on the up stream, once the graph that last read its binding's inputs is done
+    auto copy_in = [&](int i) -> int {
+        const int k = slot(i);
+        const std::vector<ntg_batch_texture> &io = k ? b->alt : b->tex;
+        if (i >= lag) NTG_CUDA(cudaStreamWaitEvent(ctx->up, ctx->ev_done[k], 0));
+        for (size_t t = 0; t < nt; t++)
+            NTG_CUDA(cudaMemcpyAsync(const_cast<void *>(io[t].d_bgra), h_bgra[i][t], (size_t)io[t].w * io[t].h * 4,
+                                     cudaMemcpyHostToDevice, ctx->up));
+        NTG_CUDA(cudaEventRecord(ctx->ev_in[k], ctx->up));
+        return NTG_OK;
+    };
+    // the same events as the single-chain pipeline: their previous users ended with drained streams.
+    // The next set's copy-in is issued before this set's copy-out: a copy-out to memory the driver
+    // does not treat as page-locked returns only once it is done, and must not hold back the copy-in.
+    if (count > 0) NTG_TRY(copy_in(0));
+    for (int i = 0; i < count; i++) {
+        const int k = slot(i);
+        const std::vector<ntg_batch_texture> &io = k ? b->alt : b->tex;
+        NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_in[k], 0));
+        if (i >= lag) NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_out[k], 0));  // earlier blocks copied out
+        NTG_CUDA(cudaGraphLaunch(k ? b->exec_alt : b->exec, s));
+        NTG_CUDA(cudaEventRecord(ctx->ev_done[k], s));
+        if (i + 1 < count) NTG_TRY(copy_in(i + 1));
+        NTG_CUDA(cudaStreamWaitEvent(ctx->down, ctx->ev_done[k], 0));
+        for (size_t t = 0; t < nt; t++)
+            NTG_CUDA(cudaMemcpyAsync(h_blocks[i][t], io[t].d_blocks, ntg_chain_bytes(io[t].w, io[t].h, &io[t].opt),
+                                     cudaMemcpyDeviceToHost, ctx->down));
+        NTG_CUDA(cudaEventRecord(ctx->ev_out[k], ctx->down));
+    }
+    NTG_CUDA(cudaStreamSynchronize(ctx->up));
+    NTG_CUDA(cudaStreamSynchronize(s));
+    NTG_CUDA(cudaStreamSynchronize(ctx->down));
     return NTG_OK;
 }
 

@@ -101,6 +101,7 @@ def lib():
         "ntg_compress_chain_host": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
         "ntg_batch_bind_alternate": (_i, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
         "ntg_batch_launch_alternate": (_i, [_vp, _vp]),
+        "ntg_batch_process_host": (_i, [_vp, _i, _vp, _vp, _vp]),
         "ntg_compress_chains_host": (_i, [_vp, _i, ctypes.POINTER(_vp), _i, _i, ctypes.POINTER(ChainOptions),
                                           ctypes.POINTER(_vp), _vp]),
         "ntg_mip_chain": (_i, [_vp, _vp, _i, _i, ctypes.POINTER(ChainOptions), _vp, _vp]),
@@ -413,6 +414,25 @@ class Batch:
         a = (_vp * n)(*[x.data_ptr() for x in inputs])
         b = (_vp * n)(*[y.data_ptr() for y in outputs])
         _check(lib().ntg_batch_bind_alternate(self.h, a, b))
+
+    def process_host(self, sets, stream=None):
+        """The batch over host buffers (ntg_batch_process_host): sets = [(inputs, outputs), ...], one
+        host buffer per texture each (numpy arrays or CPU tensors; page-locked ones overlap the copies
+        with the neighbouring sets' graphs when an alternate binding is bound). Returns when the last
+        set's blocks are on the host."""
+        n = len(self._keep)
+
+        def ptr(x):
+            return x.data_ptr() if hasattr(x, "data_ptr") else x.ctypes.data
+
+        inner = []
+        for ins, outs in sets:
+            assert len(ins) == n and len(outs) == n
+            inner.append(((_vp * n)(*[ptr(x) for x in ins]), (_vp * n)(*[ptr(y) for y in outs])))
+        a = (_vp * len(sets))(*[ctypes.cast(i[0], _vp).value for i in inner])
+        b = (_vp * len(sets))(*[ctypes.cast(i[1], _vp).value for i in inner])
+        _check(lib().ntg_batch_process_host(self.h, len(sets), ctypes.cast(a, _vp), ctypes.cast(b, _vp),
+                                            _stream_ptr(stream)))
 
     def autotune(self, stream=None):
         _check(lib().ntg_batch_autotune(self.h, _stream_ptr(stream)))

@@ -154,6 +154,39 @@ def test_alternate_binding(ctx, tmp_path, monkeypatch):
         b.close()
 
 
+@pytest.mark.parametrize("alternate", [False, True])
+def test_process_host_sets(ctx, tmp_path, monkeypatch, alternate):
+    """ntg_batch_process_host: several sets of host images through the batch, each set's host blocks
+    equal to the single-chain encodes of its images, with one binding (sets in turn) and with two
+    (copies beside the neighbouring sets' graphs; page-locked and pageable host buffers)."""
+    import torch
+    monkeypatch.setenv("NTG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    cases = MIXED[:6]
+    _, textures, _ = make_batch(ctx, cases, 500)
+    b = ntg.Batch(ctx, textures)
+    try:
+        if alternate:
+            b.bind_alternate([torch.empty_like(t[0]) for t in textures], [torch.empty_like(t[4]) for t in textures])
+        sets, refs = [], []
+        for k in range(5):
+            ins, outs, rs = [], [], []
+            for i, (c, t) in enumerate(zip(cases, textures)):
+                img = image(c, 2000 + 10 * k + i).reshape(-1).view(np.uint32)
+                x = torch.from_numpy(img.copy())
+                ins.append(x.pin_memory() if k % 2 == 0 else x)
+                y = torch.zeros(t[4].numel(), dtype=torch.uint8)
+                outs.append(y.pin_memory() if k % 2 == 0 else y)
+                rs.append(host(ctx.compress_chain(dev(img), c[0], c[1], t[3])))
+            sets.append((ins, outs))
+            refs.append(rs)
+        b.process_host(sets)
+        for (ins, outs), rs in zip(sets, refs):
+            for y, r in zip(outs, rs):
+                assert np.array_equal(y.numpy(), r)
+    finally:
+        b.close()
+
+
 def test_autotune_keeps_results_and_caches_shape(ctx, tmp_path, monkeypatch):
     cache = tmp_path / "tune.json"
     monkeypatch.setenv("NTG_TUNE_CACHE", str(cache))
