@@ -940,8 +940,11 @@ def run_gpu_learned(args):
         return sum(a.elapsed_time(b) for a, b in ev) / args.steps
 
     with ClockSampler(torch.cuda.current_device()) as clk:
+        n0 = ntg.launch_count()
         learned_ms = timed_steps(lambda: ctx.compress_chain_learned(net, d, size, size, opt, radius=cfg["radius"],
                                                                     margin=cfg["margin"], out=out, stats=False))
+        # the library's kernel launches per learned chain (the timed steps and their warm-up)
+        learned_launches = (ntg.launch_count() - n0) // (args.steps + args.warmup)
         plain_ms = timed_steps(lambda: ctx.compress_chain(d, size, size, opt, out=plain))
     value = texels / (learned_ms / 1000.0) / 1e6
     rmse_plain = learned.chain_rmse(ctx, d, size, size, opt, plain)
@@ -998,7 +1001,7 @@ def run_gpu_learned(args):
                         "frontier": frontier},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(img.nbytes),
                     "d2h_bytes_per_step": int(out.numel()), "matches_device_path": bool(torch.equal(h_out, out.cpu()))},
-            "gpu_launches": None, "clocks": clk.summary(),
+            "gpu_launches": learned_launches * args.steps, "clocks": clk.summary(),
             "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
                          "traffic": None, "kernel": "k_mlp_infer (fused 3-layer tcgen05 inference, one call over all blocks)",
                          "flop_per_block": 2 * (48 * 256 + 256 * 256 + 256 * 16), "ms": infer_ms, "peak_source": peak_src},
