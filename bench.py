@@ -498,6 +498,8 @@ def measure_chain(ctx, name, args, world, rank, with_cpu):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "base_level": {"value": w * h * args.steps / (dev_ms / 1000.0) / 1e6, "unit": UNIT,
+                               "texels_per_step": w * h, "note": "level-0 texels only, same device time"},
                 "config": {"workload": desc, "texels_per_step": texels, "blocks_per_step": ntg.chain_bytes(w, h, opt) // 16
                            if fmt != 1 else ntg.chain_bytes(w, h, opt) // 8, "l2": "flushed (256 MiB write) between steps",
                            "method": "plain (non-learned) cluster fit", "replicas": world},
@@ -662,6 +664,7 @@ def run_gpu_batch(args):
     # N GPUs: the batch's textures split across the ranks (largest first by chain texels), each rank
     # running the batch of its own part; the whole batch's work is fixed (strong scaling)
     total_texels = sum(chain_texels(sp[0], sp[1]) for sp in specs)
+    base_texels = sum(sp[0] * sp[1] for sp in specs)
     if world > 1:
         from ntg import partition
         parts = partition.partition_textures([(sp[0], sp[1]) for sp in specs], world)
@@ -783,6 +786,8 @@ def run_gpu_batch(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
                 "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "base_level": {"value": base_texels * args.steps / (dev_ms / 1000.0) / 1e6, "unit": UNIT,
+                               "texels_per_step": base_texels, "note": "level-0 texels only, same device time"},
                 "config": {"workload": desc, "textures": BATCHES[name][0], "texels_per_step": total_texels,
                            "blocks_per_step": info["blocks"] if world == 1 else None,
                            "l2": "inputs (14 GB for c4) larger than L2, and L2 flushed (256 MiB write) between steps",
