@@ -1018,10 +1018,6 @@ __device__ int pruned_three(const Lane<float4> &sat, int n, f3 metric, int e0, i
 // Steepest descent over cluster_fit_four's orderings from (e0, e1, e2): each move evaluates the
 // orderings one step away in any of the three ends (up to 26) and goes to the lowest error if it is
 // strictly below the current one; at most `moves` moves. Returns the number evaluated.
-// After a move by (pa_, pb_, pc_), the new neighbours that were also neighbours of the previous
-// ordering (or that ordering itself) are skipped: the move chose the first strict minimum among them,
-// so none is strictly below the new current error and none could be chosen. The descent's path and
-// result are those of evaluating every neighbour.
 __device__ int descend_four(const Lane<float4> &sat, int n, f3 metric, int e0, int e1, int e2, int moves, f3 &start,
                             f3 &end) {
     const float4 s = sat[n];  // a ZERO table
@@ -1031,25 +1027,19 @@ __device__ int descend_four(const Lane<float4> &sat, int n, f3 metric, int e0, i
     f3 pa, pb;
     float best = four_eval<true>(sat, pack_order(a, b, c), sum, wsum, metric, pa, pb);
     int evaluated = 1;
-    int pda = 0, pdb = 0, pdc = 0;  // the last move (none yet)
     for (int m = 0; m < moves; m++) {
         float mbest = best;
         int na = a, nb = b, nc = c;
-        const bool moved = (pda | pdb | pdc) != 0;
         for (int dc = -1; dc <= 1; dc++)
             for (int da = -1; da <= 1; da++)
                 for (int db = -1; db <= 1; db++) {
                     const int cc = c + dc, aa = a + da, bb = b + db;
                     if ((dc | da | db) == 0 || cc < 0 || cc > n - 1 || aa < -1 || aa > bb || bb > cc) continue;
-                    if (moved && (pda + da) >= -1 && (pda + da) <= 1 && (pdb + db) >= -1 && (pdb + db) <= 1 &&
-                        (pdc + dc) >= -1 && (pdc + dc) <= 1)
-                        continue;  // one step from the previous ordering too: not below the current error
                     const float e = four_eval<true>(sat, pack_order(aa, bb, cc), sum, wsum, metric, pa, pb);
                     evaluated++;
                     if (e < mbest) { mbest = e; na = aa; nb = bb; nc = cc; }
                 }
         if (!(mbest < best)) break;
-        pda = na - a; pdb = nb - b; pdc = nc - c;
         best = mbest; a = na; b = nb; c = nc;
     }
     start = mk3(0, 0, 0);
@@ -1066,23 +1056,19 @@ __device__ int descend_three(const Lane<float4> &sat, int n, f3 metric, int e0, 
     f3 pa, pb;
     float best = three_eval<true>(sat, (uint32_t)(a + 1) | ((uint32_t)(c + 1) << 8), sum, wsum, metric, pa, pb);
     int evaluated = 1;
-    int pda = 0, pdc = 0;  // the last move (none yet); neighbours of the previous ordering are skipped
     for (int m = 0; m < moves; m++) {
         float mbest = best;
         int na = a, nc = c;
-        const bool moved = (pda | pdc) != 0;
         for (int dc = -1; dc <= 1; dc++)
             for (int da = -1; da <= 1; da++) {
                 const int cc = c + dc, aa = a + da;
                 if ((dc | da) == 0 || cc < 0 || cc > n - 1 || aa < -1 || aa > cc) continue;
-                if (moved && (pda + da) >= -1 && (pda + da) <= 1 && (pdc + dc) >= -1 && (pdc + dc) <= 1) continue;
                 const float e = three_eval<true>(sat, (uint32_t)(aa + 1) | ((uint32_t)(cc + 1) << 8), sum, wsum, metric,
                                                  pa, pb);
                 evaluated++;
                 if (e < mbest) { mbest = e; na = aa; nc = cc; }
             }
         if (!(mbest < best)) break;
-        pda = na - a; pdc = nc - c;
         best = mbest; a = na; c = nc;
     }
     start = mk3(0, 0, 0);
