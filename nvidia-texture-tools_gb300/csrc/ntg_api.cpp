@@ -1816,23 +1816,37 @@ int ntg_batch_process_host(ntg_batch *b, int count, const void *const *const *h_
         NTG_CUDA(cudaEventRecord(ctx->ev_in[k], ctx->up));
         return NTG_OK;
     };
+    // graph of set i on the compute stream, once its inputs are in and the blocks of the set that last
+    // used its binding are out
+    auto run = [&](int i) -> int {
+        const int k = slot(i);
+        NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_in[k], 0));
+        if (i >= lag) NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_out[k], 0));
+        NTG_CUDA(cudaGraphLaunch(k ? b->exec_alt : b->exec, s));
+        NTG_CUDA(cudaEventRecord(ctx->ev_done[k], s));
+        return NTG_OK;
+    };
     // the same events as the single-chain pipeline: their previous users ended with drained streams.
-    // The next set's copy-in is issued before this set's copy-out: a copy-out to memory the driver
-    // does not treat as page-locked returns only once it is done, and must not hold back the copy-in.
-    if (count > 0) NTG_TRY(copy_in(0));
+    // A copy-out to memory the driver does not treat as page-locked returns only once it is done, so
+    // everything that can run beside it is issued first: the next set's copy-in, and with two bindings
+    // the next set's graph too (its binding's previous blocks, set i - 1's, were copied out earlier).
+    if (count > 0) {
+        NTG_TRY(copy_in(0));
+        NTG_TRY(run(0));
+    }
     for (int i = 0; i < count; i++) {
         const int k = slot(i);
         const std::vector<ntg_batch_texture> &io = k ? b->alt : b->tex;
-        NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_in[k], 0));
-        if (i >= lag) NTG_CUDA(cudaStreamWaitEvent(s, ctx->ev_out[k], 0));  // earlier blocks copied out
-        NTG_CUDA(cudaGraphLaunch(k ? b->exec_alt : b->exec, s));
-        NTG_CUDA(cudaEventRecord(ctx->ev_done[k], s));
-        if (i + 1 < count) NTG_TRY(copy_in(i + 1));
+        if (i + 1 < count) {
+            NTG_TRY(copy_in(i + 1));
+            if (two) NTG_TRY(run(i + 1));
+        }
         NTG_CUDA(cudaStreamWaitEvent(ctx->down, ctx->ev_done[k], 0));
         for (size_t t = 0; t < nt; t++)
             NTG_CUDA(cudaMemcpyAsync(h_blocks[i][t], io[t].d_blocks, ntg_chain_bytes(io[t].w, io[t].h, &io[t].opt),
                                      cudaMemcpyDeviceToHost, ctx->down));
         NTG_CUDA(cudaEventRecord(ctx->ev_out[k], ctx->down));
+        if (!two && i + 1 < count) NTG_TRY(run(i + 1));  // one binding: after this set's blocks are out
     }
     NTG_CUDA(cudaStreamSynchronize(ctx->up));
     NTG_CUDA(cudaStreamSynchronize(s));
