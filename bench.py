@@ -179,6 +179,9 @@ def dist_setup(args):
     if world > 1:
         import torch.distributed as dist
         backend = "nccl" if args.impl != "reference" else "gloo"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(local)  # one GPU per rank, before the communicator exists
         dist.init_process_group(backend=backend)
     return world, rank, local
 
@@ -186,7 +189,11 @@ def dist_setup(args):
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
-        dist.barrier()
+        if dist.get_backend() == "nccl":
+            import torch
+            dist.barrier(device_ids=[torch.cuda.current_device()])
+        else:
+            dist.barrier()
 
 
 def max_over_ranks(world, value, device=None):
