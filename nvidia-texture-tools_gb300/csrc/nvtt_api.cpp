@@ -606,13 +606,36 @@ uint32_t fourcc(char a, char b, char c, char d) {
     return (uint32_t)(uint8_t)a | ((uint32_t)(uint8_t)b << 8) | ((uint32_t)(uint8_t)c << 16) | ((uint32_t)(uint8_t)d << 24);
 }
 
-bool dds_header(Format format, int w, int h, int mipmapCount, bool isNormalMap, const OutputOptions::Private &oo,
-                std::vector<uint32_t> &words) {
+// nv::getTargetExtent (src/nvtt/Surface.cpp:220-283) for the InputOptions' layout: the largest extent
+// scaled down to maxExtent (a power of two when rounding), a cube map's faces made square at the mean
+// of the scaled extents, then the round mode. False for a layout without a positive extent.
+bool target_extent(const InputOptions::Private &io, int *w, int *h) {
+    if (io.width <= 0 || io.height <= 0) return false;
+    if (io.textureType != TextureType_Cube)
+        return ntg_target_extent(io.width, io.height, io.maxExtent, (int)io.roundMode, w, h) == NTG_OK;
+    int maxExtent = io.maxExtent;
+    if (io.roundMode != RoundMode_None && maxExtent > 0) {  // the power of two at or below it
+        int p = 1;
+        while (p <= maxExtent / 2) p *= 2;
+        maxExtent = p;
+    }
+    int sw = io.width, sh = io.height;
+    const int m = std::max(sw, sh);
+    if (maxExtent > 0 && m > maxExtent) { sw = std::max(sw * maxExtent / m, 1); sh = std::max(sh * maxExtent / m, 1); }
+    const int side = (sw + sh) / 2;
+    return ntg_target_extent(side, side, 0, (int)io.roundMode, w, h) == NTG_OK;
+}
+
+// `type` is TextureType_2D, _Cube or _Array; `arraySize` the image count of an array (1 otherwise).
+bool dds_header(Format format, TextureType type, int w, int h, int arraySize, int mipmapCount, bool isNormalMap,
+                const OutputOptions::Private &oo, std::vector<uint32_t> &words) {
     enum : uint32_t {
         CAPS = 0x1, HEIGHT = 0x2, WIDTH = 0x4, PIXELFORMAT = 0x1000, MIPMAPCOUNT = 0x20000, LINEARSIZE = 0x80000,
         CAPS_COMPLEX = 0x8, CAPS_TEXTURE = 0x1000, CAPS_MIPMAP = 0x400000,
+        CAPS2_CUBEMAP = 0x200, CAPS2_ALL_FACES = 0xFC00,  // +X -X +Y -Y +Z -Z
         PF_ALPHAPIXELS = 0x1, PF_FOURCC = 0x4, PF_NORMAL = 0x80000000u, PF_SRGB = 0x40000000u,
     };
+    const bool cube = type == TextureType_Cube;
     words.assign(37, 0);                            // magic + 124-byte header + 20-byte DX10 extension
     words[0] = fourcc('D', 'D', 'S', ' ');
     words[1] = 124;
@@ -626,13 +649,16 @@ bool dds_header(Format format, int w, int h, int mipmapCount, bool isNormalMap, 
     reserved[10] = (2u << 16) | (1u << 8) | 2u;     // the reference writes its own version, 2.1.2
     uint32_t *pf = &words[19];                      // size, flags, fourcc, bitcount, r, g, b, a masks
     pf[0] = 32;
-    uint32_t caps1 = CAPS_TEXTURE;
+    // a cube map is a complex surface with all six faces present, even with a single level
+    uint32_t caps1 = CAPS_TEXTURE | (cube ? CAPS_COMPLEX : 0u);
     if (mipmapCount > 1) { flags |= MIPMAPCOUNT; words[7] = (uint32_t)mipmapCount; caps1 |= CAPS_COMPLEX | CAPS_MIPMAP; }
     else words[7] = 1;
     words[27] = caps1;
+    words[28] = cube ? CAPS2_CUBEMAP | CAPS2_ALL_FACES : 0u;
     uint32_t *h10 = &words[32];                     // dxgiFormat, dimension, miscFlag, arraySize, reserved
     h10[1] = 3;                                     // DDS_DIMENSION_TEXTURE2D
-    h10[3] = 1;
+    h10[2] = cube ? 4u : 0u;                        // DDS_RESOURCE_MISC_TEXTURECUBE
+    h10[3] = type == TextureType_Array ? (uint32_t)arraySize : 1u;  // only the DX10 extension records layers
     if (oo.container == Container_DDS10) {
         pf[1] = PF_FOURCC;
         pf[2] = fourcc('D', 'X', '1', '0');
@@ -676,12 +702,15 @@ struct Compressor::Private {
                       const CompressionOptions::Private &co, const OutputOptions::Private &oo) const {
         if (w <= 0 || h <= 0 || d <= 0 || arraySize <= 0 || mipmapCount <= 0) { oo.error(Error_InvalidInput); return false; }
         if (!oo.outputHeader) return true;
-        if (oo.container == Container_KTX || type != TextureType_2D || d != 1 || arraySize != 1) {
+        // 3D textures and KTX files are outside the GPU path. The reference asserts (nvCheck) that a 2D
+        // texture or a cube map has an array size of 1; here that is refused as invalid input.
+        if (oo.container == Container_KTX || type == TextureType_3D || d != 1) {
             oo.error(Error_UnsupportedFeature);
             return false;
         }
+        if (type != TextureType_Array && arraySize != 1) { oo.error(Error_InvalidInput); return false; }
         std::vector<uint32_t> words;
-        if (!dds_header(co.format, w, h, mipmapCount, isNormalMap, oo, words)) {
+        if (!dds_header(co.format, type, w, h, arraySize, mipmapCount, isNormalMap, oo, words)) {
             oo.error(Error_UnsupportedOutputFormat);
             return false;
         }
@@ -738,10 +767,8 @@ int Compressor::estimateSize(const Surface &img, int mipmapCount, const Compress
 }
 // Compressor::estimateSize(InputOptions) (src/nvtt/Context.cpp:122-137), at the target extent.
 int Compressor::estimateSize(const InputOptions &io, const CompressionOptions &co) const {
-    int w = io.m.width, h = io.m.height;
-    if (w <= 0 || h <= 0 || ntg_target_extent(io.m.width, io.m.height, io.m.maxExtent, (int)io.m.roundMode, &w, &h) != NTG_OK ||
-        w <= 0 || h <= 0)
-        return 0;
+    int w = 0, h = 0;
+    if (!target_extent(io.m, &w, &h) || w <= 0 || h <= 0) return 0;
     int mc = io.m.generateMipmaps ? count_mipmaps(w, h) : 1;
     if (io.m.generateMipmaps && io.m.maxLevel > 0) mc = std::min(mc, io.m.maxLevel);
     return io.m.faceCount * estimateSize(w, h, io.m.depth, mc, co);
@@ -779,8 +806,8 @@ bool Compressor::process(const InputOptions &inputOptions, const CompressionOpti
     if (!oo.hasValidOutputHandler()) { oo.error(Error_FileOpen); return false; }
     if (!m.ctx) { oo.error(Error_CudaError); return false; }
     // the InputOptions resize step: nv::getTargetExtent, then Surface::resize(box) of level 0
-    int w = io.width, h = io.height;
-    if (io.width <= 0 || io.height <= 0 || ntg_target_extent(io.width, io.height, io.maxExtent, (int)io.roundMode, &w, &h) != NTG_OK) {
+    int w = 0, h = 0;
+    if (!target_extent(io, &w, &h)) {
         oo.error(Error_InvalidInput);
         return false;
     }
@@ -790,12 +817,14 @@ bool Compressor::process(const InputOptions &inputOptions, const CompressionOpti
         mipmapCount = count_mipmaps(w, h);
         if (io.maxLevel > 0) mipmapCount = std::min(mipmapCount, io.maxLevel);
     }
-    if (!m.outputHeader(io.textureType, w, h, io.depth, 1, mipmapCount, io.isNormalMap, co, oo)) return false;
+    // an array's layers are counted in the header; cube faces and 2D images are not
+    const int arraySize = io.textureType == TextureType_Array ? io.faceCount : 1;
+    if (!m.outputHeader(io.textureType, w, h, io.depth, arraySize, mipmapCount, io.isNormalMap, co, oo)) return false;
     // (an extent rounded to 0, ToPreviousMultipleOfFour below 4 texels, fails in outputHeader with
     // Error_InvalidInput, as in the reference)
-    // outside this path: normal-map generation / renormalisation, dithering, 3D/cube
+    // outside this path: normal-map generation / renormalisation, dithering, 3D textures
     const bool normalMips = io.isNormalMap && io.normalizeMipmaps && mipmapCount > 1;
-    if (io.textureType != TextureType_2D || io.depth != 1 || io.convertToNormalMap || normalMips ||
+    if (io.textureType == TextureType_3D || io.depth != 1 || io.convertToNormalMap || normalMips ||
         co.colorDithering || co.alphaDithering || co.binaryAlpha || ntg_format(co.format) < 0) {
         oo.error(Error_UnsupportedFeature);
         return false;

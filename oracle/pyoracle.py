@@ -475,14 +475,18 @@ class Reference:
 
     def process_ex(self, data, w, h, fmt, input_format=0, nsrc_levels=1, quality=1, mip_filter=0, alpha_mode=0,
                    wrap=2, max_level=-1, header=True, kaiser=(3.0, 4.0, 1.0), gamma=(2.2, 2.2), cw=(1, 1, 1, 1),
-                   container=0, srgb=0, version=0, normal_map=0, normalize_mips=1, max_extent=0, round_mode=0):
-        """Compressor::process with containers, flags, Kaiser parameters, source mipmaps and float
-        input; returns the bytes, or the negative nvtt::Error - 100 on failure."""
+                   container=0, srgb=0, version=0, normal_map=0, normalize_mips=1, max_extent=0, round_mode=0,
+                   texture_type=0, layers=1):
+        """Compressor::process with containers, flags, Kaiser parameters, source mipmaps, float
+        input, cube maps (texture_type 1) and arrays (3, `layers` images); returns the bytes, or the
+        negative nvtt::Error - 100 on failure."""
         b = np.ascontiguousarray(data).view(np.uint8)
         opts = np.array(list(kaiser) + list(gamma) + list(cw), np.float32)
-        flags = np.array([container, srgb, version, normal_map, normalize_mips, max_extent, round_mode], np.int32)
+        flags = np.array([container, srgb, version, normal_map, normalize_mips, max_extent, round_mode, texture_type,
+                          layers], np.int32)
         side = 1 << (max(w, h) - 1).bit_length()  # rounding modes may grow the extents up to the next power of two
-        cap = 16 * Oracle.nblocks(side, side) * 2 + 4096
+        faces = 6 if texture_type == 1 else (layers if texture_type == 3 else 1)
+        cap = faces * 16 * Oracle.nblocks(side, side) * 2 + 4096
         out = np.zeros(cap, np.uint8)
         n = self._process_ex(_ptr(b), w, h, input_format, nsrc_levels, fmt, quality, mip_filter, alpha_mode, wrap,
                              max_level, int(header), _ptr(opts), _ptr(flags), _ptr(out), cap)

@@ -358,26 +358,30 @@ long long ref_process(const unsigned char * bgra, int w, int h, int format, int 
     return copy_out(mem.bytes, out, cap);
 }
 
-// Compressor::process with the rest of the options the GPU drop-in mirrors. `data` holds
-// `nsrc_levels` source levels back to back (largest first) in `input_format` (0 BGRA8, 1 RGBA16F,
-// 2 RGBA32F, interleaved); opts[] = {kaiser width, kaiser alpha, kaiser stretch, in gamma,
-// out gamma, colour weights r, g, b, a}; flags[] = {container, srgb, user version, normal map,
-// normalize mipmaps}.
+// Compressor::process with the rest of the options the GPU drop-in mirrors. `data` holds, for each
+// face (cube map) or layer (array), `nsrc_levels` source levels back to back (largest first) in
+// `input_format` (0 BGRA8, 1 RGBA16F, 2 RGBA32F, interleaved); opts[] = {kaiser width, kaiser alpha,
+// kaiser stretch, in gamma, out gamma, colour weights r, g, b, a}; flags[] = {container, srgb, user
+// version, normal map, normalize mipmaps, max extent, round mode, texture type, layers}.
 long long ref_process_ex(const void * data, int w, int h, int input_format, int nsrc_levels,
                          int format, int quality, int mip_filter, int alpha_mode, int wrap,
                          int max_level, int header, const float * opts, const int * flags,
                          unsigned char * out, long long cap) {
     InputOptions io;
-    io.setTextureLayout(TextureType_2D, w, h);
+    const TextureType type = (TextureType)flags[7];
+    const int faces = type == TextureType_Cube ? 6 : (type == TextureType_Array ? flags[8] : 1);
+    io.setTextureLayout(type, w, h, 1, type == TextureType_Array ? faces : 1);
     io.setFormat((InputFormat)input_format);
     const int bpp = input_format == 0 ? 4 : (input_format == 1 ? 8 : 16);
     const unsigned char * p = (const unsigned char *)data;
-    int lw = w, lh = h;
-    for (int l = 0; l < nsrc_levels; l++) {
-        io.setMipmapData(p, lw, lh, 1, 0, l);
-        p += (size_t)lw * lh * bpp;
-        lw = lw > 1 ? lw / 2 : 1;
-        lh = lh > 1 ? lh / 2 : 1;
+    for (int f = 0; f < faces; f++) {
+        int lw = w, lh = h;
+        for (int l = 0; l < nsrc_levels; l++) {
+            io.setMipmapData(p, lw, lh, 1, f, l);
+            p += (size_t)lw * lh * bpp;
+            lw = lw > 1 ? lw / 2 : 1;
+            lh = lh > 1 ? lh / 2 : 1;
+        }
     }
     io.setAlphaMode((AlphaMode)alpha_mode);
     io.setWrapMode((WrapMode)wrap);

@@ -79,17 +79,22 @@ int main(int argc, char **argv) {
     if (!input) return 2;
 
     NvttInputOptions *io = nvttCreateInputOptions();
-    nvttSetInputOptionsTextureLayout(io, NVTT_TextureType_2D, w, h, 1, 1);
+    /* type=0 2D, 1 cube map (six faces), 3 array of `layers` images, face by face in the input */
+    const NvttTextureType type = (NvttTextureType)(int)num("type", 0);
+    const int faces = type == NVTT_TextureType_Cube ? 6 : (type == TextureType_Array ? (int)num("layers", 1) : 1);
+    nvttSetInputOptionsTextureLayout(io, type, w, h, 1, type == TextureType_Array ? faces : 1);
     nvttSetInputOptionsFormat(io, (NvttInputFormat)in_format);
     const size_t bpp = in_format == NVTT_InputFormat_BGRA_8UB ? 4 : (in_format == NVTT_InputFormat_RGBA_16F ? 8 : 16);
     size_t off = 0;
-    int lw = w, lh = h;
-    for (int l = 0; l < nsrc; l++) {
-        if (off + (size_t)lw * lh * bpp > in_len) return 2;
-        if (nvttSetInputOptionsMipmapData(io, input + off, lw, lh, 1, 0, l) != NVTT_True) return 2;
-        off += (size_t)lw * lh * bpp;
-        lw = lw > 1 ? lw / 2 : 1;
-        lh = lh > 1 ? lh / 2 : 1;
+    for (int f = 0; f < faces; f++) {
+        int lw = w, lh = h;
+        for (int l = 0; l < nsrc; l++) {
+            if (off + (size_t)lw * lh * bpp > in_len) return 2;
+            if (nvttSetInputOptionsMipmapData(io, input + off, lw, lh, 1, f, l) != NVTT_True) return 2;
+            off += (size_t)lw * lh * bpp;
+            lw = lw > 1 ? lw / 2 : 1;
+            lh = lh > 1 ? lh / 2 : 1;
+        }
     }
     nvttSetInputOptionsAlphaMode(io, (NvttAlphaMode)(int)num("alpha", 0));
     nvttSetInputOptionsWrapMode(io, (NvttWrapMode)(int)num("wrap", 2));

@@ -109,20 +109,28 @@ int main(int argc, char **argv) {
     }
 
     if (mode == "header") {
-        if (!compressor.outputHeader(nvtt::TextureType_2D, w, h, 1, 1, mipmapCount, normal, co, oo)) return fail(err);
+        const nvtt::TextureType type = (nvtt::TextureType)(int)num("type", 0);
+        const int arraySize = type == nvtt::TextureType_Array ? (int)num("layers", 1) : 1;
+        if (!compressor.outputHeader(type, w, h, 1, arraySize, mipmapCount, normal, co, oo)) return fail(err);
     } else if (mode == "process") {
+        // type=0 2D, 1 cube map (six faces), 3 array of `layers` images; the input holds each face's
+        // (or layer's) source levels, face by face
         nvtt::InputOptions io;
-        io.setTextureLayout(nvtt::TextureType_2D, w, h);
+        const nvtt::TextureType type = (nvtt::TextureType)(int)num("type", 0);
+        const int faces = type == nvtt::TextureType_Cube ? 6 : (type == nvtt::TextureType_Array ? (int)num("layers", 1) : 1);
+        io.setTextureLayout(type, w, h, 1, type == nvtt::TextureType_Array ? faces : 1);
         io.setFormat(inFormat);
         const size_t bpp = inFormat == nvtt::InputFormat_BGRA_8UB ? 4 : (inFormat == nvtt::InputFormat_RGBA_16F ? 8 : 16);
         size_t off = 0;
-        int lw = w, lh = h;
-        for (int l = 0; l < nsrc; l++) {
-            if (off + (size_t)lw * lh * bpp > input.size()) { std::fprintf(stderr, "short input\n"); return 2; }
-            if (!io.setMipmapData(input.data() + off, lw, lh, 1, 0, l)) { std::fprintf(stderr, "setMipmapData\n"); return 2; }
-            off += (size_t)lw * lh * bpp;
-            lw = lw > 1 ? lw / 2 : 1;
-            lh = lh > 1 ? lh / 2 : 1;
+        for (int f = 0; f < faces; f++) {
+            int lw = w, lh = h;
+            for (int l = 0; l < nsrc; l++) {
+                if (off + (size_t)lw * lh * bpp > input.size()) { std::fprintf(stderr, "short input\n"); return 2; }
+                if (!io.setMipmapData(input.data() + off, lw, lh, 1, f, l)) { std::fprintf(stderr, "setMipmapData\n"); return 2; }
+                off += (size_t)lw * lh * bpp;
+                lw = lw > 1 ? lw / 2 : 1;
+                lh = lh > 1 ? lh / 2 : 1;
+            }
         }
         io.setAlphaMode((nvtt::AlphaMode)(int)num("alpha", 0));
         io.setWrapMode((nvtt::WrapMode)(int)num("wrap", 2));

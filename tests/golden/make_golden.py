@@ -185,6 +185,12 @@ DDS_CASES = [
     dict(w=30, h=18, format=2, quality=1, round_mode=2, alpha_mode=1),                  # 32 x 16
     dict(w=45, h=27, format=4, quality=1, round_mode=5, max_level=1),                   # unchanged (reference quirk)
     dict(w=3, h=9, format=1, quality=1, round_mode=6),                                  # width 0: rejected
+    # cube maps (six faces, each a whole chain, face by face) and texture arrays
+    dict(w=32, h=32, format=1, quality=1, mip_filter=2, texture_type=1),
+    dict(w=24, h=24, format=4, quality=1, mip_filter=1, alpha_mode=1, texture_type=1, container=1, srgb=1),
+    dict(w=40, h=24, format=7, quality=1, texture_type=1, max_extent=16, round_mode=1),   # (40+24)/2 -> 16
+    dict(w=20, h=12, format=4, quality=1, mip_filter=2, texture_type=3, layers=3, container=1),
+    dict(w=16, h=16, format=1, quality=2, texture_type=3, layers=2),                    # array in a DDS9 file
 ]
 
 
@@ -193,17 +199,20 @@ def dds_input(i, case):
     w, h = case["w"], case["h"]
     levels = pyoracle.level_sizes(w, h)[:case.get("nsrc_levels", 1)]
     fmt = case.get("input_format", 0)
+    tt = case.get("texture_type", 0)
+    faces = 6 if tt == 1 else (case.get("layers", 1) if tt == 3 else 1)
     parts = []
-    for j, (lw, lh) in enumerate(levels):
-        rng = np.random.default_rng(9000 + 10 * i + j)
-        img = synth.colour_texture(lw, lh, 900 + 10 * i + j, scale=0.2,
-                                   alpha=rng.integers(0, 256, (lh, lw)).astype(np.uint8))
-        if fmt == 0:
-            parts.append(img.reshape(-1))
-        else:
-            rgba = img[..., [2, 1, 0, 3]].astype(np.float32) / 255.0 + rng.normal(0, 0.01, (lh, lw, 4)).astype(np.float32)
-            rgba = np.clip(rgba, 0, 1).astype(np.float32)
-            parts.append((rgba.astype(np.float16) if fmt == 1 else rgba).reshape(-1).view(np.uint8))
+    for f in range(faces):  # face (or layer) by face, each with its source levels
+        for j, (lw, lh) in enumerate(levels):
+            s = 9000 + 10 * i + j + 100 * f
+            rng = np.random.default_rng(s)
+            img = synth.colour_texture(lw, lh, s - 8100, scale=0.2, alpha=rng.integers(0, 256, (lh, lw)).astype(np.uint8))
+            if fmt == 0:
+                parts.append(img.reshape(-1))
+            else:
+                rgba = img[..., [2, 1, 0, 3]].astype(np.float32) / 255.0 + rng.normal(0, 0.01, (lh, lw, 4)).astype(np.float32)
+                rgba = np.clip(rgba, 0, 1).astype(np.float32)
+                parts.append((rgba.astype(np.float16) if fmt == 1 else rgba).reshape(-1).view(np.uint8))
     return np.concatenate(parts)
 
 

@@ -35,7 +35,7 @@ def harness_args(c, **extra):
     names = dict(w="w", h="h", format="format", quality="quality", mip_filter="filter", alpha_mode="alpha",
                  wrap="wrap", max_level="max_level", container="container", srgb="srgb", version="version",
                  normal_map="normal", normalize_mips="normalize", input_format="input_format", nsrc_levels="nsrc",
-                 max_extent="max_extent", round_mode="round_mode")
+                 max_extent="max_extent", round_mode="round_mode", texture_type="type", layers="layers")
     args = {}
     for k, v in c.items():
         if k in names:
@@ -95,12 +95,23 @@ def test_harness_compiles_and_links(harness):
 
 
 def target_args(i):
-    """For a case with the InputOptions resize step: the extents the header carries (nv::getTargetExtent)."""
+    """For a case with the InputOptions resize step: the extents the header carries (nv::getTargetExtent,
+    src/nvtt/Surface.cpp:220-283: a cube map's faces become square at the mean of the scaled extents)."""
     import ntg
     c = case(i)
-    if not c.get("max_extent") and not c.get("round_mode"):
+    max_extent, round_mode = c.get("max_extent", 0), c.get("round_mode", 0)
+    if c.get("texture_type", 0) == 1:
+        if round_mode and max_extent > 0:
+            max_extent = 1 << (max_extent.bit_length() - 1)
+        w, h = c["w"], c["h"]
+        m = max(w, h)
+        if max_extent > 0 and m > max_extent:
+            w, h = max(w * max_extent // m, 1), max(h * max_extent // m, 1)
+        w, h = ntg.target_extent((w + h) // 2, (w + h) // 2, 0, round_mode)
+        return dict(w=w, h=h, max_extent=0, round_mode=0)
+    if not max_extent and not round_mode:
         return {}
-    w, h = ntg.target_extent(c["w"], c["h"], c.get("max_extent", 0), c.get("round_mode", 0))
+    w, h = ntg.target_extent(c["w"], c["h"], max_extent, round_mode)
     return dict(w=w, h=h, max_extent=0, round_mode=0)
 
 
@@ -145,8 +156,8 @@ def test_process_matches_reference(harness, tmp_path, i):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("i", [i for i in range(NCASES)
-                               if expected_error(i) is None and case(i).get("nsrc_levels", 1) == 1])
+@pytest.mark.parametrize("i", [i for i in range(NCASES) if expected_error(i) is None and
+                               case(i).get("nsrc_levels", 1) == 1 and case(i).get("texture_type", 0) == 0])
 def test_surface_loop_matches_reference(harness, tmp_path, i):
     """The imperative Surface API loop writes the same file as Compressor::process."""
     rc, log, data = run(harness, "surface", i, tmp_path)
