@@ -64,7 +64,9 @@ extern "C" {
 typedef struct ntg_context ntg_context;
 
 /* Per-device state: constant tables, a grow-only scratch workspace and staging buffers.
- * Replaces the reference's CudaContext (src/nvtt/Context.cpp:81-98). */
+ * Replaces the reference's CudaContext (src/nvtt/Context.cpp:81-98). The first context on a device
+ * also builds that device's sRGB correction tables (about 55 MB of device memory, held until exit);
+ * later contexts on the device allocate nothing until their first call that needs scratch. */
 int ntg_create(int device, ntg_context **out);
 int ntg_destroy(ntg_context *ctx);
 const char *ntg_last_error_string(void);
@@ -133,8 +135,9 @@ int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, 
  * loading this library holds until exit; levels above NTG_NOALLOC_MAX_TEXELS texels are rejected
  * with NTG_ERROR_INVALID_INPUT. The first call on a device looks up the array's device address
  * (make it before any stream capture). All calls share the array: calls that overlap on the GPU
- * race, so issue them on one stream. The context must come from ntg_create (which allocates nothing
- * on the device); same arguments and results as ntg_encode. */
+ * race, so issue them on one stream. The context must come from ntg_create (whose allocations, the
+ * per-device sRGB tables, happen there, before any frame loop); same arguments and results as
+ * ntg_encode. */
 #define NTG_NOALLOC_MAX_TEXELS 1048576
 #define NTG_NOALLOC_SCRATCH_BYTES (4 * NTG_NOALLOC_MAX_TEXELS + 2048)
 int ntg_encode_noalloc(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,

@@ -29,6 +29,20 @@ struct LaneW {
     __device__ __forceinline__ float &operator[](int k) const { return base[(k >> 2) * stride + (k & 3)]; }
 };
 
+// One thread's 16 weights derived from its gathered texels when they are read: saturate(alpha)
+// under AlphaMode_Transparency, else 1, and 0 for the texels outside the image (bit k of `valid`
+// clear). It needs no storage of its own, and reads right while the slots hold the gathered texels:
+// reduce_colors reads slot k's weight before it writes there, and the output stage gathers again.
+struct AlphaW {
+    const float4 *base;  // this thread's first slot
+    int stride;          // float4 between consecutive slots of one thread
+    bool transparency;
+    uint32_t valid;
+    __device__ __forceinline__ float operator[](int k) const {
+        return ((valid >> k) & 1u) ? (transparency ? ic_clamp(base[k * stride].w, 0.0f, 1.0f) : 1.0f) : 0.0f;
+    }
+};
+
 // The device's toSrgb correction table (set once per device when a context is created).
 static __device__ const uint8_t *g_to_srgb_fix;
 
@@ -554,6 +568,20 @@ __device__ __forceinline__ int find_job(const EncJob *jobs, int njobs, long long
 }
 
 
+__device__ __forceinline__ void put_weight(const LaneW &w, int k, float v) { w[k] = v; }
+__device__ __forceinline__ void put_weight(const Lane<float> &w, int k, float v) { w[k] = v; }
+__device__ __forceinline__ void put_weight(const AlphaW &, int, float) {}  // derived when read
+
+// Bit 4y + x set for the texels (x, y) of block `blk` that lie inside the image.
+__device__ __forceinline__ uint32_t valid_texels(const EncJob &J, int blk) {
+    const int bx = blk % J.bw, by = blk / J.bw;
+    const int vw = min(J.w - bx * 4, 4), vh = min(J.h - by * 4, 4);
+    const uint32_t row = (1u << vw) - 1u;
+    uint32_t m = 0;
+    for (int y = 0; y < vh; y++) m |= row << (4 * y);
+    return m;
+}
+
 // FloatColorCompressorTask gather (src/nvtt/BlockCompressor.cpp:116-166): the block's 16 texels
 // after the output transform, weight saturate(alpha) under AlphaMode_Transparency, texels outside
 // the image at weight 0.
@@ -581,10 +609,10 @@ __device__ __forceinline__ void gather_block(const EncJob &J, int blk, const Lan
                     else if (J.out_xform == 2) { r = to_srgb(r); g = to_srgb(g); b = to_srgb(b); }
                 }
                 in[k] = make_float4(r, g, b, al);
-                wi[k] = J.alpha_mode == 1 ? ic_clamp(al, 0.0f, 1.0f) : 1.0f;
+                put_weight(wi, k, J.alpha_mode == 1 ? ic_clamp(al, 0.0f, 1.0f) : 1.0f);
             } else {
                 in[k] = make_float4(0, 0, 0, 0);
-                wi[k] = 0.0f;
+                put_weight(wi, k, 0.0f);
             }
         }
 }
@@ -645,15 +673,15 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     }
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
-    // 20 float4 slots per thread: the texels (16), then the weights packed in 4. The reduced colours
-    // overwrite the texels in place (reduce_colors only writes slots it has already read), the
-    // summed-area table overwrites the colours in place with a zero entry first (17 entries: the
-    // last takes the first weight slot, whose weights are dead during the fits), and the texels
-    // and weights are gathered again for the output stage once the cluster fits are done.
+    // 17 float4 slots per thread: the texels (16) and one more. The weights are derived from the
+    // texels when read (AlphaW). The reduced colours overwrite the texels in place (reduce_colors
+    // only writes slots it has already read), the summed-area table overwrites the colours in place
+    // with a zero entry first (17 entries), and the texels are gathered again for the output stage
+    // once the cluster fits are done.
     Lane<float4> in{smem + t, T};
     Lane<float4> col = in;
     Lane<float4> sat = in;
-    LaneW wi{reinterpret_cast<float *>(smem + 16 * T + t), 4 * T};
+    const AlphaW wi{smem + t, T, J.alpha_mode == 1, valid_texels(J, blk)};
     const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
     uint8_t *const out = J.out + 8 * (size_t)blk;
 
@@ -1131,11 +1159,11 @@ __global__ void __launch_bounds__(64) k_bc1_learned(const EncJob *__restrict__ j
     const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
     const int blk = (int)(gblk - J.first_block);
     // the layout of k_bc1: colours reduced over the texels in place, the ZERO SAT built over the
-    // colours in place, texels and weights gathered again for the output stage
+    // colours in place, texels gathered again for the output stage, weights derived from the texels
     Lane<float4> in{smem + t, T};
     Lane<float4> col = in;
     Lane<float4> sat = in;
-    LaneW wi{reinterpret_cast<float *>(smem + 16 * T + t), 4 * T};
+    const AlphaW wi{smem + t, T, J.alpha_mode == 1, valid_texels(J, blk)};
     const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
     uint8_t *const out = J.out + 8 * (size_t)blk;
     gather_block(J, blk, in, wi);
@@ -1247,9 +1275,11 @@ __global__ void __launch_bounds__(64) k_bc1_work(const EncJob *__restrict__ jobs
     }
 }
 
-// Shared memory of k_bc1: per thread the texels (then the reduced colours, then the SAT) and the
-// weights.
-static size_t bc1_fit_smem(int T) { return (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float)); }
+// Shared memory of k_bc1 and k_bc1_learned: per thread 17 float4 slots, the texels, then the
+// reduced colours, then the SAT (its weights are derived from the texels).
+static size_t bc1_fit_smem(int T) { return (size_t)T * 17 * sizeof(float4); }
+// k_bc1_work: per thread the texels and 16 stored weights.
+static size_t bc1_work_smem(int T) { return (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float)); }
 
 int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
@@ -1307,7 +1337,7 @@ int launch_bc1_learned(const EncJob *d_jobs, int njobs, long long nblocks, const
 int launch_bc1_work(const EncJob *d_jobs, int njobs, long long nblocks, unsigned long long *work, cudaStream_t s) {
     if (nblocks == 0) return 0;
     const int T = 64;
-    k_bc1_work<<<(unsigned)((nblocks + T - 1) / T), T, bc1_fit_smem(T), s>>>(d_jobs, njobs, nblocks, work);
+    k_bc1_work<<<(unsigned)((nblocks + T - 1) / T), T, bc1_work_smem(T), s>>>(d_jobs, njobs, nblocks, work);
     return launch_status();
 }
 
