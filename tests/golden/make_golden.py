@@ -191,6 +191,9 @@ DDS_CASES = [
     dict(w=40, h=24, format=7, quality=1, texture_type=1, max_extent=16, round_mode=1),   # (40+24)/2 -> 16
     dict(w=20, h=12, format=4, quality=1, mip_filter=2, texture_type=3, layers=3, container=1),
     dict(w=16, h=16, format=1, quality=2, texture_type=3, layers=2),                    # array in a DDS9 file
+    dict(w=16, h=16, format=4, quality=1, mip_filter=1, alpha_mode=1, texture_type=1, nsrc_levels=2),  # faces' own mips
+    dict(w=12, h=20, format=1, quality=1, texture_type=3, layers=2, input_format=2, container=1, srgb=1),
+    dict(w=8, h=8, format=7, quality=1, texture_type=1, max_level=1),                   # one level: no mipmap caps
 ]
 
 
