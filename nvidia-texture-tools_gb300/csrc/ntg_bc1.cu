@@ -787,6 +787,139 @@ __global__ void __launch_bounds__(64) k_bc1(const EncJob *__restrict__ jobs, int
     store_block(out, o);
 }
 
+// The first strict minimum of a search split over the K lanes of a group, lane j having taken the
+// orderings i = j (mod K) with its own first strict minimum (e, i) (FLT_MAX, -1 when none): the
+// smallest error, and among equal errors the smallest ordering - the ordering the sequential search
+// keeps. Every lane of the group returns it.
+template <int K>
+__device__ __forceinline__ int group_first_min(unsigned gmask, float e, int i) {
+#pragma unroll
+    for (int off = K / 2; off > 0; off >>= 1) {
+        const float eo = __shfl_xor_sync(gmask, e, off, K);
+        const int io = __shfl_xor_sync(gmask, i, off, K);
+        if (eo < e || (eo == e && io < i)) { e = eo; i = io; }
+    }
+    return i;
+}
+
+// cluster_fit_four / cluster_fit_three over a ZERO table, lane j of K evaluating the orderings
+// j, j + K, ... of the icbc tables (listed in the sequential search's order); returns the group's best
+// ordering (-1 when none).
+template <int K>
+__device__ int split_fit_four(unsigned gmask, const Lane<float4> &sat, int n, f3 metric, int j) {
+    const float4 s = sat[n];
+    const f3 sum = xyz(s);
+    float best = FLT_MAX;
+    int bi = -1;
+    const int total = c_tab.four_total[n - 1];
+    for (int i = j; i < total; i += K) {
+        f3 a, b;
+        const float e = four_eval<true>(sat, c_tab.four[i], sum, s.w, metric, a, b);
+        if (e < best) { best = e; bi = i; }
+    }
+    return group_first_min<K>(gmask, best, bi);
+}
+template <int K>
+__device__ int split_fit_three(unsigned gmask, const Lane<float4> &sat, int n, f3 metric, int j) {
+    const float4 s = sat[n];
+    const f3 sum = xyz(s);
+    float best = FLT_MAX;
+    int bi = -1;
+    const int total = c_tab.three_total[n - 1];
+    for (int i = j; i < total; i += K) {
+        f3 a, b;
+        const float e = three_eval<true>(sat, c_tab.three[i], sum, s.w, metric, a, b);
+        if (e < best) { best = e; bi = i; }
+    }
+    return group_first_min<K>(gmask, best, bi);
+}
+
+// k_bc1 for launches too small to fill the GPU with one thread per block: a group of K lanes of one
+// warp encodes each block (64 / K blocks per 64-thread CTA). The group's first lane gathers, reduces
+// and builds the summed-area table, in 17 float4 slots of shared memory per block; the K lanes split
+// the orderings of each cluster fit; the first lane recomputes the winners' endpoints and runs the
+// output stage. The same operations on the same values as k_bc1, so the same blocks.
+template <int LEVEL, int K>
+__global__ void __launch_bounds__(64) k_bc1_split(const EncJob *__restrict__ jobs, int njobs, long long nblocks) {
+    extern __shared__ float4 smem[];
+    constexpr int G = 64 / K;  // blocks per CTA
+    const int t = threadIdx.x, g = t / K, j = t % K;
+    const long long gblk = (long long)blockIdx.x * G + g;
+    if (gblk >= nblocks) return;  // the whole group leaves together
+    const unsigned gmask = ((1u << K) - 1u) << ((t & 31) & ~(K - 1));
+    const EncJob &J = jobs[find_job(jobs, njobs, gblk)];
+    const int blk = (int)(gblk - J.first_block);
+    Lane<float4> in{smem + 17 * g, 1};  // one block's slots, consecutive: the lanes read different ones
+    Lane<float4> col = in;
+    Lane<float4> sat = in;
+    const AlphaW wi{smem + 17 * g, 1, J.alpha_mode == 1, valid_texels(J, blk)};
+    const f3 cw = mk3(J.cw[0], J.cw[1], J.cw[2]);
+    const f3 metric = cw * cw;
+    uint8_t *const out = J.out + 8 * (size_t)blk;
+
+    int cnt = 0, sn = 0, black = 0;
+    if (j == 0) {
+        gather_block(J, blk, in, wi);
+        bool any_black = false;
+        cnt = reduce_colors(in, wi, col, any_black);
+        black = any_black;
+        if (cnt == 0) store_block(out, Block1{0, 0, 0});
+        else if (cnt == 1) store_block(out, single_colour(col[0]));
+        else sn = compute_sat_inplace(col, cnt);
+    }
+    cnt = __shfl_sync(gmask, cnt, 0, K);
+    if (cnt <= 1) return;
+    sn = __shfl_sync(gmask, sn, 0, K);
+    black = __shfl_sync(gmask, black, 0, K);
+    __syncwarp(gmask);  // the table is written
+
+    f3 s0 = mk3(0, 0, 0), s1 = mk3(0, 0, 0), t0 = mk3(0, 0, 0), t1 = mk3(0, 0, 0);
+    const int b4 = split_fit_four<K>(gmask, sat, sn, metric, j);
+    int run3 = 1;
+    if (j == 0) {
+        if (b4 >= 0) four_eval<true>(sat, c_tab.four[b4], xyz(sat[sn]), sat[sn].w, metric, s0, s1);
+    }
+    __syncwarp(gmask);  // every lane is done with the table
+    if (black) {
+        if (j == 0) {
+            // the table has replaced the colours: reduce them again, then keep the non-black ones
+            gather_block(J, blk, in, wi);
+            bool again = false;
+            reduce_colors(in, wi, col, again);
+            int m = 0;
+            for (int i = 0; i < cnt; i++) {
+                float4 q = col[i];
+                if (is_black(xyz(q))) continue;
+                col[m++] = q;
+            }
+            if (m == 0) run3 = 0;
+            else sn = compute_sat_inplace(col, m);
+        }
+        run3 = __shfl_sync(gmask, run3, 0, K);
+        sn = __shfl_sync(gmask, sn, 0, K);
+        __syncwarp(gmask);
+    }
+    if (run3) {
+        const int b3 = split_fit_three<K>(gmask, sat, sn, metric, j);
+        if (j == 0 && b3 >= 0) three_eval<true>(sat, c_tab.three[b3], xyz(sat[sn]), sat[sn].w, metric, t0, t1);
+        __syncwarp(gmask);
+    }
+    if (j != 0) return;
+    gather_block(J, blk, in, wi);
+    Block1 o{0, 0, 0};
+    float err = FLT_MAX;
+    Block1 cf;
+    float cerr = output_block4(in, wi, cw, s0, s1, cf);
+    if (run3) {
+        Block1 c3;
+        const float e3 = output_block3(in, wi, cw, true, t0, t1, c3);
+        if (e3 < cerr) { cerr = e3; cf = c3; }
+    }
+    if (cerr < err) { o = cf; err = cerr; }
+    if (LEVEL == 8) err = refine_endpoints(in, wi, cw, err, o);
+    store_block(out, o);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Learned endpoint proposal (no counterpart in the reference). The network reads a block's texels
 // and proposes its two endpoints and the error of the full cluster fit. The proposal's palette
@@ -1281,8 +1414,28 @@ static size_t bc1_fit_smem(int T) { return (size_t)T * 17 * sizeof(float4); }
 // k_bc1_work: per thread the texels and 16 stored weights.
 static size_t bc1_work_smem(int T) { return (size_t)T * (16 * sizeof(float4) + 16 * sizeof(float)); }
 
+// Blocks the one-thread-per-block fit keeps in flight on a full GB300 (152 SMs x 12 CTAs of 64).
+constexpr long long kBc1InFlight = 152LL * 12 * 64;
+
+template <int LEVEL, int K>
+static void launch_bc1_split(const EncJob *d_jobs, int njobs, long long nblocks, cudaStream_t stream) {
+    constexpr int G = 64 / K;
+    k_bc1_split<LEVEL, K><<<(unsigned)((nblocks + G - 1) / G), 64, (size_t)G * 17 * sizeof(float4), stream>>>(
+        d_jobs, njobs, nblocks);
+}
+
 int launch_bc1(const EncJob *d_jobs, int njobs, long long nblocks, int quality, int threads, cudaStream_t stream) {
     if (nblocks == 0) return 0;
+    if (quality != 0 && nblocks * 4 <= 2 * kBc1InFlight) {
+        // too few blocks to keep the SMs busy one thread each (a single 512x512 chain has 21,847):
+        // 8 or 4 lanes per block, for up to two waves of threads
+        const bool eight = nblocks * 8 <= 2 * kBc1InFlight;
+        if (quality == 2) eight ? launch_bc1_split<8, 8>(d_jobs, njobs, nblocks, stream)
+                                : launch_bc1_split<8, 4>(d_jobs, njobs, nblocks, stream);
+        else eight ? launch_bc1_split<7, 8>(d_jobs, njobs, nblocks, stream)
+                   : launch_bc1_split<7, 4>(d_jobs, njobs, nblocks, stream);
+        return launch_status();
+    }
     const int T = threads == 32 ? 32 : 64;  // blocks per CTA (one thread per 4x4 block)
     const size_t sm = bc1_fit_smem(T);
     const unsigned grid = (unsigned)((nblocks + T - 1) / T);
