@@ -4,7 +4,9 @@
 //   nvtt_harness <mode> <input file | -> <output file | -> key=value ...
 //
 // modes:
-//   process  InputOptions + Compressor::process (levels 0..nsrc-1 of the input file are source mipmaps)
+//   process  InputOptions + Compressor::process (levels 0..nsrc-1 of the input file are source mipmaps,
+//            for each face of a cube map (type=1) or layer of an array (type=3, layers=n) in turn)
+//   estimate the same InputOptions, Compressor::estimateSize only (no GPU work): prints "estimate=<n>"
 //   surface  the Surface loop: setImage, toLinear, {copy, toGamma, compress, buildNextMipmap}
 //   header   Compressor::outputHeader only (no GPU work)
 //   rms      BC-encode level 0, decode it with setImage2D, print rmsError / rmsAlphaError
@@ -65,7 +67,7 @@ int fail(const LastError &err) {
 
 int main(int argc, char **argv) {
     if (argc < 4) {
-        std::fprintf(stderr, "usage: nvtt_harness <process|surface|header|rms> <in> <out> key=value...\n");
+        std::fprintf(stderr, "usage: nvtt_harness <process|estimate|surface|header|rms> <in> <out> key=value...\n");
         return 2;
     }
     const std::string mode = argv[1];
@@ -112,7 +114,7 @@ int main(int argc, char **argv) {
         const nvtt::TextureType type = (nvtt::TextureType)(int)num("type", 0);
         const int arraySize = type == nvtt::TextureType_Array ? (int)num("layers", 1) : 1;
         if (!compressor.outputHeader(type, w, h, 1, arraySize, mipmapCount, normal, co, oo)) return fail(err);
-    } else if (mode == "process") {
+    } else if (mode == "process" || mode == "estimate") {
         // type=0 2D, 1 cube map (six faces), 3 array of `layers` images; the input holds each face's
         // (or layer's) source levels, face by face
         nvtt::InputOptions io;
@@ -143,6 +145,10 @@ int main(int argc, char **argv) {
         io.setMaxExtents((int)num("max_extent", 0));
         io.setRoundMode((nvtt::RoundMode)(int)num("round_mode", 0));
         estimate = compressor.estimateSize(io, co);
+        if (mode == "estimate") {  // the size process() would write after the header; needs no GPU
+            std::printf("estimate=%d\n", estimate);
+            return 0;
+        }
         if (!compressor.process(io, co, oo)) return fail(err);
     } else if (mode == "surface" || mode == "rms") {
         nvtt::Surface img;

@@ -129,6 +129,17 @@ def test_header_matches_reference(harness, tmp_path, i):
     np.testing.assert_array_equal(data, gold[:n])
 
 
+@pytest.mark.parametrize("i", [i for i in range(NCASES) if expected_error(i) is None])
+def test_estimate_size_matches_reference(harness, tmp_path, i):
+    """Compressor::estimateSize(InputOptions) (no GPU work) equals the size of what the reference's process
+    writes after the header: the target extent (a cube map's square faces included), the level count and
+    the faces or layers."""
+    rc, log, _ = run(harness, "estimate", i, tmp_path)
+    assert rc == 0, log
+    gold = GOLD[f"dds_{i}"]
+    assert int(log.split("estimate=")[1].split()[0]) == gold.size - header_size(gold)
+
+
 def test_process_fails_loudly_without_gpu(harness, tmp_path):
     if not no_gpu():
         pytest.skip("a GPU is present")
