@@ -100,6 +100,10 @@ int ntg_selftest_srgb_quantizer(ntg_context *ctx, unsigned long long *mismatches
  * Compressor::process resizes to for InputOptions::setMaxExtent / setRoundMode (round_mode is an
  * nvtt::RoundMode). A result may be 0 (ToPreviousMultipleOfFour below 4), as in the reference. */
 int ntg_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, int *out_h);
+/* The same for an nvtt::TextureType: 0 (2D) and 3 (array) as above; 1 (cube map) makes the faces
+ * square at the mean of the scaled extents before rounding (src/nvtt/Surface.cpp:248-252). 3D
+ * textures (2) are outside this path: NTG_ERROR_UNSUPPORTED_FEATURE. */
+int ntg_target_extent_ex(int w, int h, int max_extent, int round_mode, int texture_type, int *out_w, int *out_h);
 
 /* Surface::buildNextMipmap (src/nvtt/Surface.cpp:1344-1406): one level down from a planar FP32
  * level to max(1, w/2) x max(1, h/2). params = {kaiser alpha, kaiser stretch} (ignored otherwise).

@@ -916,13 +916,15 @@ int ntg_selftest_srgb_quantizer(ntg_context *ctx, unsigned long long *mismatches
     return r;
 }
 
-// nv::getTargetExtent (src/nvtt/Surface.cpp:220-326), 2D, no shape restriction, with the rounding
-// helpers of src/nvtt/Surface.cpp:60-105. Its else-if chain tests RoundMode_ToNextMultipleOfFour
-// twice, so RoundMode_ToNearestMultipleOfFour leaves the extents unchanged; kept that way.
-int ntg_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, int *out_h) {
+// nv::getTargetExtent (src/nvtt/Surface.cpp:220-326) for 2D textures, cube maps and arrays, no shape
+// restriction, with the rounding helpers of src/nvtt/Surface.cpp:60-105. Its else-if chain tests
+// RoundMode_ToNextMultipleOfFour twice, so RoundMode_ToNearestMultipleOfFour leaves the extents
+// unchanged; kept that way.
+int ntg_target_extent_ex(int w, int h, int max_extent, int round_mode, int texture_type, int *out_w, int *out_h) {
     g_error.clear();
-    if (w <= 0 || h <= 0 || !out_w || !out_h || round_mode < 0 || round_mode > 6)
+    if (w <= 0 || h <= 0 || !out_w || !out_h || round_mode < 0 || round_mode > 6 || texture_type < 0 || texture_type > 3)
         return fail(NTG_ERROR_INVALID_INPUT, "bad arguments");
+    if (texture_type == 2) return fail(NTG_ERROR_UNSUPPORTED_FEATURE, "3D textures are not supported");
     auto next_pow2 = [](unsigned x) {
         x--;
         x |= x >> 1; x |= x >> 2; x |= x >> 4; x |= x >> 8; x |= x >> 16;
@@ -939,6 +941,7 @@ int ntg_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, 
         w = std::max((w * max_extent) / m, 1);
         h = std::max((h * max_extent) / m, 1);
     }
+    if (texture_type == 1) w = h = (w + h) / 2;  // a cube map's faces are square
     if (round_mode == 1) { w = (int)next_pow2((unsigned)w); h = (int)next_pow2((unsigned)h); }
     else if (round_mode == 2) { w = (int)nearest_pow2((unsigned)w); h = (int)nearest_pow2((unsigned)h); }
     else if (round_mode == 3) { w = (int)prev_pow2((unsigned)w); h = (int)prev_pow2((unsigned)h); }
@@ -947,6 +950,10 @@ int ntg_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, 
     *out_w = w;
     *out_h = h;
     return NTG_OK;
+}
+
+int ntg_target_extent(int w, int h, int max_extent, int round_mode, int *out_w, int *out_h) {
+    return ntg_target_extent_ex(w, h, max_extent, round_mode, 0, out_w, out_h);
 }
 
 int ntg_encode(ntg_context *ctx, int format, const float *d_rgba, int w, int h, int quality, int alpha_mode,

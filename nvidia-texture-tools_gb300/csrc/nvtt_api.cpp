@@ -606,24 +606,12 @@ uint32_t fourcc(char a, char b, char c, char d) {
     return (uint32_t)(uint8_t)a | ((uint32_t)(uint8_t)b << 8) | ((uint32_t)(uint8_t)c << 16) | ((uint32_t)(uint8_t)d << 24);
 }
 
-// nv::getTargetExtent (src/nvtt/Surface.cpp:220-283) for the InputOptions' layout: the largest extent
-// scaled down to maxExtent (a power of two when rounding), a cube map's faces made square at the mean
-// of the scaled extents, then the round mode. False for a layout without a positive extent.
+// nv::getTargetExtent (src/nvtt/Surface.cpp:220-283) for the InputOptions' layout (a cube map's faces
+// square). False for a layout without a positive extent. A 3D layout takes the 2D extent here, and
+// process() then refuses it as unsupported.
 bool target_extent(const InputOptions::Private &io, int *w, int *h) {
-    if (io.width <= 0 || io.height <= 0) return false;
-    if (io.textureType != TextureType_Cube)
-        return ntg_target_extent(io.width, io.height, io.maxExtent, (int)io.roundMode, w, h) == NTG_OK;
-    int maxExtent = io.maxExtent;
-    if (io.roundMode != RoundMode_None && maxExtent > 0) {  // the power of two at or below it
-        int p = 1;
-        while (p <= maxExtent / 2) p *= 2;
-        maxExtent = p;
-    }
-    int sw = io.width, sh = io.height;
-    const int m = std::max(sw, sh);
-    if (maxExtent > 0 && m > maxExtent) { sw = std::max(sw * maxExtent / m, 1); sh = std::max(sh * maxExtent / m, 1); }
-    const int side = (sw + sh) / 2;
-    return ntg_target_extent(side, side, 0, (int)io.roundMode, w, h) == NTG_OK;
+    const int type = io.textureType == TextureType_3D ? (int)TextureType_2D : (int)io.textureType;
+    return ntg_target_extent_ex(io.width, io.height, io.maxExtent, (int)io.roundMode, type, w, h) == NTG_OK;
 }
 
 // `type` is TextureType_2D, _Cube or _Array; `arraySize` the image count of an array (1 otherwise).

@@ -90,6 +90,7 @@ def lib():
         "ntg_mip_level": (_i, [_vp, _vp, _i, _i, _vp, _i, _f, _vp, _i, _i, _i, _vp]),
         "ntg_resize": (_i, [_vp, _vp, _i, _i, _vp, _i, _i, _i, _f, _vp, _i, _i, _vp]),
         "ntg_target_extent": (_i, [_i, _i, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+        "ntg_target_extent_ex": (_i, [_i, _i, _i, _i, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
         "ntg_selftest_srgb_quantizer": (_i, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "ntg_mip_set_wait_limit": (_i, [_vp, _i]),
         "ntg_mip_status": (_i, [_vp, ctypes.POINTER(ctypes.c_int)]),
@@ -161,10 +162,10 @@ def _stream_ptr(stream=None):
     return ctypes.c_void_p(s.cuda_stream)
 
 
-def target_extent(w: int, h: int, max_extent: int, round_mode: int):
-    """nv::getTargetExtent for a 2D texture (ntg_target_extent)."""
+def target_extent(w: int, h: int, max_extent: int, round_mode: int, texture_type: int = 0):
+    """nv::getTargetExtent (ntg_target_extent_ex): texture_type 0 2D, 1 cube map (square faces), 3 array."""
     ow, oh = _i(), _i()
-    _check(lib().ntg_target_extent(w, h, max_extent, round_mode, ctypes.byref(ow), ctypes.byref(oh)))
+    _check(lib().ntg_target_extent_ex(w, h, max_extent, round_mode, texture_type, ctypes.byref(ow), ctypes.byref(oh)))
     return ow.value, oh.value
 
 

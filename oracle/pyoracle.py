@@ -318,6 +318,7 @@ class Reference:
         self._dxt5a_quick = _bind(lib, "ref_dxt5a_quick", None, [_vp, _vp])
         self._surface_resize = _bind(lib, "ref_surface_resize", None, [_vp, _i, _i, _i, _i, _i, _f, _f, _f, _i, _i, _vp])
         self._target_extent = _bind(lib, "ref_target_extent", None, [_i, _i, _i, _i, _vp, _vp])
+        self._target_extent_type = _bind(lib, "ref_target_extent_type", None, [_i, _i, _i, _i, _i, _vp, _vp])
         self._dxt5a_optimal = _bind(lib, "ref_dxt5a_optimal", None, [_vp, _vp])
         self._dxt1_single = _bind(lib, "ref_dxt1_single_color", None, [_i, _i, _i, _vp])
         self._quick_dxt1 = _bind(lib, "ref_quick_dxt1", None, [_vp, _vp])
@@ -347,9 +348,13 @@ class Reference:
         self._surface_resize(_ptr(r), w, h, dw, dh, filt, width, p0, p1, wrap, alpha_mode, _ptr(out))
         return out
 
-    def target_extent(self, w, h, max_extent, round_mode):
+    def target_extent(self, w, h, max_extent, round_mode, texture_type=None):
+        """nv::getTargetExtent; texture_type (nvtt::TextureType) None keeps the 2D entry point."""
         ow, oh = _i(), _i()
-        self._target_extent(w, h, max_extent, round_mode, ctypes.byref(ow), ctypes.byref(oh))
+        if texture_type is None:
+            self._target_extent(w, h, max_extent, round_mode, ctypes.byref(ow), ctypes.byref(oh))
+        else:
+            self._target_extent_type(w, h, max_extent, round_mode, texture_type, ctypes.byref(ow), ctypes.byref(oh))
         return ow.value, oh.value
 
     def compress(self, rgba, w, h, fmt, quality=1, alpha_mode=0, cw=(1, 1, 1, 1)):

@@ -309,6 +309,14 @@ void ref_target_extent(int w, int h, int max_extent, int round_mode, int * out_w
     *out_h = h;
 }
 
+// The same for a texture type (TextureType_2D, _Cube or _Array).
+void ref_target_extent_type(int w, int h, int max_extent, int round_mode, int type, int * out_w, int * out_h) {
+    int d = 1;
+    nv::getTargetExtent(&w, &h, &d, max_extent, (RoundMode)round_mode, (TextureType)type);
+    *out_w = w;
+    *out_h = h;
+}
+
 // Decode blocks with Surface::setImage2D (src/nvtt/Surface.cpp:908) into planar FP32.
 int ref_decode(int format, const unsigned char * blocks, int w, int h, float * out) {
     Surface s;

@@ -187,7 +187,7 @@ def test_images_vs_reference(oracle, reference, fmt, quality, alpha_mode):
 
 def test_target_extent_vs_reference(oracle, reference):
     """nv::getTargetExtent for every round mode, with and without a maximum extent (the library's
-    own ntg_target_extent is held to the same values)."""
+    own ntg_target_extent is held to the same values, and ntg_target_extent_ex for cube maps and arrays)."""
     import ntg
     for w in list(range(1, 40)) + [63, 64, 65, 100, 127, 1000, 4095]:
         for h in (1, 2, 3, 7, 64, 300):
@@ -196,6 +196,8 @@ def test_target_extent_vs_reference(oracle, reference):
                     ref = reference.target_extent(w, h, me, rm)
                     assert oracle.target_extent(w, h, me, rm) == ref
                     assert ntg.target_extent(w, h, me, rm) == ref
+                    for tt in (1, 3):  # cube map (square faces), array
+                        assert ntg.target_extent(w, h, me, rm, tt) == reference.target_extent(w, h, me, rm, tt)
 
 
 @pytest.mark.parametrize("alpha_mode", [0, 1])
