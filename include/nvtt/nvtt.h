@@ -1,14 +1,15 @@
 // nvtt.h -- drop-in C++ API of the GB300 texture path.
 //
 // The subset of NVTT 2.1.2's public API (src/nvtt/nvtt.h:52-444, 472-605 of the reference) that the
-// mip-chain + BC1/BC3/BC5 path needs, with the same class names, method names, argument meaning,
-// enum values and error behaviour (bool results plus ErrorHandler::error), implemented on the
-// sm_103a kernels behind include/ntg.h. Surfaces keep their pixels in GPU memory; Surface::data()
-// and channel() mirror them to the host on demand.
+// mip-chain + BC1/BC1a/BC3/BC4/BC5 path needs, with the same class names, method names, argument
+// meaning, enum values and error behaviour (bool results plus ErrorHandler::error), implemented on
+// the sm_103a kernels behind include/ntg.h. Surfaces keep their pixels in GPU memory; Surface::data()
+// and channel() mirror them to the host on demand. Compressor::process takes 2D textures, cube maps
+// and texture arrays, with the InputOptions resize step (max extent, round mode).
 //
 // What is outside the path reports Error_UnsupportedFeature (or returns false) instead of silently
-// doing something else: formats other than BC1/BC3/BC5, cube/3D/array textures, normal-map
-// generation and renormalisation of normal-map mipmaps, resizing of the input, dithering, KTX.
+// doing something else: other formats, BC1a at Fastest quality, 3D textures, normal-map generation
+// and renormalisation of normal-map mipmaps, dithering, KTX.
 #ifndef NVTT_GB300_NVTT_H
 #define NVTT_GB300_NVTT_H
 
