@@ -1,6 +1,6 @@
 /* ntg.h -- C ABI of the GB300 (sm_103a) texture hot path.
  *
- * Drop-in boundary for NVTT 2.1.2's mip-chain + BC1/BC3/BC5 path. Plain C types only: device
+ * Drop-in boundary for NVTT 2.1.2's mip-chain + BC1/BC1a/BC3/BC4/BC5 path. Plain C types only: device
  * pointers are caller-owned CUDA allocations, host pointers are plain memory, every call takes an
  * explicit CUDA stream (cudaStream_t passed as void *; NULL = the legacy default stream) and
  * returns an int status:

@@ -2,7 +2,8 @@
  * library's GPU path: opaque handles for the option objects and the compressor, the same function
  * names, argument meaning and enum values, so that a C program (or a language binding over a C FFI)
  * written against NVTT's C interface recompiles against this header unchanged as long as it stays on
- * the path (BC1/BC1a/BC3/BC4/BC5, Box/Triangle/Kaiser mipmaps, 2D textures). Requests outside the path
+ * the path (BC1/BC1a/BC3/BC4/BC5, Box/Triangle/Kaiser mipmaps, 2D textures, cube maps and texture
+ * arrays). Requests outside the path
  * fail the way the C++ interface reports them: nvttCompress returns NVTT_False and the error callback
  * receives NVTT_Error_UnsupportedFeature (or NVTT_Error_UnsupportedOutputFormat). Implemented in
  * nvidia-texture-tools_gb300/csrc/nvtt_wrapper.cpp over include/nvtt/nvtt.h; links with libntg.so. */
